@@ -1,0 +1,525 @@
+// gx_api.cu -- the extern "C" boundary of libgalaxcu.so (declared in
+// include/galax_gb300.h).  Host-side orchestration only; all compute is in the
+// kernels of gx_tree.cu, gx_lists.cu, gx_fmm.cu and gx_kdk.cu.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "gx_internal.cuh"
+
+int gx_tree_balance(gx_ctx *ctx, int64_t n_max, const double bounds[4]);
+
+int gx_fail(gx_ctx *ctx, int code, const std::string &msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int gx_cuda_check(gx_ctx *ctx, cudaError_t e, const char *what) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+    int code = GX_ERR_CUDA;
+    if (e == cudaErrorMemoryAllocation) code = GX_ERR_ALLOC;
+    if (e == cudaErrorNoKernelImageForDevice || e == cudaErrorInvalidKernelImage) code = GX_ERR_KERNEL_LOAD;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) code = GX_ERR_INIT;
+    return gx_fail(ctx, code, buf);
+}
+
+int gx_ensure(gx_ctx *ctx, DevBuf &b, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (b.bytes >= bytes) return GX_OK;
+    if (b.p) {
+        cudaStreamSynchronize(ctx->stream);  // nothing queued may still use the old block
+        cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    size_t nb = bytes + bytes / 8;
+    cudaError_t e = cudaMalloc(&b.p, nb);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        char msg[128];
+        snprintf(msg, sizeof msg, "device allocation of %zu bytes failed", nb);
+        return gx_fail(ctx, GX_ERR_ALLOC, msg);
+    }
+    b.bytes = nb;
+    return GX_OK;
+}
+
+static void free_buf(DevBuf &b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+static int check_ctx(gx_ctx *ctx) { return ctx ? GX_OK : GX_ERR_INVALID_ARG; }
+
+static int sync_status(gx_ctx *ctx, unsigned *out) {
+    GX_CUDA(ctx, cudaMemcpyAsync(out, ctx->status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
+extern "C" {
+
+int gx_abi_version(void) { return GX_ABI_VERSION; }
+
+int gx_config_default(gx_config *cfg) {
+    if (!cfg) return GX_ERR_INVALID_ARG;
+    cfg->max_n = 262144;
+    cfg->max_nodes = 524288;
+    cfg->max_interactions = 1u << 24;
+    cfg->p = 4;
+    cfg->eps = 0.1f;
+    cfg->eps64 = 0.0;
+    cfg->device = 0;
+    return GX_OK;
+}
+
+const char *gx_last_error(const gx_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int gx_create(const gx_config *cfg, gx_ctx **out) {
+    if (!cfg || !out) return GX_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (cfg->p > GX_MAXP) return GX_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return GX_ERR_INIT;
+    }
+    if (cfg->device < 0 || cfg->device >= ndev) return GX_ERR_INVALID_ARG;
+    if (cudaSetDevice(cfg->device) != cudaSuccess) return GX_ERR_INIT;
+    gx_ctx *ctx = new gx_ctx();
+    ctx->cfg = *cfg;
+    ctx->device = cfg->device;
+    ctx->p = (int)cfg->p;
+    ctx->eps = cfg->eps64 > 0.0 ? cfg->eps64 : (double)cfg->eps;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, cfg->device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return GX_ERR_INIT;
+    }
+    for (auto &e : ctx->ev) cudaEventCreate(&e);
+    // kernel-image check: the status allocation and a memset are the first device work
+    int s = gx_ensure(ctx, ctx->status, 64);
+    if (s != GX_OK) {
+        gx_destroy(ctx);
+        return s;
+    }
+    cudaMemsetAsync(ctx->status.p, 0, 64, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        gx_destroy(ctx);
+        return GX_ERR_INIT;
+    }
+    *out = ctx;
+    return GX_OK;
+}
+
+int gx_destroy(gx_ctx *ctx) {
+    if (!ctx) return GX_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    DevBuf *bufs[] = {&ctx->cx, &ctx->cy, &ctx->hw, &ctx->mass, &ctx->comx, &ctx->comy, &ctx->bs, &ctx->be,
+                      &ctx->child, &ctx->parent, &ctx->is_leaf, &ctx->keys, &ctx->x, &ctx->y, &ctx->vx, &ctx->vy,
+                      &ctx->m, &ctx->ax, &ctx->ay, &ctx->vdata, &ctx->vlen, &ctx->udata, &ctx->ulen, &ctx->p2p_off,
+                      &ctx->p2p_idx, &ctx->ref_voff, &ctx->ref_did, &ctx->ref_G, &ctx->radius, &ctx->far_off, &ctx->far_idx,
+                      &ctx->near_off, &ctx->near_idx, &ctx->M, &ctx->L, &ctx->Lf, &ctx->Mf32, &ctx->Lf32,
+                      &ctx->Lff32, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
+                      &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush};
+    for (DevBuf *b : bufs) free_buf(*b);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GX_OK;
+}
+
+int gx_set_mode(gx_ctx *ctx, int mode, int precision, double theta) {
+    GX_TRY(check_ctx(ctx));
+    if (mode < GX_MODE_REF || mode > GX_MODE_ACCURATE) return gx_fail(ctx, GX_ERR_INVALID_ARG, "unknown mode");
+    if (precision != GX_PREC_FP64 && precision != GX_PREC_MIXED) return gx_fail(ctx, GX_ERR_INVALID_ARG, "unknown precision");
+    if (mode == GX_MODE_ACCURATE && !(theta > 0.0 && theta < 2.0))
+        return gx_fail(ctx, GX_ERR_INVALID_ARG, "theta must be in (0, 2)");
+    ctx->mode = mode;
+    ctx->prec = precision;
+    if (mode == GX_MODE_ACCURATE && theta != ctx->theta) ctx->plan_acc_valid = false;
+    if (mode == GX_MODE_ACCURATE) ctx->theta = theta;
+    return GX_OK;
+}
+
+int gx_set_params(gx_ctx *ctx, uint32_t p, double eps) {
+    GX_TRY(check_ctx(ctx));
+    if (p > GX_MAXP) return gx_fail(ctx, GX_ERR_INVALID_ARG, "p must be in 0..16");
+    if (!(eps >= 0.0) || !isfinite(eps)) return gx_fail(ctx, GX_ERR_INVALID_ARG, "eps must be finite and >= 0");
+    if ((int)p != ctx->p || eps != ctx->eps) ctx->plan_ref_valid = false;
+    ctx->p = (int)p;
+    ctx->eps = eps;
+    return GX_OK;
+}
+
+// Copies the given host arrays to the resident bodies.  A NULL array is zeroed when
+// zero_missing is set; otherwise its resident contents are kept (zeroed only if the
+// buffer had to be allocated).
+static int upload_bodies_impl(gx_ctx *ctx, int64_t n, const double *x, const double *y, const double *vx,
+                              const double *vy, const double *m, const double *ax, const double *ay,
+                              bool zero_missing = true) {
+    if (n < 0) return gx_fail(ctx, GX_ERR_INVALID_ARG, "n < 0");
+    if (ctx->cfg.max_n && (uint64_t)n > ctx->cfg.max_n) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "n exceeds max_n");
+    size_t bytes = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    DevBuf *dst[7] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->m, &ctx->ax, &ctx->ay};
+    const double *src[7] = {x, y, vx, vy, m, ax, ay};
+    bool same_n = ctx->have_bodies && ctx->n_bodies == n;
+    for (int k = 0; k < 7; k++) {
+        void *before = dst[k]->p;
+        GX_TRY(gx_ensure(ctx, *dst[k], bytes));
+        if (n == 0) continue;
+        if (!src[k] && !zero_missing && same_n && before == dst[k]->p) continue;
+        if (src[k]) {
+            GX_CUDA(ctx, cudaMemcpyAsync(dst[k]->p, src[k], sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        } else {
+            GX_CUDA(ctx, cudaMemsetAsync(dst[k]->p, 0, sizeof(double) * n, ctx->stream));
+        }
+    }
+    ctx->have_bodies = true;
+    return GX_OK;
+}
+
+int gx_upload_bodies(gx_ctx *ctx, int64_t n, const double *x, const double *y, const double *vx, const double *vy,
+                     const double *m, const double *ax, const double *ay) {
+    GX_TRY(check_ctx(ctx));
+    if (!x || !y || !m) return gx_fail(ctx, GX_ERR_INVALID_ARG, "x, y and m are required");
+    if (ctx->have_tree && n != ctx->n_bodies) return gx_fail(ctx, GX_ERR_INVALID_ARG, "n differs from the tree's body count");
+    GX_TRY(upload_bodies_impl(ctx, n, x, y, vx, vy, m, ax, ay));
+    ctx->n_bodies = n;
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
+int gx_download_bodies(gx_ctx *ctx, double *x, double *y, double *vx, double *vy, double *m, double *ax, double *ay) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no resident bodies");
+    int64_t n = ctx->n_bodies;
+    DevBuf *srcb[7] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->m, &ctx->ax, &ctx->ay};
+    double *dst[7] = {x, y, vx, vy, m, ax, ay};
+    for (int k = 0; k < 7; k++)
+        if (dst[k] && n > 0)
+            GX_CUDA(ctx, cudaMemcpyAsync(dst[k], srcb[k]->p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
+int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, double *vy, double *m, double *ax,
+                  double *ay, int64_t n_max, const double bounds[4], int flags) {
+    GX_TRY(check_ctx(ctx));
+    if (n < 0 || n_max <= 0 || !bounds) return gx_fail(ctx, GX_ERR_INVALID_ARG, "bad n, n_max or bounds");
+    if (n > 0 && (!x || !y || !m)) return gx_fail(ctx, GX_ERR_INVALID_ARG, "x, y and m are required");
+    ctx->have_tree = false;
+    ctx->plan_ref_valid = ctx->plan_acc_valid = false;
+    GX_TRY(upload_bodies_impl(ctx, n, x, y, vx, vy, m, ax, ay));
+    ctx->n_bodies = n;
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
+    if (flags & GX_BUILD_BALANCED) {
+        if (n == 0) {
+            GX_TRY(gx_tree_build_device(ctx, 0, n_max, bounds, 0));
+        } else {
+            GX_TRY(gx_tree_balance(ctx, n_max, bounds));
+        }
+    } else {
+        GX_TRY(gx_tree_build_device(ctx, n, n_max, bounds, 0));
+    }
+    if (ctx->cfg.max_nodes && (uint64_t)ctx->n_nodes > ctx->cfg.max_nodes)
+        return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "tree node count exceeds max_nodes");
+    GX_TRY(gx_lists_build_ref(ctx));
+    // Tree::build permutes the caller's arrays (lib.rs:204); so do we.
+    if (!(flags & GX_BUILD_BALANCED)) GX_TRY(gx_download_bodies(ctx, x, y, vx, vy, m, ax, ay));
+    ctx->have_tree = true;
+    return GX_OK;
+}
+
+int gx_upload_tree(gx_ctx *ctx, int64_t n_nodes, int64_t n_bodies, const double *cx, const double *cy,
+                   const double *hw, const double *mass, const double *comx, const double *comy,
+                   const int64_t *body_start, const int64_t *body_end, const int32_t *child, const int32_t *parent,
+                   const uint8_t *is_leaf, const uint32_t *vlist_data, const uint8_t *vlist_len,
+                   const uint32_t *ulist_data, const uint8_t *ulist_len) {
+    GX_TRY(check_ctx(ctx));
+    if (n_nodes < 0 || n_bodies < 0 || n_bodies >= 0x7fffffffLL || n_nodes >= 0x7fffffffLL)
+        return gx_fail(ctx, GX_ERR_INVALID_ARG, "bad sizes");
+    if (n_nodes > 0 && (!cx || !cy || !hw || !mass || !comx || !comy || !body_start || !body_end || !child || !parent ||
+                        !is_leaf || !vlist_data || !vlist_len || !ulist_data || !ulist_len))
+        return gx_fail(ctx, GX_ERR_INVALID_ARG, "null tree array");
+    if (ctx->cfg.max_nodes && (uint64_t)n_nodes > ctx->cfg.max_nodes)
+        return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "n_nodes exceeds max_nodes");
+    ctx->have_tree = false;
+    ctx->plan_ref_valid = ctx->plan_acc_valid = false;
+    // levels = height (compute_levels, lib.rs:426-438); Tree::build appends each
+    // round contiguously, which the device passes rely on.
+    std::vector<int32_t> lev((size_t)n_nodes);
+    std::vector<int32_t> bs32((size_t)n_nodes), be32((size_t)n_nodes);
+    int32_t maxlev = 0;
+    int64_t nl = 0;
+    for (int64_t i = 0; i < n_nodes; i++) {
+        int32_t l = 0;
+        for (int k = 0; k < 4; k++) {
+            int32_t c = child[4 * i + k];
+            if (c >= 0) {
+                if (c >= i) return gx_fail(ctx, GX_ERR_INVALID_ARG, "child id must precede its parent");
+                l = std::max(l, lev[c] + 1);
+            }
+        }
+        lev[i] = l;
+        maxlev = std::max(maxlev, l);
+        if (is_leaf[i]) {
+            if (l != 0) return gx_fail(ctx, GX_ERR_INVALID_ARG, "leaf with children");
+            nl++;
+        }
+        if (body_start[i] < 0 || body_end[i] > n_bodies || body_start[i] > body_end[i])
+            return gx_fail(ctx, GX_ERR_INVALID_ARG, "body range out of bounds");
+        bs32[i] = (int32_t)body_start[i];
+        be32[i] = (int32_t)body_end[i];
+    }
+    std::vector<int64_t> ls;
+    ls.push_back(0);
+    for (int64_t i = 0; i < n_nodes; i++) {
+        if (i > 0 && lev[i] < lev[i - 1]) return gx_fail(ctx, GX_ERR_INVALID_ARG, "levels are not contiguous");
+        if (i > 0 && lev[i] != lev[i - 1]) ls.push_back(i);
+    }
+    ls.push_back(n_nodes);
+    for (int64_t i = 0; i < nl; i++)
+        if (!is_leaf[i]) return gx_fail(ctx, GX_ERR_INVALID_ARG, "leaves must come first");
+    struct F { DevBuf *b; const void *src; size_t sz; };
+    F f[] = {{&ctx->cx, cx, 8}, {&ctx->cy, cy, 8}, {&ctx->hw, hw, 8}, {&ctx->mass, mass, 8},
+             {&ctx->comx, comx, 8}, {&ctx->comy, comy, 8}, {&ctx->bs, bs32.data(), 4}, {&ctx->be, be32.data(), 4},
+             {&ctx->child, child, 16}, {&ctx->parent, parent, 4}, {&ctx->is_leaf, is_leaf, 1},
+             {&ctx->vlen, vlist_len, 1}, {&ctx->ulen, ulist_len, 1},
+             {&ctx->vdata, vlist_data, 4 * GX_LIST_CAP}, {&ctx->udata, ulist_data, 4 * GX_LIST_CAP}};
+    for (auto &e : f) {
+        GX_TRY(gx_ensure(ctx, *e.b, e.sz * (size_t)(n_nodes > 0 ? n_nodes : 1)));
+        if (n_nodes > 0)
+            GX_CUDA(ctx, cudaMemcpyAsync(e.b->p, e.src, e.sz * (size_t)n_nodes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->n_nodes = n_nodes;
+    ctx->n_leaves = nl;
+    ctx->n_levels = n_nodes > 0 ? maxlev + 1 : 0;
+    ctx->level_start = n_nodes > 0 ? ls : std::vector<int64_t>(1, 0);
+    if (ctx->have_bodies && ctx->n_bodies != n_bodies) ctx->have_bodies = false;
+    ctx->n_bodies = n_bodies;
+    ctx->have_tree = true;
+    return GX_OK;
+}
+
+int gx_tree_info(gx_ctx *ctx, int64_t *n_nodes, int64_t *n_leaves, int32_t *n_levels, int64_t *n_bodies) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree");
+    if (n_nodes) *n_nodes = ctx->n_nodes;
+    if (n_leaves) *n_leaves = ctx->n_leaves;
+    if (n_levels) *n_levels = ctx->n_levels;
+    if (n_bodies) *n_bodies = ctx->n_bodies;
+    return GX_OK;
+}
+
+int gx_export_tree(gx_ctx *ctx, double *cx, double *cy, double *hw, double *mass, double *comx, double *comy,
+                   int64_t *body_start, int64_t *body_end, int32_t *child, int32_t *parent, uint8_t *is_leaf,
+                   int64_t *level_start) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree");
+    size_t nn = (size_t)ctx->n_nodes;
+    if (nn > 0) {
+        struct F { DevBuf *b; void *dst; size_t sz; };
+        F f[] = {{&ctx->cx, cx, 8}, {&ctx->cy, cy, 8}, {&ctx->hw, hw, 8}, {&ctx->mass, mass, 8},
+                 {&ctx->comx, comx, 8}, {&ctx->comy, comy, 8}, {&ctx->child, child, 16}, {&ctx->parent, parent, 4},
+                 {&ctx->is_leaf, is_leaf, 1}};
+        for (auto &e : f)
+            if (e.dst) GX_CUDA(ctx, cudaMemcpyAsync(e.dst, e.b->p, e.sz * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        std::vector<int32_t> b32(nn), e32(nn);
+        GX_CUDA(ctx, cudaMemcpyAsync(b32.data(), ctx->bs.p, 4 * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(e32.data(), ctx->be.p, 4 * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (size_t i = 0; i < nn; i++) {
+            if (body_start) body_start[i] = b32[i];
+            if (body_end) body_end[i] = e32[i];
+        }
+    }
+    if (level_start)
+        for (size_t i = 0; i < ctx->level_start.size(); i++) level_start[i] = ctx->level_start[i];
+    return GX_OK;
+}
+
+int gx_export_lists(gx_ctx *ctx, int which, uint32_t *data, uint8_t *lengths) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree");
+    if (which != GX_LIST_V && which != GX_LIST_U) return gx_fail(ctx, GX_ERR_INVALID_ARG, "unknown list");
+    DevBuf &d = which == GX_LIST_V ? ctx->vdata : ctx->udata;
+    DevBuf &l = which == GX_LIST_V ? ctx->vlen : ctx->ulen;
+    size_t nn = (size_t)ctx->n_nodes;
+    if (nn == 0) return GX_OK;
+    if (data) GX_CUDA(ctx, cudaMemcpyAsync(data, d.p, 4 * GX_LIST_CAP * nn, cudaMemcpyDeviceToHost, ctx->stream));
+    if (lengths) GX_CUDA(ctx, cudaMemcpyAsync(lengths, l.p, nn, cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
+static int ensure_plan(gx_ctx *ctx) {
+    if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree: call gx_build_tree or gx_upload_tree first");
+    if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no bodies");
+    if (ctx->mode == GX_MODE_ACCURATE) {
+        if (!ctx->plan_acc_valid || ctx->plan_theta != ctx->theta) GX_TRY(gx_plan_accurate(ctx));
+    } else {
+        if (!ctx->plan_ref_valid || ctx->plan_p != ctx->p || ctx->plan_eps != ctx->eps) GX_TRY(gx_plan_ref(ctx));
+    }
+    return GX_OK;
+}
+
+int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64_t *n_p2p_interactions) {
+    GX_TRY(check_ctx(ctx));
+    GX_TRY(ensure_plan(ctx));
+    if (ctx->mode == GX_MODE_ACCURATE) {
+        if (n_far_pairs) *n_far_pairs = ctx->n_far_pairs;
+        if (n_near_pairs) *n_near_pairs = ctx->n_near_pairs;
+    } else {
+        if (n_far_pairs) *n_far_pairs = ctx->n_v_pairs;
+        if (n_near_pairs) *n_near_pairs = ctx->n_p2p_pairs;
+    }
+    if (n_p2p_interactions) {
+        // sum over target leaves of (targets x sources), from the host copy of the lists
+        int64_t nl = ctx->n_leaves, nn = ctx->n_nodes;
+        std::vector<int32_t> bs((size_t)nn), be((size_t)nn);
+        GX_CUDA(ctx, cudaMemcpyAsync(bs.data(), ctx->bs.p, 4 * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(be.data(), ctx->be.p, 4 * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        std::vector<int64_t> st((size_t)nl + 1);
+        std::vector<int32_t> cnt((size_t)nl);
+        int64_t tot_idx;
+        const int32_t *idxp;
+        if (ctx->mode == GX_MODE_ACCURATE) {
+            GX_CUDA(ctx, cudaMemcpyAsync(st.data(), ctx->near_off.p, 8 * nl, cudaMemcpyDeviceToHost, ctx->stream));
+            GX_CUDA(ctx, cudaMemcpyAsync(cnt.data(), static_cast<char *>(ctx->near_off.p) + 8 * nn, 4 * nl,
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+            idxp = dptr<int32_t>(ctx->near_idx);
+            GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            tot_idx = 0;
+            for (int64_t a = 0; a < nl; a++) tot_idx = std::max(tot_idx, st[a] + cnt[a]);
+        } else {
+            GX_CUDA(ctx, cudaMemcpyAsync(st.data(), ctx->p2p_off.p, 8 * (nl + 1), cudaMemcpyDeviceToHost, ctx->stream));
+            GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            for (int64_t a = 0; a < nl; a++) cnt[a] = (int32_t)(st[a + 1] - st[a]);
+            idxp = dptr<int32_t>(ctx->p2p_idx);
+            tot_idx = st[nl];
+        }
+        std::vector<int32_t> idx((size_t)tot_idx + 1);
+        if (tot_idx > 0)
+            GX_CUDA(ctx, cudaMemcpyAsync(idx.data(), idxp, 4 * tot_idx, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int64_t inter = 0;
+        for (int64_t a = 0; a < nl; a++) {
+            int64_t nt = be[a] - bs[a], ns = 0;
+            for (int64_t q = st[a]; q < st[a] + cnt[a]; q++) ns += be[idx[q]] - bs[idx[q]];
+            inter += nt * ns - nt;  // minus self pairs
+        }
+        *n_p2p_interactions = inter;
+    }
+    return GX_OK;
+}
+
+static int forces_and_check(gx_ctx *ctx, bool timed) {
+    GX_TRY(ensure_plan(ctx));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
+    GX_TRY(gx_forces_device(ctx, timed));
+    unsigned st = 0;
+    GX_TRY(sync_status(ctx, &st));
+    if (timed && ctx->n_nodes > 0) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[6]);
+        ctx->last_ms[0] = ms;
+        for (int k = 0; k < 6; k++) {
+            cudaEventElapsedTime(&ms, ctx->ev[k], ctx->ev[k + 1]);
+            ctx->last_ms[k + 1] = ms;
+        }
+    }
+    return GX_OK;
+}
+
+int gx_compute_forces(gx_ctx *ctx, const double *x, const double *y, const double *m, double *ax, double *ay) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree: call gx_build_tree or gx_upload_tree first");
+    if (!x || !y || !m || !ax || !ay) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null array");
+    int64_t n = ctx->n_bodies;
+    GX_TRY(upload_bodies_impl(ctx, n, x, y, nullptr, nullptr, m, nullptr, nullptr, false));
+    GX_TRY(forces_and_check(ctx, true));
+    if (n > 0) {
+        GX_CUDA(ctx, cudaMemcpyAsync(ax, ctx->ax.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(ay, ctx->ay.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
+int gx_forces_resident(gx_ctx *ctx) {
+    GX_TRY(check_ctx(ctx));
+    return forces_and_check(ctx, true);
+}
+
+int gx_kdk_run(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag) {
+    GX_TRY(check_ctx(ctx));
+    if (n_steps < 0) return gx_fail(ctx, GX_ERR_INVALID_ARG, "n_steps < 0");
+    GX_TRY(ensure_plan(ctx));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
+    GX_TRY(gx_kdk_device(ctx, n_steps, dt, energy_every, diag, n_diag));
+    return GX_OK;
+}
+
+int gx_diagnostics(gx_ctx *ctx, double out[5]) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no resident bodies");
+    if (!out) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null output");
+    return gx_diag_device(ctx, out);
+}
+
+int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, double *ay) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no resident bodies");
+    if (n_idx < 0 || (n_idx > 0 && (!idx || !ax || !ay))) return gx_fail(ctx, GX_ERR_INVALID_ARG, "bad sample arrays");
+    return gx_n2_device(ctx, idx, n_idx, ax, ay);
+}
+
+int gx_last_timings(gx_ctx *ctx, double out[7]) {
+    GX_TRY(check_ctx(ctx));
+    for (int k = 0; k < 7; k++) out[k] = ctx->last_ms[k];
+    return GX_OK;
+}
+
+int gx_last_launch_count(gx_ctx *ctx, int64_t *count) {
+    GX_TRY(check_ctx(ctx));
+    *count = ctx->last_launches;
+    return GX_OK;
+}
+
+int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each, int32_t which,
+                    double *kernel_ms_each) {
+    GX_TRY(check_ctx(ctx));
+    if (reps <= 0) return gx_fail(ctx, GX_ERR_INVALID_ARG, "reps <= 0");
+    GX_TRY(ensure_plan(ctx));
+    size_t flush_bytes = (size_t)256 << 20;  // twice the 129 MB L2
+    if (flush_l2) GX_TRY(gx_ensure(ctx, ctx->flush, flush_bytes));
+    for (int r = 0; r < reps; r++) {
+        if (flush_l2) GX_CUDA(ctx, cudaMemsetAsync(ctx->flush.p, r & 0xff, flush_bytes, ctx->stream));
+        GX_TRY(forces_and_check(ctx, true));
+        if (ms_each) ms_each[r] = ctx->last_ms[0];
+        if (kernel_ms_each) kernel_ms_each[r] = which == 1 ? ctx->last_ms[4] : ctx->last_ms[6];
+    }
+    return GX_OK;
+}
+
+void *gx_host_alloc(size_t bytes) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 16) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void gx_host_free(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,148 @@
+// gx_internal.cuh -- shared declarations of libgalaxcu (GB300 / sm_103a FMM backend).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/galax_gb300.h"
+
+#define GX_MAXP 16
+#define GX_LIST_CAP 64
+#define GX_WARP 32
+
+// ---------------------------------------------------------------- device buffers
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+// Host-side error helper: records the message in the context and returns the code.
+struct gx_ctx;
+int gx_fail(gx_ctx *ctx, int code, const std::string &msg);
+int gx_cuda_check(gx_ctx *ctx, cudaError_t e, const char *what);
+
+#define GX_CUDA(ctx, call)                                             \
+    do {                                                               \
+        cudaError_t _e = (call);                                       \
+        if (_e != cudaSuccess) return gx_cuda_check((ctx), _e, #call); \
+    } while (0)
+#define GX_TRY(call)                  \
+    do {                              \
+        int _s = (call);              \
+        if (_s != GX_OK) return _s;   \
+    } while (0)
+
+// Grow-only device allocation; contents are not preserved on growth.
+int gx_ensure(gx_ctx *ctx, DevBuf &b, size_t bytes);
+template <class T>
+inline T *dptr(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
+
+// Device status word bits (read back at pass boundaries).
+enum : unsigned {
+    GX_DEV_NONFINITE_INPUT = 1u,
+    GX_DEV_LIST_OVERFLOW = 2u,
+    GX_DEV_STACK_OVERFLOW = 4u,
+};
+
+// ---------------------------------------------------------------- the context
+struct gx_ctx {
+    gx_config cfg{};
+    int device = 0;
+    int p = 4;
+    double eps = 0.1;
+    int mode = GX_MODE_REF;
+    int prec = GX_PREC_FP64;
+    double theta = 0.5;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int sm_count = 0;
+
+    // tree (device, SoA); node ids are int32, body indices int32
+    int64_t n_nodes = 0, n_bodies = 0, n_leaves = 0;
+    int32_t n_levels = 0;
+    std::vector<int64_t> level_start;  // n_levels + 1
+    bool have_tree = false;
+    DevBuf cx, cy, hw, mass, comx, comy, bs, be, child, parent, is_leaf;
+    DevBuf keys;  // Morton keys of the bodies in tree order (device build only)
+
+    // bodies (device, tree order)
+    DevBuf x, y, vx, vy, m, ax, ay;
+    bool have_bodies = false;
+
+    // REF lists, reference layout
+    DevBuf vdata, vlen, udata, ulen;
+
+    // plans (static per tree, mode, p, eps)
+    bool plan_ref_valid = false, plan_acc_valid = false;
+    double plan_eps = -1.0, plan_theta = -1.0;
+    int plan_p = -1;
+    DevBuf p2p_off, p2p_idx;         // REF gather lists: per leaf, the source leaves
+    int64_t n_p2p_pairs = 0;
+    DevBuf ref_voff;                 // per node: offset of its V pairs (REF pair order)
+    DevBuf ref_did;                  // per V pair: derivative-set id
+    DevBuf ref_G;                    // n_keys x (2p+1)^2 doubles
+    int64_t n_ref_keys = 0, n_v_pairs = 0;
+    DevBuf radius;                   // accurate mode node radii
+    DevBuf far_off, far_idx, near_off, near_idx;
+    int64_t n_far_pairs = 0, n_near_pairs = 0, n_p2p_inter = 0;
+
+    // expansions
+    DevBuf M, L, Lf;
+    DevBuf Mf32, Lf32, Lff32;
+
+    // scratch
+    DevBuf scratch_a, scratch_b, scratch_c, scratch_d, scratch_e, scratch_f, scratch_g;
+    DevBuf status;     // unsigned, device status word
+    DevBuf red;        // reduction scratch (doubles)
+    DevBuf flush;      // L2 flush buffer for timing
+
+    // timing
+    cudaEvent_t ev[16] = {};
+    double last_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+    int64_t last_launches = 0;
+    int64_t launches = 0;
+};
+
+// ---------------------------------------------------------------- sub-modules
+// gx_tree.cu
+int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bounds[4], int flags);
+// gx_lists.cu
+int gx_lists_build_ref(gx_ctx *ctx);
+int gx_plan_ref(gx_ctx *ctx);
+int gx_plan_accurate(gx_ctx *ctx);
+// gx_fmm.cu
+int gx_forces_device(gx_ctx *ctx, bool timed);
+int gx_poly_table_host(int p, double eps, std::vector<double> &out);
+// gx_scan.cu
+int gx_exclusive_scan_i64(gx_ctx *ctx, const int64_t *in, int64_t *out, int64_t n);
+int gx_exclusive_scan_i32(gx_ctx *ctx, const int32_t *in, int32_t *out, int64_t n, int32_t *total_host);
+int gx_radix_sort_u64(gx_ctx *ctx, uint64_t *keys, uint32_t *vals, int64_t n, int begin_bit, int end_bit,
+                      uint64_t *keys_alt, uint32_t *vals_alt, bool *result_in_alt);
+// gx_kdk.cu
+int gx_kdk_device(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag);
+int gx_diag_device(gx_ctx *ctx, double out[5]);
+int gx_n2_device(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, double *ay);
+
+// grid helpers
+inline unsigned gx_blocks(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// ---------------------------------------------------------------- device helpers
+#ifdef __CUDACC__
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__host__ __device__ constexpr int gx_nc(int p) { return (p + 1) * (p + 2) / 2; }
+__host__ __device__ constexpr int gx_mi(int i, int j) { return (i + j) * (i + j + 1) / 2 + j; }
+__host__ __device__ constexpr int gx_kdi(int k, int l, int p) { return (k + l) * (2 * p + 1) + l; }
+#endif

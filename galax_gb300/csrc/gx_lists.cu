@@ -1,0 +1,898 @@
+// gx_lists.cu -- device interaction lists and static per-tree plans.
+//
+//  * V-list: InteractionLists::build (galax-core/src/lib.rs:947-1025)
+//  * U-list: build_p2p_lists (lib.rs:1358-1392)
+//  * build_constrained's neighbour search (neighbors_geometric, lib.rs:382-423)
+//  * REF P2P gather lists: p2p (lib.rs:1395-1462) updates both sides of a leaf
+//    pair when the partner id is higher and skips lower partners, so leaf a
+//    receives from b != a iff (b > a and b in U(a)) or (b < a and a in U(b)).
+//  * REF M2L derivative plan: m2l's cache (lib.rs:1209-1247) keyed on
+//    (dx as i64, dy as i64) where the first pair in (target id, slot) order wins.
+//  * ACCURATE mode near/far lists (not in the reference).
+//
+// The reference scans every node of a level for every query.  Here each query
+// walks a bounding-volume hierarchy built over the level's nodes in id order
+// (buckets of 8 consecutive ids), visiting buckets left to right, so candidates
+// come out in ascending id order; the reference's own floating-point test is
+// then applied to each candidate, so the lists are identical.  Boxes are widened
+// by a margin that covers every rounding of the exact test.  Levels that hold a
+// node with a non-finite box fall back to scanning the level in id order.
+#include <climits>
+
+#include <algorithm>
+#include <set>
+
+#include "gx_internal.cuh"
+
+int gx_tree_rebuild_with_splits(gx_ctx *ctx, int64_t n_max, const double bounds[4], const std::vector<int64_t> &splits);
+int gx_add_offsets(gx_ctx *ctx, const int64_t *o, int64_t *dst, int64_t c, int64_t add);
+
+namespace {
+
+constexpr int BVH_B = 8;
+
+struct Level {
+    int64_t s, e, p2;
+    double4 *box;
+    bool brute;
+    double maxabs;
+    double4 *cbox;  // optional: per BVH node, bounding box of the children's centres
+    double *cmh;    //           and the minimum child half-width (-inf if any child is non-finite)
+    double cmax;
+};
+
+__device__ __forceinline__ bool finite3(double a, double b, double c) {
+    return isfinite(a) && isfinite(b) && isfinite(c);
+}
+
+__device__ __forceinline__ void atomic_max_pos(double *addr, double v) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long *>(addr), (unsigned long long)__double_as_longlong(v));
+}
+
+__global__ void k_bvh_leaves(int64_t s, int64_t cnt, int64_t p2, const double *cx, const double *cy, const double *hw,
+                             double4 *box, unsigned *nonfinite, double *maxabs) {
+    int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= p2) return;
+    double4 bx = make_double4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+    double ma = 0.0;
+    unsigned nf = 0;
+    for (int64_t k = b * BVH_B; k < b * BVH_B + BVH_B && k < cnt; k++) {
+        int64_t id = s + k;
+        double c_x = cx[id], c_y = cy[id], h = hw[id];
+        if (!finite3(c_x, c_y, h)) { nf++; continue; }
+        bx.x = fmin(bx.x, c_x - h); bx.y = fmax(bx.y, c_x + h);
+        bx.z = fmin(bx.z, c_y - h); bx.w = fmax(bx.w, c_y + h);
+        ma = fmax(ma, fabs(c_x) + fabs(c_y) + fabs(h));
+    }
+    box[p2 + b] = bx;
+    if (nf) atomicAdd(nonfinite, nf);
+    if (ma > 0.0) atomic_max_pos(maxabs, ma);
+}
+
+__global__ void k_bvh_up(int64_t lo, int64_t hi, double4 *box) {
+    int64_t h = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= hi) return;
+    double4 a = box[2 * h], b = box[2 * h + 1];
+    box[h] = make_double4(fmin(a.x, b.x), fmax(a.y, b.y), fmin(a.z, b.z), fmax(a.w, b.w));
+}
+
+// Calls f(id) for every node of the level whose box may overlap the query box,
+// in ascending id order.  Returns false if the traversal stack overflowed.
+template <class F>
+__device__ bool level_query(const Level &L, const double *cx, const double *cy, const double *hw, double qx0,
+                            double qx1, double qy0, double qy1, bool qfinite, F &&f) {
+    if (L.brute || !qfinite) {
+        for (int64_t id = L.s; id < L.e; id++) f(id);
+        return true;
+    }
+    int64_t stack[64];
+    int sp = 0;
+    stack[sp++] = 1;
+    while (sp > 0) {
+        int64_t h = stack[--sp];
+        double4 b = L.box[h];
+        if (b.x > qx1 || b.y < qx0 || b.z > qy1 || b.w < qy0) continue;
+        if (h >= L.p2) {
+            int64_t k0 = (h - L.p2) * BVH_B;
+            for (int64_t k = k0; k < k0 + BVH_B && L.s + k < L.e; k++) {
+                int64_t id = L.s + k;
+                double c_x = cx[id], c_y = cy[id], hh = hw[id];
+                if (c_x - hh > qx1 || c_x + hh < qx0 || c_y - hh > qy1 || c_y + hh < qy0) continue;
+                f(id);
+            }
+        } else {
+            if (sp + 2 > 64) return false;
+            stack[sp++] = 2 * h + 1;
+            stack[sp++] = 2 * h;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ double margin(const Level &L, double qabs) { return 1e-15 + 1e-12 * (L.maxabs + qabs + 1.0); }
+
+// V-list parent test (lib.rs:990-995): pn skipped iff dx > h_sum + 1e-15 || dy > h_sum + 1e-15
+__device__ __forceinline__ bool vparent_near(const double *cx, const double *cy, const double *hw, int64_t P, int64_t pn) {
+    double dx = fabs(__dsub_rn(cx[pn], cx[P])), dy = fabs(__dsub_rn(cy[pn], cy[P]));
+    double hs = __dadd_rn(hw[P], hw[pn]);
+    double lim = __dadd_rn(hs, 1e-15);
+    return !(dx > lim || dy > lim);
+}
+
+// V-list child adjacency (lib.rs:1000-1006)
+__device__ __forceinline__ bool vchild_adjacent(const double *cx, const double *cy, const double *hw, int64_t n, int64_t c) {
+    double cdx = fabs(__dsub_rn(cx[c], cx[n])), cdy = fabs(__dsub_rn(cy[c], cy[n]));
+    double lim = __dadd_rn(__dadd_rn(hw[n], hw[c]), 1e-15);
+    return (cdx <= lim) && (cdy <= lim);
+}
+
+// U-list touch (lib.rs:1380-1384)
+__device__ __forceinline__ bool utouch(const double *cx, const double *cy, const double *hw, int64_t a, int64_t b) {
+    double dx = fabs(__dsub_rn(cx[a], cx[b])), dy = fabs(__dsub_rn(cy[a], cy[b]));
+    double lim = __dadd_rn(__dadd_rn(hw[a], hw[b]), 1e-15);
+    return dx <= lim && dy <= lim;
+}
+
+__device__ __forceinline__ void qbox(const double *cx, const double *cy, const double *hw, int64_t q, const Level &L,
+                                     double &x0, double &x1, double &y0, double &y1, bool &fin) {
+    double c_x = cx[q], c_y = cy[q], h = hw[q];
+    fin = finite3(c_x, c_y, h);
+    double mg = margin(L, fabs(c_x) + fabs(c_y) + fabs(h));
+    x0 = c_x - h - mg; x1 = c_x + h + mg; y0 = c_y - h - mg; y1 = c_y + h + mg;
+}
+
+__global__ void k_cenv_leaves(int64_t s, int64_t cnt, int64_t p2, const int4 *child, const double *cx,
+                              const double *cy, const double *hw, double4 *cbox, double *cmh, double *cmax) {
+    int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= p2) return;
+    double4 bx = make_double4(INFINITY, -INFINITY, INFINITY, -INFINITY);
+    double mh = INFINITY, ma = 0.0;
+    for (int64_t k = b * BVH_B; k < b * BVH_B + BVH_B && k < cnt; k++) {
+        int4 c4 = child[s + k];
+        int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+        for (int q = 0; q < 4; q++) {
+            int c = cc[q];
+            if (c < 0) continue;
+            double c_x = cx[c], c_y = cy[c], h = hw[c];
+            if (!finite3(c_x, c_y, h)) { mh = -INFINITY; continue; }
+            bx.x = fmin(bx.x, c_x); bx.y = fmax(bx.y, c_x);
+            bx.z = fmin(bx.z, c_y); bx.w = fmax(bx.w, c_y);
+            mh = fmin(mh, h);
+            ma = fmax(ma, fabs(c_x) + fabs(c_y) + h);
+        }
+    }
+    cbox[p2 + b] = bx;
+    cmh[p2 + b] = mh;
+    if (ma > 0.0) atomic_max_pos(cmax, ma);
+}
+
+__global__ void k_cenv_up(int64_t lo, int64_t hi, double4 *cbox, double *cmh) {
+    int64_t h = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= hi) return;
+    double4 a = cbox[2 * h], b = cbox[2 * h + 1];
+    cbox[h] = make_double4(fmin(a.x, b.x), fmax(a.y, b.y), fmin(a.z, b.z), fmax(a.w, b.w));
+    cmh[h] = fmin(cmh[2 * h], cmh[2 * h + 1]);
+}
+
+// V-list of every node of level lv, one thread per node: walks the parent level's
+// hierarchy in ascending id order, pruning subtrees with no parent near P and
+// subtrees whose every child is certainly adjacent to the node; stops at the cap.
+__global__ void k_vlist_node(int64_t s0, int64_t e0, Level pl, const int32_t *parent, const int4 *child,
+                             const double *cx, const double *cy, const double *hw, uint32_t *vdata, uint8_t *vlen,
+                             unsigned *status) {
+    int64_t n = s0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= e0) return;
+    int32_t P = parent[n];
+    int len = 0;
+    auto visit = [&](int64_t pn) {
+        if (pn == P || !vparent_near(cx, cy, hw, P, pn)) return;
+        int4 c4 = child[pn];
+        int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+        for (int k = 0; k < 4; k++) {
+            int c = cc[k];
+            if (c < 0 || vchild_adjacent(cx, cy, hw, n, c)) continue;
+            if (len < GX_LIST_CAP) vdata[n * GX_LIST_CAP + len++] = (uint32_t)c;
+        }
+    };
+    if (P >= 0) {
+        if (pl.brute) {
+            for (int64_t pn = pl.s; pn < pl.e && len < GX_LIST_CAP; pn++) visit(pn);
+        } else {
+            double pcx = cx[P], pcy = cy[P], phw = hw[P];
+            bool pfin = finite3(pcx, pcy, phw);
+            double mg = margin(pl, fabs(pcx) + fabs(pcy) + fabs(phw));
+            double qx0 = pcx - phw - mg, qx1 = pcx + phw + mg, qy0 = pcy - phw - mg, qy1 = pcy + phw + mg;
+            double ncx = cx[n], ncy = cy[n], nhw = hw[n];
+            double dl = 1e-12 * (fabs(ncx) + fabs(ncy) + fabs(nhw) + pl.cmax + 1.0);
+            int64_t stack[64];
+            int sp = 0;
+            stack[sp++] = 1;
+            while (sp > 0 && len < GX_LIST_CAP) {
+                int64_t h = stack[--sp];
+                double4 b = pl.box[h];
+                if (pfin && (b.x > qx1 || b.y < qx0 || b.z > qy1 || b.w < qy0)) continue;
+                double4 cbx = pl.cbox[h];
+                double wx = fmax(fabs(cbx.x - ncx), fabs(cbx.y - ncx));
+                double wy = fmax(fabs(cbx.z - ncy), fabs(cbx.w - ncy));
+                double lim = nhw + pl.cmh[h] - dl;
+                if (wx <= lim && wy <= lim) continue;  // every child adjacent to n
+                if (h >= pl.p2) {
+                    int64_t i0 = pl.s + (h - pl.p2) * BVH_B;
+                    for (int64_t pn = i0; pn < i0 + BVH_B && pn < pl.e && len < GX_LIST_CAP; pn++) visit(pn);
+                } else {
+                    if (sp + 2 > 64) { atomicOr(status, GX_DEV_STACK_OVERFLOW); break; }
+                    stack[sp++] = 2 * h + 1;
+                    stack[sp++] = 2 * h;
+                }
+            }
+        }
+    }
+    vlen[n] = (uint8_t)len;
+}
+
+__global__ void k_ulist(Level lv0, const double *cx, const double *cy, const double *hw, uint32_t *udata, uint8_t *ulen,
+                        unsigned *status) {
+    int64_t a = lv0.s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= lv0.e) return;
+    int len = 0;
+    udata[a * GX_LIST_CAP + len++] = (uint32_t)a;
+    double x0, x1, y0, y1;
+    bool fin;
+    qbox(cx, cy, hw, a, lv0, x0, x1, y0, y1, fin);
+    bool ok = level_query(lv0, cx, cy, hw, x0, x1, y0, y1, fin, [&](int64_t b) {
+        if (b == a || len >= GX_LIST_CAP) return;
+        if (utouch(cx, cy, hw, a, b)) udata[a * GX_LIST_CAP + len++] = (uint32_t)b;
+    });
+    if (!ok) atomicOr(status, GX_DEV_STACK_OVERFLOW);
+    ulen[a] = (uint8_t)len;
+}
+
+// REF P2P gather lists: per receiving leaf a, {a} then ascending b with
+// (b > a and b in U(a)) or (b < a and a in U(b)).
+__global__ void k_p2p_gather(Level lv0, const double *cx, const double *cy, const double *hw, const uint32_t *udata,
+                             const uint8_t *ulen, int pass, int32_t *cnt, const int64_t *off, int32_t *out,
+                             unsigned *status) {
+    int64_t a = lv0.s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= lv0.e) return;
+    int64_t base = pass ? off[a] : 0;
+    int32_t c = 0;
+    if (pass) out[base] = (int32_t)a;
+    c = 1;
+    int ua = ulen[a];
+    double x0, x1, y0, y1;
+    bool fin;
+    qbox(cx, cy, hw, a, lv0, x0, x1, y0, y1, fin);
+    bool ok = level_query(lv0, cx, cy, hw, x0, x1, y0, y1, fin, [&](int64_t b) {
+        if (b == a) return;
+        bool take = false;
+        if (b > a) {
+            for (int k = 1; k < ua; k++)
+                if (udata[a * GX_LIST_CAP + k] == (uint32_t)b) { take = true; break; }
+        } else {
+            int ub = ulen[b];
+            for (int k = 1; k < ub; k++)
+                if (udata[b * GX_LIST_CAP + k] == (uint32_t)a) { take = true; break; }
+        }
+        if (take) {
+            if (pass) out[base + c] = (int32_t)b;
+            c++;
+        }
+    });
+    if (!ok) atomicOr(status, GX_DEV_STACK_OVERFLOW);
+    if (!pass) cnt[a] = c;
+}
+
+// Rust `f64 as i64`
+__device__ __forceinline__ long long f64_as_i64(double v) {
+    if (v != v) return 0;
+    if (v >= 9223372036854775808.0) return LLONG_MAX;
+    if (v < -9223372036854775808.0) return LLONG_MIN;
+    return __double2ll_rz(v);
+}
+
+__global__ void k_ref_pair_keys(int64_t nn, const uint32_t *vdata, const uint8_t *vlen, const int64_t *voff,
+                                const double *comx, const double *comy, uint64_t *klo, uint64_t *khi, uint32_t *pidx,
+                                double *pdx, double *pdy) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t n = t / GX_LIST_CAP;
+    int s = (int)(t % GX_LIST_CAP);
+    if (n >= nn || s >= vlen[n]) return;
+    uint32_t src = vdata[n * GX_LIST_CAP + s];
+    double dx = __dsub_rn(comx[n], comx[src]), dy = __dsub_rn(comy[n], comy[src]);
+    int64_t pi = voff[n] + s;
+    klo[pi] = (uint64_t)f64_as_i64(dx);
+    khi[pi] = (uint64_t)f64_as_i64(dy);
+    pidx[pi] = (uint32_t)pi;
+    pdx[pi] = dx;
+    pdy[pi] = dy;
+}
+
+__global__ void k_gather_u64(const uint32_t *idx, const uint64_t *in, uint64_t *out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[idx[i]];
+}
+
+__global__ void k_run_heads(const uint64_t *a, const uint64_t *b, int64_t n, int32_t *head) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    head[i] = (i == 0) ? 1 : (a[i] != a[i - 1] || b[i] != b[i - 1]);
+}
+
+__global__ void k_run_assign(const int32_t *head, const int32_t *hex, const uint32_t *pidx, int64_t n, int32_t *did,
+                             int32_t *first_pair) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int32_t k = hex[i] + head[i] - 1;
+    did[pidx[i]] = k;
+    if (head[i]) first_pair[k] = (int32_t)pidx[i];
+}
+
+// x^a by binary exponentiation: the expansion LLVM uses for f64::powi
+__device__ __forceinline__ double powi_dev(double x, int a) {
+    double r = 1.0;
+    for (;;) {
+        if (a & 1) r = __dmul_rn(r, x);
+        a >>= 1;
+        if (a == 0) break;
+        x = __dmul_rn(x, x);
+    }
+    return r;
+}
+
+// compute_kernel_derivs (lib.rs:1040-1151) evaluated from the polynomial table
+// (built on the host by the same recurrence): G^(k,l) = sum N_kl[a][b] x^a y^b / R^(1+2k+2l).
+__global__ void k_ref_derivs(int64_t nk, const int32_t *first_pair, const double *pdx, const double *pdy,
+                             const double *poly, int p, double eps, double *G) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    int S = 2 * p + 1;
+    double x = pdx[first_pair[k]], y = pdy[first_pair[k]];
+    double eps2 = __dmul_rn(eps, eps);
+    double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), eps2);
+    double r = __dsqrt_rn(r2);
+    double inv_r[2 + 4 * GX_MAXP + 2];
+    inv_r[1] = __ddiv_rn(1.0, r);
+    for (int n = 3; n <= 1 + 2 * (2 * p); n += 2) inv_r[n] = __ddiv_rn(inv_r[n - 2], r2);
+    double *g = G + k * (int64_t)S * S;
+    for (int i = 0; i < S * S; i++) g[i] = 0.0;
+    for (int kk = 0; kk < S; kk++)
+        for (int l = 0; l < S - kk; l++) {
+            const double *pl = poly + ((int64_t)kk * S + l) * S * S;
+            double val = 0.0;
+            for (int a = 0; a < S; a++)
+                for (int b = 0; b < S - a; b++) {
+                    double c = pl[a * S + b];
+                    if (c != 0.0) val = __dadd_rn(val, __dmul_rn(__dmul_rn(c, powi_dev(x, a)), powi_dev(y, b)));
+                }
+            g[(kk + l) * S + l] = __dmul_rn(val, inv_r[1 + 2 * kk + 2 * l]);
+        }
+}
+
+__global__ void k_u8_to_i64(const uint8_t *in, int64_t *out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i];
+}
+__global__ void k_i32_to_i64(const int32_t *in, int64_t *out, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i];
+}
+
+// ---------------------------------------------------------------- accurate mode
+// sqrt(dx*dx + dy*dy) with separately rounded operations: the same bits as the
+// oracle, so near/far decisions agree exactly.
+__device__ __forceinline__ double dist_rn(double dx, double dy) {
+    return __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+}
+
+__global__ void k_radius_leaves(int64_t nl, const double *x, const double *y, const double *comx, const double *comy,
+                                const int32_t *bs, const int32_t *be, double *R) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    double r = 0.0;
+    for (int32_t i = bs[L]; i < be[L]; i++) r = fmax(r, dist_rn(x[i] - comx[L], y[i] - comy[L]));
+    R[L] = r;
+}
+
+__global__ void k_radius_parents(int64_t s, int64_t e, const int4 *child, const double *comx, const double *comy,
+                                 double *R) {
+    int64_t q = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= e) return;
+    int4 c4 = child[q];
+    int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+    double r = 0.0;
+    for (int k = 0; k < 4; k++) {
+        int c = cc[k];
+        if (c < 0) continue;
+        r = fmax(r, __dadd_rn(dist_rn(comx[c] - comx[q], comy[c] - comy[q]), R[c]));
+    }
+    R[q] = r;
+}
+
+__device__ __forceinline__ bool mac_far(const double *comx, const double *comy, const double *R, int64_t a, int64_t b,
+                                        double theta) {
+    double d = dist_rn(comx[a] - comx[b], comy[a] - comy[b]);
+    return __dmul_rn(d, theta) > __dadd_rn(R[a], R[b]);
+}
+
+// Per node x of a level: children of Near(parent(x)) split into far (M2L) and near.
+__global__ void k_mac(int64_t s, int64_t e, int pass, const int32_t *parent, const int4 *child, const double *comx,
+                      const double *comy, const double *R, double theta, const int64_t *near_start,
+                      const int32_t *near_cnt, const int32_t *near_idx_in, int32_t *fcnt, int32_t *ncnt,
+                      const int64_t *fstart, const int64_t *nstart, int32_t *far_idx, int32_t *near_idx) {
+    int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= e) return;
+    int32_t P = parent[x];
+    int32_t nf = 0, nn = 0;
+    int64_t fb = pass ? fstart[x] : 0, nb = pass ? nstart[x] : 0;
+    if (P >= 0) {
+        int64_t q0 = near_start[P], q1 = q0 + near_cnt[P];
+        for (int64_t q = q0; q < q1; q++) {
+            int4 c4 = child[near_idx_in[q]];
+            int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+            for (int k = 0; k < 4; k++) {
+                int c = cc[k];
+                if (c < 0) continue;
+                if (mac_far(comx, comy, R, x, c, theta)) {
+                    if (pass) far_idx[fb + nf] = c;
+                    nf++;
+                } else {
+                    if (pass) near_idx[nb + nn] = c;
+                    nn++;
+                }
+            }
+        }
+    }
+    if (!pass) {
+        fcnt[x] = nf;
+        ncnt[x] = nn;
+    }
+}
+
+// ---------------------------------------------------------------- balanced build
+// neighbors_geometric (lib.rs:382-423) + the 2:1 test of build_constrained
+// (lib.rs:558-579): per leaf, the split point it asks for, or -1.
+struct LevelSet {
+    Level lv[64];
+    int n;
+};
+
+__device__ __forceinline__ bool cells_adjacent_dev(const double *cx, const double *cy, const double *hw, int64_t a,
+                                                   int64_t b) {
+    double ha = hw[a], hb = hw[b];
+    double mx = (ha != ha) ? hb : ((hb != hb) ? ha : (hb > ha ? hb : ha));
+    double mn = (ha != ha) ? hb : ((hb != hb) ? ha : (hb < ha ? hb : ha));
+    double ratio = __ddiv_rn(mx, mn);
+    if (ratio > 8.0) return false;
+    double dx = fabs(__dsub_rn(cx[a], cx[b])), dy = fabs(__dsub_rn(cy[a], cy[b]));
+    double lim = __dadd_rn(__dadd_rn(ha, hb), 1e-15);
+    return dx <= lim && dy <= lim;
+}
+
+__global__ void k_balance_splits(LevelSet ls, int64_t nl, const double *cx, const double *cy, const double *hw,
+                                 const int32_t *bs, const int32_t *be, int64_t *mid_out, unsigned *status) {
+    int64_t lid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (lid >= nl) return;
+    double c_x = cx[lid], c_y = cy[lid], h = hw[lid];
+    double d = __dmul_rn(h, 2.0);
+    double px[8] = {__dadd_rn(c_x, d), __dadd_rn(c_x, d), c_x, __dsub_rn(c_x, d),
+                    __dsub_rn(c_x, d), __dsub_rn(c_x, d), c_x, __dadd_rn(c_x, d)};
+    double py[8] = {c_y, __dadd_rn(c_y, d), __dadd_rn(c_y, d), __dadd_rn(c_y, d),
+                    c_y, __dsub_rn(c_y, d), __dsub_rn(c_y, d), __dsub_rn(c_y, d)};
+    int64_t mid = -1;
+    for (int k = 0; k < 8; k++) {
+        int64_t best = -1;
+        double bd = 1.7976931348623157e308;
+        double qa = fabs(px[k]) + fabs(py[k]);
+        bool qf = isfinite(px[k]) && isfinite(py[k]);
+        for (int L = 0; L < ls.n; L++) {
+            const Level &lv = ls.lv[L];
+            double mg = margin(lv, qa);
+            bool ok = level_query(lv, cx, cy, hw, px[k] - mg, px[k] + mg, py[k] - mg, py[k] + mg, qf, [&](int64_t o) {
+                if (o == lid) return;
+                double dx = fabs(__dsub_rn(px[k], cx[o])), dy = fabs(__dsub_rn(py[k], cy[o]));
+                double lim = __dadd_rn(hw[o], 1e-15);
+                if (!(dx <= lim && dy <= lim)) return;
+                if (!cells_adjacent_dev(cx, cy, hw, lid, o)) return;
+                double ex = __dsub_rn(px[k], cx[o]), ey = __dsub_rn(py[k], cy[o]);
+                double dist = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+                if (dist < bd) {  // candidates arrive in ascending id: ties keep the lowest id
+                    bd = dist;
+                    best = o;
+                }
+            });
+            if (!ok) atomicOr(status, GX_DEV_STACK_OVERFLOW);
+        }
+        if (best >= 0) {
+            double nhw = hw[best];
+            if (h > __dmul_rn(nhw, 2.1)) {
+                int64_t s = bs[lid], e = be[lid];
+                if (e - s > 2) mid = (s + e) / 2;
+                break;
+            }
+        }
+    }
+    mid_out[lid] = mid;
+}
+
+}  // namespace
+
+// Builds a BVH over nodes [s, e) into `storage` (grown as needed).
+static int build_level(gx_ctx *ctx, int64_t s, int64_t e, DevBuf &storage, size_t offset_bytes, Level &L,
+                       size_t *used_bytes) {
+    int64_t cnt = e - s;
+    int64_t nb = (cnt + BVH_B - 1) / BVH_B;
+    if (nb < 1) nb = 1;
+    int64_t p2 = 1;
+    while (p2 < nb) p2 *= 2;
+    size_t need = sizeof(double4) * (size_t)(2 * p2) + 64;
+    L.s = s; L.e = e; L.p2 = p2;
+    L.box = reinterpret_cast<double4 *>(static_cast<char *>(storage.p) + offset_bytes);
+    L.cbox = nullptr;
+    L.cmh = nullptr;
+    L.cmax = 0.0;
+    *used_bytes = need;
+    (void)need;
+    // status buffer: bytes [8,12) non-finite count, [16,24) max |c|+|hw|
+    unsigned *nf = reinterpret_cast<unsigned *>(static_cast<char *>(ctx->status.p) + 8);
+    double *ma = reinterpret_cast<double *>(static_cast<char *>(ctx->status.p) + 16);
+    GX_CUDA(ctx, cudaMemsetAsync(nf, 0, 16, ctx->stream));
+    k_bvh_leaves<<<gx_blocks(p2, 128), 128, 0, ctx->stream>>>(s, cnt, p2, dptr<double>(ctx->cx), dptr<double>(ctx->cy),
+                                                             dptr<double>(ctx->hw), L.box, nf, ma);
+    ctx->launches++;
+    for (int64_t lo = p2 / 2; lo >= 1; lo /= 2) {
+        k_bvh_up<<<gx_blocks(lo, 128), 128, 0, ctx->stream>>>(lo, 2 * lo, L.box);
+        ctx->launches++;
+    }
+    GX_CUDA(ctx, cudaGetLastError());
+    struct { unsigned nf; unsigned pad; double ma; } h{};
+    GX_CUDA(ctx, cudaMemcpyAsync(&h, nf, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    L.brute = h.nf > 0;
+    L.maxabs = h.ma;
+    return GX_OK;
+}
+
+static size_t bvh_bytes(int64_t cnt) {
+    int64_t nb = (cnt + BVH_B - 1) / BVH_B;
+    if (nb < 1) nb = 1;
+    int64_t p2 = 1;
+    while (p2 < nb) p2 *= 2;
+    return sizeof(double4) * (size_t)(2 * p2) + 256;
+}
+
+static int check_status(gx_ctx *ctx) {
+    unsigned st = 0;
+    GX_CUDA(ctx, cudaMemcpyAsync(&st, dptr<unsigned>(ctx->status), sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (st & GX_DEV_STACK_OVERFLOW) return gx_fail(ctx, GX_ERR_STATE, "list builder: traversal stack overflow");
+    return GX_OK;
+}
+
+// V-list and U-list in the reference layout.
+int gx_lists_build_ref(gx_ctx *ctx) {
+    int64_t nn = ctx->n_nodes;
+    GX_TRY(gx_ensure(ctx, ctx->vdata, sizeof(uint32_t) * GX_LIST_CAP * (size_t)(nn > 0 ? nn : 1)));
+    GX_TRY(gx_ensure(ctx, ctx->udata, sizeof(uint32_t) * GX_LIST_CAP * (size_t)(nn > 0 ? nn : 1)));
+    GX_TRY(gx_ensure(ctx, ctx->vlen, (size_t)(nn > 0 ? nn : 1)));
+    GX_TRY(gx_ensure(ctx, ctx->ulen, (size_t)(nn > 0 ? nn : 1)));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->vdata.p, 0xFF, sizeof(uint32_t) * GX_LIST_CAP * (size_t)nn, ctx->stream));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->udata.p, 0xFF, sizeof(uint32_t) * GX_LIST_CAP * (size_t)nn, ctx->stream));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->vlen.p, 0, (size_t)nn, ctx->stream));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->ulen.p, 0, (size_t)nn, ctx->stream));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
+    if (nn == 0) return GX_OK;
+    const double *cx = dptr<double>(ctx->cx), *cy = dptr<double>(ctx->cy), *hw = dptr<double>(ctx->hw);
+    // V-list, level by level
+    for (int lv = 0; lv + 1 < ctx->n_levels; lv++) {
+        int64_t s0 = ctx->level_start[lv], e0 = ctx->level_start[lv + 1];
+        int64_t s1 = ctx->level_start[lv + 1], e1 = ctx->level_start[lv + 2];
+        int64_t np = e1 - s1;
+        size_t bb = bvh_bytes(np);
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, 2 * bb + bb / 4 + 256));
+        Level L;
+        size_t used = 0;
+        GX_TRY(build_level(ctx, s1, e1, ctx->scratch_a, 0, L, &used));
+        L.cbox = reinterpret_cast<double4 *>(static_cast<char *>(ctx->scratch_a.p) + bb);
+        L.cmh = reinterpret_cast<double *>(static_cast<char *>(ctx->scratch_a.p) + 2 * bb);
+        double *cmax = reinterpret_cast<double *>(static_cast<char *>(ctx->status.p) + 24);
+        GX_CUDA(ctx, cudaMemsetAsync(cmax, 0, sizeof(double), ctx->stream));
+        k_cenv_leaves<<<gx_blocks(L.p2, 128), 128, 0, ctx->stream>>>(s1, np, L.p2, dptr<int4>(ctx->child), cx, cy, hw,
+                                                                     L.cbox, L.cmh, cmax);
+        ctx->launches++;
+        for (int64_t lo = L.p2 / 2; lo >= 1; lo /= 2) {
+            k_cenv_up<<<gx_blocks(lo, 128), 128, 0, ctx->stream>>>(lo, 2 * lo, L.cbox, L.cmh);
+            ctx->launches++;
+        }
+        GX_CUDA(ctx, cudaMemcpyAsync(&L.cmax, cmax, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        k_vlist_node<<<gx_blocks(e0 - s0, 64), 64, 0, ctx->stream>>>(s0, e0, L, dptr<int32_t>(ctx->parent),
+                                                                    dptr<int4>(ctx->child), cx, cy, hw,
+                                                                    dptr<uint32_t>(ctx->vdata), dptr<uint8_t>(ctx->vlen),
+                                                                    dptr<unsigned>(ctx->status));
+        ctx->launches++;
+        GX_CUDA(ctx, cudaGetLastError());
+    }
+    // U-list over the leaves
+    {
+        int64_t nl = ctx->level_start[1];
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, bvh_bytes(nl)));
+        Level L;
+        size_t used = 0;
+        GX_TRY(build_level(ctx, 0, nl, ctx->scratch_a, 0, L, &used));
+        k_ulist<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(L, cx, cy, hw, dptr<uint32_t>(ctx->udata),
+                                                            dptr<uint8_t>(ctx->ulen), dptr<unsigned>(ctx->status));
+        ctx->launches++;
+        GX_CUDA(ctx, cudaGetLastError());
+    }
+    return check_status(ctx);
+}
+
+// REF plan: P2P gather lists and the derivative-set id of every V pair.
+int gx_plan_ref(gx_ctx *ctx) {
+    int64_t nn = ctx->n_nodes;
+    ctx->plan_ref_valid = false;
+    if (nn == 0) { ctx->plan_ref_valid = true; return GX_OK; }
+    const double *cx = dptr<double>(ctx->cx), *cy = dptr<double>(ctx->cy), *hw = dptr<double>(ctx->hw);
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
+    // ---- P2P gather lists
+    int64_t nl = ctx->level_start[1];
+    GX_TRY(gx_ensure(ctx, ctx->scratch_a, bvh_bytes(nl)));
+    Level L0;
+    size_t used = 0;
+    GX_TRY(build_level(ctx, 0, nl, ctx->scratch_a, 0, L0, &used));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int32_t) * (size_t)(nl + 1)));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nl + 1)));
+    GX_TRY(gx_ensure(ctx, ctx->p2p_off, sizeof(int64_t) * (size_t)(nl + 1)));
+    int32_t *cnt = dptr<int32_t>(ctx->scratch_b);
+    int64_t *cnt64 = dptr<int64_t>(ctx->scratch_c);
+    int64_t *off = dptr<int64_t>(ctx->p2p_off);
+    k_p2p_gather<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(L0, cx, cy, hw, dptr<uint32_t>(ctx->udata),
+                                                             dptr<uint8_t>(ctx->ulen), 0, cnt, nullptr, nullptr,
+                                                             dptr<unsigned>(ctx->status));
+    GX_CUDA(ctx, cudaMemsetAsync(cnt64 + nl, 0, sizeof(int64_t), ctx->stream));
+    k_i32_to_i64<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(cnt, cnt64, nl);
+    GX_TRY(gx_exclusive_scan_i64(ctx, cnt64, off, nl + 1));
+    int64_t tot = 0;
+    GX_CUDA(ctx, cudaMemcpyAsync(&tot, off + nl, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    GX_TRY(gx_ensure(ctx, ctx->p2p_idx, sizeof(int32_t) * (size_t)(tot + 1)));
+    k_p2p_gather<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(L0, cx, cy, hw, dptr<uint32_t>(ctx->udata),
+                                                             dptr<uint8_t>(ctx->ulen), 1, cnt, off,
+                                                             dptr<int32_t>(ctx->p2p_idx), dptr<unsigned>(ctx->status));
+    ctx->launches += 3;
+    ctx->n_p2p_pairs = tot;
+    GX_CUDA(ctx, cudaGetLastError());
+
+    // ---- REF derivative plan
+    GX_TRY(gx_ensure(ctx, ctx->ref_voff, sizeof(int64_t) * (size_t)(nn + 1)));  // V pair offsets per node
+    int64_t *voff = dptr<int64_t>(ctx->ref_voff);
+    GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nn + 1)));
+    int64_t *len64 = dptr<int64_t>(ctx->scratch_c);
+    GX_CUDA(ctx, cudaMemsetAsync(len64 + nn, 0, sizeof(int64_t), ctx->stream));
+    k_u8_to_i64<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(dptr<uint8_t>(ctx->vlen), len64, nn);
+    GX_TRY(gx_exclusive_scan_i64(ctx, len64, voff, nn + 1));
+    int64_t np = 0;
+    GX_CUDA(ctx, cudaMemcpyAsync(&np, voff + nn, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->n_v_pairs = np;
+    GX_TRY(gx_ensure(ctx, ctx->ref_did, sizeof(int32_t) * (size_t)(np + 1)));
+    if (np > 0) {
+        // scratch_a: klo, khi, k_alt (3 x u64); scratch_b: pidx, pidx_alt (2 x u32) + heads;
+        // scratch_d: pdx, pdy
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(uint64_t) * (size_t)np * 4));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(uint32_t) * (size_t)np * 2 + sizeof(int32_t) * (size_t)np * 2 + 64));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_d, sizeof(double) * (size_t)np * 2));
+        uint64_t *klo = dptr<uint64_t>(ctx->scratch_a), *khi = klo + np, *ka = khi + np, *kb = ka + np;
+        uint32_t *pidx = dptr<uint32_t>(ctx->scratch_b), *palt = pidx + np;
+        int32_t *head = reinterpret_cast<int32_t *>(palt + np), *hex = head + np;
+        double *pdx = dptr<double>(ctx->scratch_d), *pdy = pdx + np;
+        k_ref_pair_keys<<<gx_blocks(nn * GX_LIST_CAP, 256), 256, 0, ctx->stream>>>(
+            nn, dptr<uint32_t>(ctx->vdata), dptr<uint8_t>(ctx->vlen), voff, dptr<double>(ctx->comx),
+            dptr<double>(ctx->comy), klo, khi, pidx, pdx, pdy);
+        ctx->launches++;
+        // stable sort by lo, then by hi -> order (hi, lo, pair index)
+        GX_CUDA(ctx, cudaMemcpyAsync(ka, klo, sizeof(uint64_t) * np, cudaMemcpyDeviceToDevice, ctx->stream));
+        bool alt = false;
+        GX_TRY(gx_radix_sort_u64(ctx, ka, pidx, np, 0, 64, kb, palt, &alt));
+        uint32_t *p1 = alt ? palt : pidx;
+        uint32_t *p1o = alt ? pidx : palt;
+        k_gather_u64<<<gx_blocks(np, 256), 256, 0, ctx->stream>>>(p1, khi, ka, np);
+        GX_TRY(gx_radix_sort_u64(ctx, ka, p1, np, 0, 64, kb, p1o, &alt));
+        uint64_t *hs = alt ? kb : ka;
+        uint32_t *p2 = alt ? p1o : p1;
+        uint64_t *ls = alt ? ka : kb;
+        k_gather_u64<<<gx_blocks(np, 256), 256, 0, ctx->stream>>>(p2, klo, ls, np);
+        k_run_heads<<<gx_blocks(np, 256), 256, 0, ctx->stream>>>(hs, ls, np, head);
+        int32_t nk = 0;
+        GX_TRY(gx_exclusive_scan_i32(ctx, head, hex, np, &nk));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int32_t) * (size_t)(nk + 1)));
+        int32_t *first = dptr<int32_t>(ctx->scratch_c);
+        k_run_assign<<<gx_blocks(np, 256), 256, 0, ctx->stream>>>(head, hex, p2, np, dptr<int32_t>(ctx->ref_did), first);
+        ctx->launches += 4;
+        // polynomial table (host, by the reference's recurrence) and the derivative sets
+        std::vector<double> poly;
+        GX_TRY(gx_poly_table_host(ctx->p, ctx->eps, poly));
+        int S = 2 * ctx->p + 1;
+        GX_TRY(gx_ensure(ctx, ctx->scratch_e, sizeof(double) * poly.size()));
+        GX_CUDA(ctx, cudaMemcpyAsync(ctx->scratch_e.p, poly.data(), sizeof(double) * poly.size(), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+        GX_TRY(gx_ensure(ctx, ctx->ref_G, sizeof(double) * (size_t)nk * S * S));
+        k_ref_derivs<<<gx_blocks(nk, 64), 64, 0, ctx->stream>>>(nk, first, pdx, pdy, dptr<double>(ctx->scratch_e),
+                                                               ctx->p, ctx->eps, dptr<double>(ctx->ref_G));
+        ctx->launches++;
+        GX_CUDA(ctx, cudaGetLastError());
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        ctx->n_ref_keys = nk;
+    }
+    GX_TRY(check_status(ctx));
+    ctx->plan_ref_valid = true;
+    ctx->plan_p = ctx->p;
+    ctx->plan_eps = ctx->eps;
+    return GX_OK;
+}
+
+// ACCURATE plan: node radii from the resident bodies, then near/far lists top-down.
+int gx_plan_accurate(gx_ctx *ctx) {
+    int64_t nn = ctx->n_nodes;
+    ctx->plan_acc_valid = false;
+    if (nn == 0) { ctx->plan_acc_valid = true; return GX_OK; }
+    if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "accurate plan needs resident bodies");
+    GX_TRY(gx_ensure(ctx, ctx->radius, sizeof(double) * (size_t)nn));
+    double *R = dptr<double>(ctx->radius);
+    int64_t nl = ctx->level_start[1];
+    k_radius_leaves<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(nl, dptr<double>(ctx->x), dptr<double>(ctx->y),
+                                                                dptr<double>(ctx->comx), dptr<double>(ctx->comy),
+                                                                dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), R);
+    ctx->launches++;
+    for (int lv = 1; lv < ctx->n_levels; lv++) {
+        int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
+        k_radius_parents<<<gx_blocks(e - s, 128), 128, 0, ctx->stream>>>(s, e, dptr<int4>(ctx->child),
+                                                                        dptr<double>(ctx->comx), dptr<double>(ctx->comy), R);
+        ctx->launches++;
+    }
+    // per-node start/count for far and near lists
+    GX_TRY(gx_ensure(ctx, ctx->far_off, sizeof(int64_t) * (size_t)nn + sizeof(int32_t) * (size_t)nn + 64));
+    GX_TRY(gx_ensure(ctx, ctx->near_off, sizeof(int64_t) * (size_t)nn + sizeof(int32_t) * (size_t)nn + 64));
+    int64_t *fstart = dptr<int64_t>(ctx->far_off);
+    int32_t *fcnt = reinterpret_cast<int32_t *>(fstart + nn);
+    int64_t *nstart = dptr<int64_t>(ctx->near_off);
+    int32_t *ncnt = reinterpret_cast<int32_t *>(nstart + nn);
+    GX_CUDA(ctx, cudaMemsetAsync(fcnt, 0, sizeof(int32_t) * (size_t)nn, ctx->stream));
+    GX_CUDA(ctx, cudaMemsetAsync(ncnt, 0, sizeof(int32_t) * (size_t)nn, ctx->stream));
+    int64_t root = nn - 1;
+    // root: near itself
+    std::vector<int64_t> hstart(1, 0);
+    int32_t one = 1;
+    int32_t root32 = (int32_t)root;
+    int64_t far_tot = 0, near_tot = 1;
+    size_t near_cap = 1 << 20, far_cap = 1 << 20;
+    GX_TRY(gx_ensure(ctx, ctx->near_idx, sizeof(int32_t) * near_cap));
+    GX_TRY(gx_ensure(ctx, ctx->far_idx, sizeof(int32_t) * far_cap));
+    near_cap = ctx->near_idx.bytes / sizeof(int32_t);
+    far_cap = ctx->far_idx.bytes / sizeof(int32_t);
+    int64_t zero = 0;
+    GX_CUDA(ctx, cudaMemcpyAsync(nstart + root, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(nn + 1) * 2));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int64_t) * (size_t)(nn + 1) * 2));
+    for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
+        int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
+        k_mac<<<gx_blocks(c, 128), 128, 0, ctx->stream>>>(s, e, 0, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
+                                                          dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta,
+                                                          nstart, ncnt, dptr<int32_t>(ctx->near_idx), fcnt, ncnt,
+                                                          nullptr, nullptr, nullptr, nullptr);
+        // offsets of this level: exclusive scans of the counts, shifted by the running totals
+        int64_t *fc64 = dptr<int64_t>(ctx->scratch_a), *nc64 = fc64 + (c + 1);
+        int64_t *fo = dptr<int64_t>(ctx->scratch_b), *no = fo + (c + 1);
+        GX_CUDA(ctx, cudaMemsetAsync(fc64 + c, 0, sizeof(int64_t), ctx->stream));
+        GX_CUDA(ctx, cudaMemsetAsync(nc64 + c, 0, sizeof(int64_t), ctx->stream));
+        k_i32_to_i64<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(fcnt + s, fc64, c);
+        k_i32_to_i64<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(ncnt + s, nc64, c);
+        GX_TRY(gx_exclusive_scan_i64(ctx, fc64, fo, c + 1));
+        GX_TRY(gx_exclusive_scan_i64(ctx, nc64, no, c + 1));
+        int64_t ft = 0, nt = 0;
+        GX_CUDA(ctx, cudaMemcpyAsync(&ft, fo + c, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(&nt, no + c, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        // grow (preserving) the index arrays
+        auto grow = [&](DevBuf &b, size_t &cap, int64_t need) -> int {
+            if ((size_t)need <= cap) return GX_OK;
+            size_t nc = std::max((size_t)need, cap * 2);
+            void *p = nullptr;
+            if (cudaMalloc(&p, nc * sizeof(int32_t)) != cudaSuccess) return gx_fail(ctx, GX_ERR_ALLOC, "list storage");
+            cudaMemcpyAsync(p, b.p, cap * sizeof(int32_t), cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(b.p);
+            b.p = p;
+            b.bytes = nc * sizeof(int32_t);
+            cap = nc;
+            return GX_OK;
+        };
+        GX_TRY(grow(ctx->far_idx, far_cap, far_tot + ft + 1));
+        GX_TRY(grow(ctx->near_idx, near_cap, near_tot + nt + 1));
+        // starts = level offsets + running totals
+        GX_TRY(gx_add_offsets(ctx, fo, fstart + s, c, far_tot));
+        GX_TRY(gx_add_offsets(ctx, no, nstart + s, c, near_tot));
+        k_mac<<<gx_blocks(c, 128), 128, 0, ctx->stream>>>(s, e, 1, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
+                                                          dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta,
+                                                          nstart, ncnt, dptr<int32_t>(ctx->near_idx), fcnt, ncnt, fstart,
+                                                          nstart, dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx));
+        ctx->launches += 6;
+        GX_CUDA(ctx, cudaGetLastError());
+        far_tot += ft;
+        near_tot += nt;
+        if (lv == 0) {
+            ctx->n_near_pairs = nt;
+        }
+    }
+    ctx->n_far_pairs = far_tot;
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->plan_acc_valid = true;
+    ctx->plan_p = ctx->p;
+    ctx->plan_eps = ctx->eps;
+    ctx->plan_theta = ctx->theta;
+    return GX_OK;
+}
+
+namespace {
+__global__ void k_add_offsets(const int64_t *o, int64_t *dst, int64_t c, int64_t add) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < c) dst[i] = o[i] + add;
+}
+}  // namespace
+
+int gx_add_offsets(gx_ctx *ctx, const int64_t *o, int64_t *dst, int64_t c, int64_t add) {
+    k_add_offsets<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(o, dst, c, add);
+    ctx->launches++;
+    GX_CUDA(ctx, cudaGetLastError());
+    return GX_OK;
+}
+
+// build_constrained (lib.rs:541-588) on the device: up to 10 rebuilds with split
+// points; the per-leaf neighbour search runs on the GPU, the split-point set (a
+// small sorted list) is kept on the host.
+int gx_tree_balance(gx_ctx *ctx, int64_t n_max, const double bounds[4]) {
+    std::vector<int64_t> splits;
+    for (int iter = 0; iter < 10; iter++) {
+        GX_TRY(gx_tree_rebuild_with_splits(ctx, n_max, bounds, splits));
+        if (ctx->n_levels > 64) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "balanced build: too many levels");
+        LevelSet ls;
+        ls.n = ctx->n_levels;
+        size_t total = 0;
+        for (int L = 0; L < ls.n; L++) total += bvh_bytes(ctx->level_start[L + 1] - ctx->level_start[L]);
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, total));
+        size_t off = 0;
+        for (int L = 0; L < ls.n; L++) {
+            size_t used = 0;
+            GX_TRY(build_level(ctx, ctx->level_start[L], ctx->level_start[L + 1], ctx->scratch_a, off, ls.lv[L], &used));
+            off += bvh_bytes(ctx->level_start[L + 1] - ctx->level_start[L]);
+        }
+        int64_t nl = ctx->n_leaves;
+        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int64_t) * (size_t)nl));
+        GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
+        k_balance_splits<<<gx_blocks(nl, 64), 64, 0, ctx->stream>>>(ls, nl, dptr<double>(ctx->cx), dptr<double>(ctx->cy),
+                                                                   dptr<double>(ctx->hw), dptr<int32_t>(ctx->bs),
+                                                                   dptr<int32_t>(ctx->be), dptr<int64_t>(ctx->scratch_b),
+                                                                   dptr<unsigned>(ctx->status));
+        ctx->launches++;
+        GX_CUDA(ctx, cudaGetLastError());
+        std::vector<int64_t> mids((size_t)nl);
+        GX_CUDA(ctx, cudaMemcpyAsync(mids.data(), ctx->scratch_b.p, sizeof(int64_t) * (size_t)nl,
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        GX_TRY(check_status(ctx));
+        std::set<int64_t> have(splits.begin(), splits.end());
+        bool added = false;
+        for (int64_t m : mids) {
+            if (m < 0 || have.count(m)) continue;
+            have.insert(m);
+            added = true;
+        }
+        if (!added) return GX_OK;
+        splits.assign(have.begin(), have.end());
+    }
+    return gx_tree_rebuild_with_splits(ctx, n_max, bounds, splits);
+}

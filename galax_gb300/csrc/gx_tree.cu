@@ -1,0 +1,336 @@
+// gx_tree.cu -- device Tree::build (galax-core/src/lib.rs:163-361) and
+// build_constrained (lib.rs:541-694).
+//
+// Bit-exactness rules: every value that decides topology or feeds a key is
+// computed with separately rounded IEEE operations (__dmul_rn / __dadd_rn /
+// __dsub_rn, which the compiler never contracts into FMA), in the reference's
+// order: Morton normalisation, leaf mass and COM sums (body order), parent sums
+// (child slot order), box centres and half-widths.
+#include <algorithm>
+
+#include "gx_internal.cuh"
+
+namespace {
+
+constexpr double kOneMinus = 1.0 - 1e-15;  // clamp bound of normalize (lib.rs:76)
+
+// normalize (lib.rs:75-78): NaN clamps to NaN and casts to 0, like Rust `as u64`.
+__device__ __forceinline__ uint64_t normalize_dev(double x, double lo, double hi) {
+    double t = __ddiv_rn(__dsub_rn(x, lo), __dsub_rn(hi, lo));
+    if (t < 0.0) t = 0.0;
+    if (t > kOneMinus) t = kOneMinus;
+    if (!(t > 0.0)) return 0ull;
+    return __double2ull_rz(__dmul_rn(t, 2097152.0));
+}
+
+// spread_bits (lib.rs:85-93)
+__device__ __forceinline__ uint64_t spread_dev(uint64_t v) {
+    uint64_t x = v & ((1ull << 21) - 1);
+    x = (x | (x << 16)) & 0x0000ffff0000ffffull;
+    x = (x | (x << 8)) & 0x00ff00ff00ff00ffull;
+    x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
+    return x;
+}
+
+__global__ void k_morton(const double *__restrict__ x, const double *__restrict__ y, int64_t n, double x0, double x1,
+                         double y0, double y1, uint64_t *__restrict__ keys, uint32_t *__restrict__ idx) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    keys[i] = spread_dev(normalize_dev(x[i], x0, x1)) | (spread_dev(normalize_dev(y[i], y0, y1)) << 1);
+    idx[i] = (uint32_t)i;
+}
+
+// gather of the seven body arrays (Tree::permute, lib.rs:146-161)
+__global__ void k_permute(const uint32_t *__restrict__ idx, int64_t n, const double *__restrict__ in,
+                          double *__restrict__ out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[idx[i]];
+}
+
+__device__ __forceinline__ double fmin_rs(double a, double b) { return (a != a) ? b : ((b != b) ? a : (b < a ? b : a)); }
+__device__ __forceinline__ double fmax_rs(double a, double b) { return (a != a) ? b : ((b != b) ? a : (b > a ? b : a)); }
+
+// leaf nodes (lib.rs:228-267); one thread per leaf, sums in body order.
+__global__ void k_leaves(const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ m,
+                         const int32_t *__restrict__ rs, const int32_t *__restrict__ re, int64_t nl, double *cx,
+                         double *cy, double *hw, double *mass, double *comx, double *comy, int32_t *bs, int32_t *be,
+                         int4 *child, int32_t *parent, uint8_t *is_leaf) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    int32_t s = rs[L], e = re[L];
+    double ms = 0.0, sx = 0.0, sy = 0.0;
+    double bx0 = 1.7976931348623157e308, bx1 = -1.7976931348623157e308;
+    double by0 = 1.7976931348623157e308, by1 = -1.7976931348623157e308;
+    for (int32_t i = s; i < e; i++) {
+        double mm = m[i], xi = x[i], yi = y[i];
+        ms = __dadd_rn(ms, mm);
+        sx = __dadd_rn(sx, __dmul_rn(xi, mm));
+        sy = __dadd_rn(sy, __dmul_rn(yi, mm));
+        bx0 = fmin_rs(bx0, xi); bx1 = fmax_rs(bx1, xi);
+        by0 = fmin_rs(by0, yi); by1 = fmax_rs(by1, yi);
+    }
+    double c_x = __dmul_rn(__dadd_rn(bx0, bx1), 0.5), c_y = __dmul_rn(__dadd_rn(by0, by1), 0.5);
+    double h = __dadd_rn(__dmul_rn(fmax_rs(__dsub_rn(bx1, bx0), __dsub_rn(by1, by0)), 0.5), 1e-15);
+    cx[L] = c_x; cy[L] = c_y; hw[L] = h; mass[L] = ms;
+    comx[L] = ms > 0.0 ? __ddiv_rn(sx, ms) : c_x;
+    comy[L] = ms > 0.0 ? __ddiv_rn(sy, ms) : c_y;
+    bs[L] = s; be[L] = e;
+    child[L] = make_int4(-1, -1, -1, -1);
+    parent[L] = -1;
+    is_leaf[L] = 1;
+}
+
+// leaf ranges of Tree::build: chunks of n_max
+__global__ void k_chunk_ranges(int64_t n, int64_t n_max, int64_t nl, int32_t *rs, int32_t *re) {
+    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (L >= nl) return;
+    int64_t s = L * n_max, e = s + n_max < n ? s + n_max : n;
+    rs[L] = (int32_t)s;
+    re[L] = (int32_t)e;
+}
+
+// ---- parent rounds (lib.rs:269-354) ----
+__global__ void k_round_heads(int64_t s, int64_t c, const uint64_t *__restrict__ keys, const int32_t *__restrict__ bs,
+                              unsigned sh, int32_t *head) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c) return;
+    uint64_t g = keys[bs[s + i]] >> sh;
+    head[i] = (i == 0) ? 1 : (g != (keys[bs[s + i - 1]] >> sh));
+}
+
+__global__ void k_seg_start(int64_t c, const int32_t *head, const int32_t *segex, int32_t *segstart) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c) return;
+    if (head[i]) segstart[segex[i]] = (int32_t)i;
+}
+
+__global__ void k_seg_groups(int64_t nseg, int64_t c, const int32_t *segstart, int32_t *gcnt) {
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nseg) return;
+    int64_t len = ((k + 1 < nseg) ? segstart[k + 1] : c) - segstart[k];
+    gcnt[k] = (int32_t)((len + 3) / 4);
+}
+
+__global__ void k_assign(int64_t s, int64_t e, int64_t c, const int32_t *head, const int32_t *segex,
+                         const int32_t *segstart, const int32_t *goff, int32_t *parent, int32_t *child) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= c) return;
+    int32_t seg = segex[i] + head[i] - 1;
+    int32_t pos = (int32_t)i - segstart[seg];
+    int64_t g = (int64_t)goff[seg] + pos / 4;
+    parent[s + i] = (int32_t)(e + g);
+    child[(e + g) * 4 + (pos & 3)] = (int32_t)(s + i);
+}
+
+__global__ void k_parent_fields(int64_t e, int64_t ng, double *cx, double *cy, double *hw, double *mass, double *comx,
+                                double *comy, int32_t *bs, int32_t *be, const int4 *child, int32_t *parent,
+                                uint8_t *is_leaf) {
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    int64_t q = e + g;
+    int4 c4 = child[q];
+    int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+    double ms = 0.0, sx = 0.0, sy = 0.0, mh = 0.0;
+    double bx0 = 1.7976931348623157e308, bx1 = -1.7976931348623157e308;
+    double by0 = 1.7976931348623157e308, by1 = -1.7976931348623157e308;
+    int first = cc[0], last = cc[0];
+    for (int k = 0; k < 4; k++) {
+        int s = cc[k];
+        if (s < 0) break;
+        last = s;
+        double cm = mass[s], h = hw[s], ccx = cx[s], ccy = cy[s];
+        ms = __dadd_rn(ms, cm);
+        sx = __dadd_rn(sx, __dmul_rn(comx[s], cm));
+        sy = __dadd_rn(sy, __dmul_rn(comy[s], cm));
+        if (h > mh) mh = h;
+        double cl = __dsub_rn(ccx, h), cr = __dadd_rn(ccx, h);
+        if (cl < bx0) bx0 = cl;
+        if (cr > bx1) bx1 = cr;
+        double cb = __dsub_rn(ccy, h), ct = __dadd_rn(ccy, h);
+        if (cb < by0) by0 = cb;
+        if (ct > by1) by1 = ct;
+    }
+    double c_x = __dmul_rn(__dadd_rn(bx0, bx1), 0.5), c_y = __dmul_rn(__dadd_rn(by0, by1), 0.5);
+    cx[q] = c_x; cy[q] = c_y; hw[q] = __dmul_rn(mh, 2.0); mass[q] = ms;
+    comx[q] = ms > 0.0 ? __ddiv_rn(sx, ms) : c_x;
+    comy[q] = ms > 0.0 ? __ddiv_rn(sy, ms) : c_y;
+    bs[q] = bs[first];
+    be[q] = be[last];
+    parent[q] = -1;
+    is_leaf[q] = 0;
+}
+
+// ---- build_constrained helpers (lib.rs:541-694) ----
+// leaf ranges bounded by n_max and by the sorted split points (lib.rs:603-613):
+// computed on the host from the split list, which is small.
+
+}  // namespace
+
+// Node storage with capacity growth (contents preserved).
+static int ensure_nodes(gx_ctx *ctx, int64_t need) {
+    struct F { DevBuf *b; size_t sz; };
+    F f[] = {{&ctx->cx, 8}, {&ctx->cy, 8}, {&ctx->hw, 8}, {&ctx->mass, 8}, {&ctx->comx, 8}, {&ctx->comy, 8},
+             {&ctx->bs, 4}, {&ctx->be, 4}, {&ctx->child, 16}, {&ctx->parent, 4}, {&ctx->is_leaf, 1}};
+    for (auto &e : f) {
+        size_t want = e.sz * (size_t)need;
+        if (e.b->bytes >= want) continue;
+        size_t nb = std::max(want, e.b->bytes * 2);
+        void *p = nullptr;
+        if (cudaMalloc(&p, nb) != cudaSuccess) return gx_fail(ctx, GX_ERR_ALLOC, "node storage allocation failed");
+        if (e.b->p) {
+            cudaMemcpyAsync(p, e.b->p, e.b->bytes, cudaMemcpyDeviceToDevice, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(e.b->p);
+        }
+        e.b->p = p;
+        e.b->bytes = nb;
+    }
+    return GX_OK;
+}
+
+// Builds nodes from leaf ranges already in scratch (rs, re as int32), using ctx->keys
+// (Morton keys of the tree-ordered bodies).
+static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, int64_t nl) {
+    int64_t guess = nl * 4 + 64;
+    GX_TRY(ensure_nodes(ctx, guess));
+    k_leaves<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(
+        dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->m), rs, re, nl, dptr<double>(ctx->cx),
+        dptr<double>(ctx->cy), dptr<double>(ctx->hw), dptr<double>(ctx->mass), dptr<double>(ctx->comx),
+        dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), dptr<int4>(ctx->child),
+        dptr<int32_t>(ctx->parent), dptr<uint8_t>(ctx->is_leaf));
+    ctx->launches++;
+    GX_CUDA(ctx, cudaGetLastError());
+    ctx->level_start.clear();
+    ctx->level_start.push_back(0);
+    int64_t s = 0, e = nl, nn = nl;
+    unsigned shift = 2;
+    // per-round scratch: head, segex, segstart, gcnt, goff (int32, <= count each)
+    GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int32_t) * (size_t)(nl + 1) * 5));
+    int rounds = 0;
+    while (e - s > 1) {
+        if (++rounds > 400) return gx_fail(ctx, GX_ERR_STATE, "tree build did not converge");
+        int64_t c = e - s;
+        int32_t *head = dptr<int32_t>(ctx->scratch_a);
+        int32_t *segex = head + c;
+        int32_t *segstart = segex + c;
+        int32_t *gcnt = segstart + c;
+        int32_t *goff = gcnt + c;
+        unsigned sh = shift & 63u;
+        k_round_heads<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, c, dptr<uint64_t>(ctx->keys),
+                                                                   dptr<int32_t>(ctx->bs), sh, head);
+        int32_t nseg = 0;
+        GX_TRY(gx_exclusive_scan_i32(ctx, head, segex, c, &nseg));
+        k_seg_start<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(c, head, segex, segstart);
+        k_seg_groups<<<gx_blocks(nseg, 256), 256, 0, ctx->stream>>>(nseg, c, segstart, gcnt);
+        int32_t ng = 0;
+        GX_TRY(gx_exclusive_scan_i32(ctx, gcnt, goff, nseg, &ng));
+        GX_TRY(ensure_nodes(ctx, nn + ng));
+        GX_CUDA(ctx, cudaMemsetAsync(dptr<int4>(ctx->child) + e, 0xFF, sizeof(int4) * (size_t)ng, ctx->stream));
+        k_assign<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, c, head, segex, segstart, goff,
+                                                             dptr<int32_t>(ctx->parent), dptr<int32_t>(ctx->child));
+        k_parent_fields<<<gx_blocks(ng, 128), 128, 0, ctx->stream>>>(
+            e, ng, dptr<double>(ctx->cx), dptr<double>(ctx->cy), dptr<double>(ctx->hw), dptr<double>(ctx->mass),
+            dptr<double>(ctx->comx), dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be),
+            dptr<int4>(ctx->child), dptr<int32_t>(ctx->parent), dptr<uint8_t>(ctx->is_leaf));
+        ctx->launches += 5;
+        GX_CUDA(ctx, cudaGetLastError());
+        ctx->level_start.push_back(e);
+        s = e;
+        e = e + ng;
+        nn = e;
+        shift += 2;
+    }
+    ctx->level_start.push_back(nn);
+    ctx->n_nodes = nn;
+    ctx->n_leaves = nl;
+    ctx->n_levels = (int32_t)ctx->level_start.size() - 1;
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
+// Bodies must already be resident (ctx->x ... in input order).  Sorts them into
+// Morton order on the device, then builds the node hierarchy.
+int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bounds[4], int flags) {
+    ctx->have_tree = false;
+    ctx->plan_ref_valid = ctx->plan_acc_valid = false;
+    if (n <= 0) {
+        ctx->n_nodes = ctx->n_leaves = 0;
+        ctx->n_levels = 0;
+        ctx->level_start.assign(1, 0);
+        ctx->have_tree = true;
+        return GX_OK;
+    }
+    if (n >= 0x7fffffffLL) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "n must be < 2^31");
+    // keys + permutation
+    GX_TRY(gx_ensure(ctx, ctx->keys, sizeof(uint64_t) * n));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(uint64_t) * n));               // keys alt
+    GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(uint32_t) * n * 2));           // idx, idx alt
+    uint64_t *keys = dptr<uint64_t>(ctx->keys), *keys_alt = dptr<uint64_t>(ctx->scratch_b);
+    uint32_t *idx = dptr<uint32_t>(ctx->scratch_c), *idx_alt = idx + n;
+    k_morton<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(dptr<double>(ctx->x), dptr<double>(ctx->y), n, bounds[0],
+                                                         bounds[1], bounds[2], bounds[3], keys, idx);
+    ctx->launches++;
+    GX_CUDA(ctx, cudaGetLastError());
+    if (!(flags & GX_BUILD_BALANCED)) {
+        bool alt = false;
+        GX_TRY(gx_radix_sort_u64(ctx, keys, idx, n, 0, 42, keys_alt, idx_alt, &alt));
+        if (alt) {
+            GX_CUDA(ctx, cudaMemcpyAsync(keys, keys_alt, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+            idx = idx_alt;
+        }
+        // permute the seven arrays through scratch_d
+        GX_TRY(gx_ensure(ctx, ctx->scratch_d, sizeof(double) * n));
+        DevBuf *arrs[7] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->m, &ctx->ax, &ctx->ay};
+        for (DevBuf *a : arrs) {
+            k_permute<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(idx, n, dptr<double>(*a), dptr<double>(ctx->scratch_d));
+            ctx->launches++;
+            std::swap(a->p, ctx->scratch_d.p);
+            std::swap(a->bytes, ctx->scratch_d.bytes);
+        }
+        GX_CUDA(ctx, cudaGetLastError());
+    }
+    int64_t nl = (n + n_max - 1) / n_max;
+    GX_TRY(gx_ensure(ctx, ctx->scratch_f, sizeof(int32_t) * (size_t)(2 * nl + 2) + 64));
+    // scratch_f is also the radix-sort flag; the sort is finished at this point
+    int32_t *rs = dptr<int32_t>(ctx->scratch_f), *re = rs + nl;
+    k_chunk_ranges<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(n, n_max, nl, rs, re);
+    ctx->launches++;
+    GX_CUDA(ctx, cudaGetLastError());
+    ctx->n_bodies = n;
+    GX_TRY(build_from_ranges(ctx, rs, re, nl));
+    ctx->have_tree = true;
+    return GX_OK;
+}
+
+// Rebuild with forced split points (build_with_constraints, lib.rs:592-694): no sort;
+// keys from the resident bodies.  Exposed to the balanced builder in gx_lists.cu.
+int gx_tree_rebuild_with_splits(gx_ctx *ctx, int64_t n_max, const double bounds[4], const std::vector<int64_t> &splits) {
+    int64_t n = ctx->n_bodies;
+    GX_TRY(gx_ensure(ctx, ctx->keys, sizeof(uint64_t) * n));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(uint32_t) * n * 2));
+    k_morton<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(dptr<double>(ctx->x), dptr<double>(ctx->y), n, bounds[0],
+                                                         bounds[1], bounds[2], bounds[3], dptr<uint64_t>(ctx->keys),
+                                                         dptr<uint32_t>(ctx->scratch_c));
+    ctx->launches++;
+    std::vector<int32_t> hrs, hre;
+    int64_t s = 0;
+    size_t k = 0;
+    while (s < n) {
+        int64_t bound = std::min(s + n_max, n);
+        while (k < splits.size() && splits[k] <= s) k++;
+        int64_t e = (k < splits.size() && splits[k] < bound) ? splits[k] : bound;
+        hrs.push_back((int32_t)s);
+        hre.push_back((int32_t)e);
+        s = e;
+    }
+    int64_t nl = (int64_t)hrs.size();
+    GX_TRY(gx_ensure(ctx, ctx->scratch_f, sizeof(int32_t) * (size_t)(2 * nl + 2) + 64));
+    int32_t *rs = dptr<int32_t>(ctx->scratch_f), *re = rs + nl;
+    GX_CUDA(ctx, cudaMemcpyAsync(rs, hrs.data(), sizeof(int32_t) * nl, cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(ctx, cudaMemcpyAsync(re, hre.data(), sizeof(int32_t) * nl, cudaMemcpyHostToDevice, ctx->stream));
+    GX_TRY(build_from_ranges(ctx, rs, re, nl));
+    ctx->have_tree = true;
+    return GX_OK;
+}

@@ -1,0 +1,162 @@
+/*
+ * galax_gb300.h -- C ABI of libgalaxcu.so, the GB300 (sm_103a) FMM force backend.
+ *
+ * This is the drop-in boundary for knekvasil/galax's GPU force backend
+ * (galax-gpu/src/lib.rs, `GpuContext`).  Each entry point names the reference
+ * interface it replaces.  Plain pointers and sizes only; all host arrays are
+ * caller-owned FP64 structure-of-arrays and are touched only during the call;
+ * device buffers are owned by the context.  One CUDA stream per context; a
+ * context is not thread-safe (callers serialise calls on it), distinct contexts
+ * are independent.  Nothing in the library traps or aborts on the device:
+ * every call returns a gx_status and gx_last_error() gives the message.
+ */
+#ifndef GALAX_GB300_H
+#define GALAX_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GX_ABI_VERSION 1
+
+/* Status codes.  Mirrors GpuError (galax-gpu/src/lib.rs:42-59: InitFailed,
+ * ShaderCompilation -> KERNEL_LOAD, BufferAllocation -> ALLOC) plus the
+ * conditions the reference reports by panicking. */
+typedef enum gx_status {
+    GX_OK = 0,
+    GX_ERR_INIT = 1,          /* no CUDA device / context creation failed */
+    GX_ERR_KERNEL_LOAD = 2,   /* the sm_103a image does not load on this device */
+    GX_ERR_ALLOC = 3,         /* device or pinned-host allocation failed */
+    GX_ERR_INVALID_ARG = 4,   /* bad pointer, size, order p, mode ... */
+    GX_ERR_NONFINITE = 5,     /* non-finite values were met (reported, not fatal) */
+    GX_ERR_CAP_EXCEEDED = 6,  /* a size is beyond the configured maximum */
+    GX_ERR_TIMEOUT = 7,       /* a bounded device wait gave up */
+    GX_ERR_STATE = 8,         /* call out of order (e.g. forces before a tree) */
+    GX_ERR_CUDA = 9           /* a CUDA runtime error; see gx_last_error */
+} gx_status;
+
+/* Evaluation modes. */
+enum {
+    GX_MODE_REF = 0,      /* galax-core semantics: capped V/U lists, first-inserter
+                             derivative cache, node-id-ascending L2L (lib.rs:1466-1499) */
+    GX_MODE_EXACT = 1,    /* REF lists, per-pair derivatives, top-down L2L */
+    GX_MODE_ACCURATE = 2  /* MAC near/far lists on the same tree (theta), per-pair
+                             derivatives, top-down L2L; not in the reference */
+};
+enum {
+    GX_PREC_FP64 = 0,     /* FP64 end to end */
+    GX_PREC_MIXED = 1     /* FP32 P2M/L2P/P2P, FP32 M2L; FP64 state and reductions */
+};
+/* gx_build_tree flags */
+enum {
+    GX_BUILD_BALANCED = 1 /* build_constrained (lib.rs:541-588) instead of Tree::build */
+};
+/* list selectors for gx_export_lists */
+enum { GX_LIST_V = 0, GX_LIST_U = 1 };
+
+/* GpuConfig (galax-gpu/src/lib.rs:22-40).  eps64 > 0 overrides the f32 eps. */
+typedef struct gx_config {
+    uint32_t max_n;             /* default 262144 */
+    uint32_t max_nodes;         /* default 524288 */
+    uint32_t max_interactions;  /* default 1<<24 */
+    uint32_t p;                 /* expansion order, 0..16; default 4 */
+    float eps;                  /* softening, f32 as in the reference; default 0.1 */
+    double eps64;               /* FP64 softening; used when > 0 */
+    int32_t device;             /* CUDA device ordinal; default 0 */
+} gx_config;
+
+typedef struct gx_ctx gx_ctx;
+
+/* GpuConfig::default (galax-gpu/src/lib.rs:32-40). */
+int gx_config_default(gx_config *cfg);
+
+/* GpuContext::new (galax-gpu/src/lib.rs:268-390): creates the stream and checks
+ * the kernel image; buffers grow on demand up to the configured maxima. */
+int gx_create(const gx_config *cfg, gx_ctx **out);
+int gx_destroy(gx_ctx *ctx);
+const char *gx_last_error(const gx_ctx *ctx);
+int gx_abi_version(void);
+
+/* Evaluation mode, precision and MAC opening angle (theta, ACCURATE only). */
+int gx_set_mode(gx_ctx *ctx, int mode, int precision, double theta);
+/* Changes p and the softening of an existing context. */
+int gx_set_params(gx_ctx *ctx, uint32_t p, double eps);
+
+/* GpuContext::upload_tree_data (galax-gpu/src/lib.rs:392-462): a host-built tree
+ * (galax-core Tree::build, lib.rs:163-361) with its V-list and U-list in the
+ * reference's fixed layout (InteractionLists, lib.rs:941-944: n_nodes*64 u32,
+ * unused slots 0xFFFFFFFF, and u8 lengths).  Bodies are taken to be in tree
+ * order (body ranges index them).  child: 4 per node, -1 = none.  parent: -1 = none. */
+int gx_upload_tree(gx_ctx *ctx, int64_t n_nodes, int64_t n_bodies, const double *cx, const double *cy,
+                   const double *hw, const double *mass, const double *comx, const double *comy,
+                   const int64_t *body_start, const int64_t *body_end, const int32_t *child,
+                   const int32_t *parent, const uint8_t *is_leaf, const uint32_t *vlist_data,
+                   const uint8_t *vlist_len, const uint32_t *ulist_data, const uint8_t *ulist_len);
+
+/* Device tree build: Tree::build (lib.rs:163-361) or, with GX_BUILD_BALANCED,
+ * build_constrained (lib.rs:541-588), then InteractionLists::build
+ * (lib.rs:947-1025) and build_p2p_lists (lib.rs:1358-1392), all on the GPU and
+ * bit-exact with the reference.  Like Tree::build it permutes the seven host
+ * arrays in place into Morton order (any of vx, vy, ax, ay may be NULL).
+ * bounds = {x_min, x_max, y_min, y_max}. */
+int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, double *vy, double *m,
+                  double *ax, double *ay, int64_t n_max, const double bounds[4], int flags);
+/* Tree shape of the current tree. */
+int gx_tree_info(gx_ctx *ctx, int64_t *n_nodes, int64_t *n_leaves, int32_t *n_levels, int64_t *n_bodies);
+/* Copies the current tree to host arrays (any pointer may be NULL); the Tree the
+ * CLI keeps on the host.  level_start has n_levels+1 entries. */
+int gx_export_tree(gx_ctx *ctx, double *cx, double *cy, double *hw, double *mass, double *comx,
+                   double *comy, int64_t *body_start, int64_t *body_end, int32_t *child, int32_t *parent,
+                   uint8_t *is_leaf, int64_t *level_start);
+/* Copies a REF list (GX_LIST_V / GX_LIST_U) in the reference layout. */
+int gx_export_lists(gx_ctx *ctx, int which, uint32_t *data, uint8_t *lengths);
+/* Sizes of the lists the current mode uses: far (M2L) pairs and P2P leaf pairs. */
+int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64_t *n_p2p_interactions);
+
+/* GpuContext::step + read_accelerations (galax-gpu/src/lib.rs:464-566): uploads
+ * x, y, m (tree order), runs the six passes, writes ax, ay.  Inputs are sanitised
+ * on the device like compute_fmm_force (lib.rs:1474-1482). */
+int gx_compute_forces(gx_ctx *ctx, const double *x, const double *y, const double *m, double *ax, double *ay);
+
+/* Device-resident state (no per-step host traffic). */
+int gx_upload_bodies(gx_ctx *ctx, int64_t n, const double *x, const double *y, const double *vx,
+                     const double *vy, const double *m, const double *ax, const double *ay);
+int gx_download_bodies(gx_ctx *ctx, double *x, double *y, double *vx, double *vy, double *m, double *ax,
+                       double *ay);
+/* One force evaluation on the resident bodies (fills the resident ax, ay). */
+int gx_forces_resident(gx_ctx *ctx);
+/* simulate / simulate_gpu (galax-integrate/src/lib.rs:204-237, 327-368) on the
+ * resident bodies: n_steps KDK steps with the static tree; every energy_every
+ * steps a row {step, KE, FMM PE, px, py, Lz} is written to diag (6 doubles per row).
+ * *n_diag receives the row count. */
+int gx_kdk_run(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag);
+/* Diagnostics of the resident bodies (lib.rs:1638-1683): {KE, FMM PE, px, py, Lz}. */
+int gx_diagnostics(gx_ctx *ctx, double out[5]);
+/* GpuContext::n2_debug (galax-gpu/src/lib.rs:670-714) restricted to sampled
+ * targets: exact FP64 softened sum (validate_fmm, lib.rs:1537-1553) over all
+ * resident bodies for the targets idx[0..n_idx). */
+int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, double *ay);
+
+/* Device time of the last force evaluation per pass, in ms:
+ * {total, prepare, p2m, m2m, m2l, l2l, l2p+p2p}; returns 7 entries. */
+int gx_last_timings(gx_ctx *ctx, double out[7]);
+/* Runs `reps` force evaluations on the resident bodies and returns the CUDA-event
+ * time of each on the context stream (ms) and the time of one pass of it
+ * (`which`: 0 = L2P+P2P, 1 = M2L).  With flush_l2 != 0 a 256 MB buffer (twice
+ * the L2) is written before each evaluation, outside its timed interval. */
+int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each, int32_t which,
+                    double *kernel_ms_each);
+/* Number of kernels the last force evaluation launched. */
+int gx_last_launch_count(gx_ctx *ctx, int64_t *count);
+
+/* Page-locked host memory for the host-buffer entry points (cudaMallocHost);
+ * NULL on failure. */
+void *gx_host_alloc(size_t bytes);
+void gx_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,136 @@
+"""Force evaluation through the C ABI against the oracle.
+
+REF mode must match compute_fmm_force (galax-core/src/lib.rs:1466-1499) within
+1e-10 relative per body (vector metric, |a*| floored at 1e-30).  EXACT and
+ACCURATE FP64 modes match the oracle's restatement of the same algorithm within
+1e-10.  The mixed-precision form is checked against the FP64 form (1e-4 median)
+and both against the exact FP64 N^2 sum.
+"""
+import numpy as np
+import pytest
+
+from helpers import oracle_case, rel_vec_err
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-10
+
+
+def _run_gpu(G, b_sorted, t, v, u, p, eps, mode, prec=0, theta=0.5, via="upload"):
+    n = len(b_sorted.x)
+    ctx = G.GpuContext(G.GpuConfig(max_n=max(n, 1), max_nodes=1 << 26, p=p, eps64=eps))
+    ctx.set_mode(mode, prec, theta)
+    if via == "upload":
+        ctx.upload_tree_data(t, v, u)
+    ax, ay = np.zeros(n), np.zeros(n)
+    x, y, m = b_sorted.x.copy(), b_sorted.y.copy(), b_sorted.mass.copy()
+    if via == "build":
+        gb = G.Bodies.from_arrays(x, y, m)
+        ctx.build_tree(gb, t.n_max, t.bounds)
+        x, y, m = gb.x, gb.y, gb.mass
+    if mode == G.MODE_ACCURATE:
+        ctx.upload_bodies(G.Bodies.from_arrays(x, y, m))
+    ctx.compute_forces(x, y, m, ax, ay)
+    ctx.close()
+    return ax, ay
+
+
+@pytest.mark.parametrize("preset,n,p", [("uniform", 10_000, 4), ("plummer", 20_000, 4), ("galaxy", 5_001, 4),
+                                        ("uniform", 3_000, 2), ("uniform", 3_000, 0)])
+@pytest.mark.parametrize("via", ["upload", "build"])
+def test_ref_mode_matches_oracle(G, oracle, preset, n, p, via):
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=1)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS[preset], p)
+    ref = ob.copy()
+    oracle.compute_fmm_force(ref, t, v, u, p, eps, oracle.MODE_REF)
+    ax, ay = _run_gpu(G, ob, t, v, u, p, eps, G.MODE_REF, via=via)
+    err = rel_vec_err(ax, ay, ref.ax, ref.ay)
+    assert err.max() < TOL_FP64, f"max {err.max():.3e} at body {err.argmax()}"
+
+
+@pytest.mark.parametrize("p", [1, 3, 6, 8])
+def test_ref_mode_orders(G, oracle, p):
+    from galax_gb300 import presets
+    b = presets.uniform(2_000, seed=4)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS["uniform"], p)
+    ref = ob.copy()
+    oracle.compute_fmm_force(ref, t, v, u, p, eps, oracle.MODE_REF)
+    ax, ay = _run_gpu(G, ob, t, v, u, p, eps, G.MODE_REF)
+    err = rel_vec_err(ax, ay, ref.ax, ref.ay)
+    assert err.max() < TOL_FP64
+
+
+def test_exact_mode_matches_oracle(G, oracle):
+    from galax_gb300 import presets
+    b = presets.uniform(10_000, seed=2)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS["uniform"], 4)
+    ref = ob.copy()
+    oracle.compute_fmm_force(ref, t, v, u, 4, eps, oracle.MODE_EXACT)
+    ax, ay = _run_gpu(G, ob, t, v, u, 4, eps, G.MODE_EXACT)
+    err = rel_vec_err(ax, ay, ref.ax, ref.ay)
+    assert err.max() < TOL_FP64
+
+
+@pytest.mark.parametrize("preset,n", [("uniform", 10_000), ("plummer", 30_000)])
+def test_accurate_mode_fp64_matches_oracle(G, oracle, preset, n):
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=6)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS[preset], 4)
+    R = oracle.node_radii(ob, t)
+    far, near = oracle.mac_lists_build(t, R, 0.5)
+    ref = ob.copy()
+    oracle.compute_fmm_force_mac(ref, t, far, near, 4, eps)
+    ax, ay = _run_gpu(G, ob, t, v, u, 4, eps, G.MODE_ACCURATE, theta=0.5)
+    err = rel_vec_err(ax, ay, ref.ax, ref.ay)
+    assert err.max() < TOL_FP64, f"max {err.max():.3e}"
+
+
+@pytest.mark.parametrize("preset,n", [("uniform", 10_000), ("plummer", 30_000)])
+def test_mixed_precision_error_budget(G, oracle, preset, n):
+    """Mixed form vs FP64 form, and both vs the exact FP64 N^2 sum on 1000 samples:
+    median relative force error <= 1e-4."""
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=8)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS[preset], 4)
+    a64 = _run_gpu(G, ob, t, v, u, 4, eps, G.MODE_ACCURATE, G.PREC_FP64)
+    a32 = _run_gpu(G, ob, t, v, u, 4, eps, G.MODE_ACCURATE, G.PREC_MIXED)
+    idx = np.random.default_rng(0).choice(n, 1000, replace=False)
+    ex, ey = oracle.n2_sampled(ob.x, ob.y, ob.mass, eps, idx)
+    e64 = rel_vec_err(a64[0][idx], a64[1][idx], ex, ey)
+    e32 = rel_vec_err(a32[0][idx], a32[1][idx], ex, ey)
+    d = rel_vec_err(a32[0], a32[1], a64[0], a64[1])
+    assert np.median(e64) <= 1e-4, np.median(e64)
+    assert np.median(e32) <= 1e-4, np.median(e32)
+    assert np.median(d) < 1e-5, np.median(d)
+
+
+def test_sanitised_inputs_match_oracle(G, oracle):
+    """compute_fmm_force zeroes invalid positions and sets bad masses to 1 (lib.rs:1474-1482)."""
+    from galax_gb300 import presets
+    b = presets.uniform(3_000, seed=12)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS["uniform"], 4)
+    bad = ob.copy()
+    bad.mass[5] = -1.0
+    bad.mass[9] = np.nan
+    bad.x[17] = 1e101
+    bad.y[23] = np.inf
+    ref = bad.copy()
+    oracle.compute_fmm_force(ref, t, v, u, 4, eps, oracle.MODE_REF)
+    ax, ay = _run_gpu(G, bad, t, v, u, 4, eps, G.MODE_REF)
+    err = rel_vec_err(ax, ay, ref.ax, ref.ay)
+    assert np.all(np.isfinite(ax)) and err.max() < TOL_FP64
+
+
+def test_p2p_only_at_p0_equals_p2p(G, oracle):
+    """test_fmm_p0_equals_p2p (lib.rs:2320-2357): at p=0 the far field vanishes."""
+    n = 200
+    t_ = np.arange(n) / n
+    from galax_gb300 import Bodies
+    b = Bodies.from_arrays(5 + 90 * np.modf(t_ * 3.7)[0], 5 + 90 * np.modf(t_ * 7.3)[0],
+                           0.1 + 10 * np.modf(t_ * 11.0)[0])
+    ob, t, v, u, _ = oracle_case(oracle, b, 16, (0.0, 100.0, 0.0, 100.0), 0)
+    pp = ob.copy()
+    oracle.p2p(pp, t, u, 0.1)
+    ax, ay = _run_gpu(G, ob, t, v, u, 0, 0.1, G.MODE_REF)
+    assert np.max(np.abs(ax - pp.ax)) < 1e-12 and np.max(np.abs(ay - pp.ay)) < 1e-12

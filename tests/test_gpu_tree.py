@@ -1,0 +1,118 @@
+"""Device tree build and interaction lists, bit-exact against the oracle.
+
+Tree::build (galax-core/src/lib.rs:163-361): Morton keys, stable sort, permute,
+leaves, parent rounds; InteractionLists::build (lib.rs:947-1025) and
+build_p2p_lists (lib.rs:1358-1392); build_constrained (lib.rs:541-588).
+"""
+import numpy as np
+import pytest
+
+from helpers import oracle_case
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["cx", "cy", "hw", "mass", "comx", "comy", "body_start", "body_end", "parent", "is_leaf"]
+
+
+def _ctx(G, n):
+    return G.GpuContext(G.GpuConfig(max_n=max(n, 1), max_nodes=1 << 26, p=4, eps64=0.1))
+
+
+def _compare_tree(G, O, b, n_max, bounds, balanced=False):
+    ob = O.Bodies.from_arrays(b.x, b.y, b.mass, b.vx, b.vy)
+    if balanced:
+        t = O.tree_build_constrained(ob, n_max, bounds, accel=True)
+    else:
+        t = O.tree_build(ob, n_max, bounds)
+    ctx = _ctx(G, len(b))
+    gb = b.copy()
+    ctx.build_tree(gb, n_max, bounds, balanced=balanced)
+    # Tree::build permutes every body array in place (lib.rs:204)
+    for name in ("x", "y", "vx", "vy", "mass"):
+        assert np.array_equal(getattr(gb, name), getattr(ob, name), equal_nan=True), name
+    dt = ctx.export_tree()
+    assert dt.n_nodes == t.n_nodes
+    assert dt.n_levels == t.n_levels
+    assert np.array_equal(dt.level_start, t.level_start)
+    for f in FIELDS:
+        a, r = getattr(dt, f), getattr(t, f)
+        assert np.array_equal(a, r, equal_nan=True), f
+    assert np.array_equal(dt.child, t.child)
+    v = O.vlist_build(t)
+    u = O.ulist_build(t)
+    vd, vl = ctx.export_lists(G.LIST_V)
+    ud, ul = ctx.export_lists(G.LIST_U)
+    assert np.array_equal(vl, v.lengths) and np.array_equal(vd, v.data)
+    assert np.array_equal(ul, u.lengths) and np.array_equal(ud, u.data)
+    ctx.close()
+    return t
+
+
+@pytest.mark.parametrize("preset,n,n_max", [
+    ("uniform", 10_000, 32),
+    ("plummer", 20_000, 32),
+    ("galaxy", 5_001, 32),
+    ("disk", 20_000, 16),
+    ("uniform", 3_000, 64),
+])
+def test_tree_and_lists_bit_exact(G, oracle, preset, n, n_max):
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=3)
+    _compare_tree(G, oracle, b, n_max, presets.BOUNDS[preset])
+
+
+def test_cli_box_clamping_and_duplicate_keys(G, oracle):
+    """Bodies outside the [-50,50]^2 CLI box clamp onto edge cells (lib.rs:76);
+    duplicates share keys and keep input order (stable sort)."""
+    from galax_gb300 import presets
+    b = presets.uniform(4_000, seed=5)  # [0,100]^2 in a [-50,50]^2 box: half clamps
+    b.x[:50] = b.x[50:100]  # exact duplicates
+    b.y[:50] = b.y[50:100]
+    _compare_tree(G, oracle, b, 32, (-50.0, 50.0, -50.0, 50.0))
+
+
+@pytest.mark.parametrize("n,n_max", [(1, 32), (2, 1), (33, 32), (64, 32), (17, 1), (200, 4)])
+def test_small_trees(G, oracle, n, n_max):
+    from galax_gb300 import presets
+    b = presets.uniform(n, seed=11)
+    _compare_tree(G, oracle, b, n_max, presets.BOUNDS["uniform"])
+
+
+def test_two_body_chain_known_answer(G, oracle):
+    """(0.25,0.25),(0.75,0.75) with n_max=1 in [0,1]^2: the keys first share a prefix
+    at shift 42, so rounds 1..20 are single-child chains: 2*21+1 = 43 nodes."""
+    from galax_gb300 import Bodies
+    b = Bodies.from_arrays([0.25, 0.75], [0.25, 0.75], [1.0, 2.0])
+    t = _compare_tree(G, oracle, b, 1, (0.0, 1.0, 0.0, 1.0))
+    assert t.n_nodes == 43
+
+
+def test_nonfinite_positions(G, oracle):
+    """NaN/inf positions before sanitising: NaN keys become 0 (Rust `as u64`)."""
+    from galax_gb300 import presets
+    b = presets.uniform(500, seed=2)
+    b.x[3] = np.nan
+    b.y[7] = np.inf
+    b.x[11] = -np.inf
+    _compare_tree(G, oracle, b, 16, presets.BOUNDS["uniform"])
+
+
+@pytest.mark.parametrize("preset,n,n_max", [("uniform", 500, 16), ("plummer", 3000, 16), ("uniform", 4000, 32)])
+def test_balanced_tree(G, oracle, preset, n, n_max):
+    """build_constrained (lib.rs:541-588): no sort, iterative 2:1 split points."""
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=9)
+    # build_constrained assumes Morton-sorted bodies: sort with Tree::build first
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass, b.vx, b.vy)
+    oracle.tree_build(ob, n_max, presets.BOUNDS[preset])
+    from galax_gb300 import Bodies
+    sb = Bodies.from_arrays(ob.x, ob.y, ob.mass, ob.vx, ob.vy)
+    _compare_tree(G, oracle, sb, n_max, presets.BOUNDS[preset], balanced=True)
+
+
+def test_empty(G):
+    from galax_gb300 import Bodies
+    ctx = _ctx(G, 1)
+    ctx.build_tree(Bodies.new(0), 32, (0.0, 1.0, 0.0, 1.0))
+    assert ctx.tree_info()[0] == 0
+    ctx.close()
