@@ -1,0 +1,314 @@
+"""Benchmark: FMM force evaluation at N = 1M Plummer, p = 4, n_max = 32.
+
+Metric (one JSON line on rank 0): bodies/s of one FMM force evaluation of the
+mixed-precision form (FP32 P2M/L2P/P2P, FP32 M2L, FP64 state) in ACCURATE mode
+(near/far lists by the opening angle theta on the reference's Morton tree,
+median relative force error <= 1e-4 against the exact FP64 N^2 sum), with the
+FP64 form and the reference-semantics (REF) FP64 form timed beside it, and the
+force error of each against the FP64 N^2 sum on 1000 seeded sample bodies.
+
+  value      whole-job bodies/s with bodies resident in HBM (CUDA events on the
+             context stream, L2 flushed by a 256 MB write before every step,
+             outside the step's timed interval)
+  e2e        the same through the C ABI call gx_compute_forces with pinned host
+             buffers: each step copies x, y, m host->device and ax, ay back
+  roofline   the dominant kernel (fused L2P+P2P, FP32 pipe): algorithmic FLOPs
+             (14 per body-body interaction) per launch / its event-timed duration,
+             against the FP32 FMA peak measured on this GPU in the same run
+  cpu_baseline  the oracle (C restatement of galax-core's CPU FMM, REF semantics,
+             OpenMP where the reference uses Rayon) on the host cores
+
+``--impl reference`` times the reference's CPU algorithm (the oracle port) on the
+same workload instead.  Multi-GPU: the force evaluation does not shard here, so
+``--gpus N`` runs N independent replicas (weak scaling); timing is the max over
+ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FMM bodies/s (1M, p=4) mixed vs FP64 at equal force error; adjoint/fwd time"
+N_DEFAULT = 1_000_000
+P, N_MAX, THETA = 4, 32, 0.5
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def _barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def _max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self._p = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                        "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                       stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self._p = None
+
+    def _read(self):
+        for line in self._p.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self._p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self._p.terminate()
+        try:
+            self._p.wait(timeout=5)
+        except Exception:
+            self._p.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows if len(r) >= 9 for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def _rel_err(ax, ay, rx, ry):
+    den = np.maximum(np.hypot(rx, ry), 1e-30)
+    return np.hypot(ax - rx, ay - ry) / den
+
+
+def _cpu_baseline(bodies_sorted, bounds, eps, n_evals: int = 2):
+    """The oracle (REF semantics) on the host: full force evaluations of the same workload."""
+    from oracle import oracle as O
+    O.build()
+    ob = O.Bodies.from_arrays(bodies_sorted.x, bodies_sorted.y, bodies_sorted.mass)
+    t = O.tree_build(ob, N_MAX, bounds)
+    v, u = O.vlist_build(t), O.ulist_build(t)
+    times = []
+    for _ in range(n_evals):
+        bb = ob.copy()
+        t0 = time.perf_counter()
+        O.compute_fmm_force(bb, t, v, u, P, eps, O.MODE_REF)
+        times.append(time.perf_counter() - t0)
+    return ob, t, v, u, times, O.get_threads()
+
+
+def run_reference(args, rank, world, pg):
+    """--impl reference: the reference's CPU FMM (oracle port) on the host cores."""
+    if rank != 0:
+        return 0
+    from galax_gb300 import presets
+    from oracle import oracle as O
+    O.build()
+    n = args.n
+    b = presets.plummer(n, seed=args.seed)
+    bounds = presets.BOUNDS["plummer"]
+    ob = O.Bodies.from_arrays(b.x, b.y, b.mass, b.vx, b.vy)
+    t = O.tree_build(ob, N_MAX, bounds)
+    v, u = O.vlist_build(t), O.ulist_build(t)
+    eps = O.cli_softening(ob)
+    for _ in range(args.warmup):
+        bb = ob.copy()
+        O.compute_fmm_force(bb, t, v, u, P, eps, O.MODE_REF)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        bb = ob.copy()
+        O.compute_fmm_force(bb, t, v, u, P, eps, O.MODE_REF)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = n / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "bodies/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Plummer preset)",
+        "config": {"workload": f"plummer N={n}, p={P}, n_max={N_MAX}, REF semantics (galax-core compute_fmm_force)",
+                   "n": n, "p": P, "n_max": N_MAX},
+        "cpu_baseline": {"value": value, "unit": "bodies/s", "cores": O.get_threads(), "kind": "port",
+                         "sample": f"{args.steps} full force evaluations at N={n} (tree and lists built once, "
+                                   f"outside the timed region)"},
+        "e2e": {"value": value, "unit": "bodies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local, pg):
+    import galax_gb300 as G
+    from galax_gb300 import build as gbuild
+    from galax_gb300 import presets
+    gbuild.build()
+    n = args.n
+    bounds = presets.BOUNDS["plummer"]
+    b = presets.plummer(n, seed=args.seed)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=P, eps64=0.1, device=local))
+    gb = b.copy()
+    t0 = time.perf_counter()
+    ctx.build_tree(gb, N_MAX, bounds)
+    setup_tree_s = time.perf_counter() - t0
+    eps = presets.cli_softening(gb.x, gb.y)
+    ctx.set_params(P, eps)
+    ctx.upload_bodies(gb)
+    nn, nl, nlev, _ = ctx.tree_info()
+
+    forms = [("mixed", G.MODE_ACCURATE, G.PREC_MIXED), ("fp64", G.MODE_ACCURATE, G.PREC_FP64),
+             ("ref_fp64", G.MODE_REF, G.PREC_FP64)]
+    res = {}
+    clocks = None
+    for name, mode, prec in forms:
+        ctx.set_mode(mode, prec, THETA)
+        t0 = time.perf_counter()
+        ctx.forces_resident()  # builds the static plan (lists) for this mode once
+        plan_s = time.perf_counter() - t0
+        steps = args.steps if name == "mixed" else max(3, min(args.steps, 5))
+        warm = args.warmup if name == "mixed" else 1
+        ctx.bench_forces(warm, True, 0)
+        sampler = None
+        if name == "mixed" and rank == 0:
+            sampler = ClockSampler(local)
+            sampler.start()
+        _barrier(pg)
+        ms, kms = ctx.bench_forces(steps, True, 0)
+        _barrier(pg)
+        if sampler is not None:
+            clocks = sampler.stop()
+        far, near, inter = ctx.plan_info()
+        bb = G.Bodies.new(n)
+        ctx.download_bodies(bb)
+        res[name] = dict(ms=ms, kms=kms, plan_s=plan_s, far=far, near=near, inter=inter,
+                         launches=ctx.last_launch_count(), passes=ctx.last_timings().tolist(),
+                         ax=bb.ax.copy(), ay=bb.ay.copy(), steps=steps)
+
+    # force error of each form against the exact FP64 N^2 sum (GPU n2 kernel), 1000 seeded samples
+    idx = np.sort(np.random.default_rng(1234).choice(n, min(1000, n), replace=False))
+    ex, ey = ctx.n2_sampled(idx)
+    for name in res:
+        e = _rel_err(res[name]["ax"][idx], res[name]["ay"][idx], ex, ey)
+        res[name]["err_median"] = float(np.median(e))
+        res[name]["err_p99"] = float(np.percentile(e, 99))
+    d = _rel_err(res["mixed"]["ax"], res["mixed"]["ay"], res["fp64"]["ax"], res["fp64"]["ay"])
+
+    # end to end through the C ABI with pinned host buffers (mixed form)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
+    hx, hy, hm, hax, hay = (G.HostArray(n) for _ in range(5))
+    hx.array[:] = gb.x
+    hy.array[:] = gb.y
+    hm.array[:] = gb.mass
+    for _ in range(max(1, args.warmup)):
+        ctx.compute_forces(hx.array, hy.array, hm.array, hax.array, hay.array)
+    _barrier(pg)
+    e2e_t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ctx.compute_forces(hx.array, hy.array, hm.array, hax.array, hay.array)
+        e2e_t.append(time.perf_counter() - t0)
+    _barrier(pg)
+    e2e_ms = _max_over_ranks(pg, float(np.mean(e2e_t)) * 1e3)
+    peak32 = ctx.probe_fp32_tflops()
+
+    mix = res["mixed"]
+    ms_step = _max_over_ranks(pg, float(np.mean(mix["ms"])))
+    kms = float(np.mean(mix["kms"]))
+    flops = 14.0 * mix["inter"]
+    achieved = flops / (kms * 1e-3) / 1e12
+    if rank != 0:
+        ctx.close()
+        return 0
+    cpu = None
+    if not args.no_cpu_baseline:
+        _, _, _, _, times, cores = _cpu_baseline(gb, bounds, eps, n_evals=2)
+        cpu = {"value": n / float(np.median(times)), "unit": "bodies/s", "cores": cores, "kind": "port",
+               "sample": f"2 full REF-mode force evaluations of the same N={n} Plummer workload (C restatement "
+                         f"of galax-core compute_fmm_force, OpenMP in m2l/l2p like the reference's Rayon)"}
+    line = {
+        "metric": METRIC, "value": world * n / (ms_step * 1e-3), "unit": "bodies/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed: FP32 P2M/M2L/L2L/L2P/P2P, FP64 state)",
+        "data": "synthetic (seeded Plummer preset: a=1, r<=10a, equal masses 1/N)",
+        "config": {"workload": f"plummer N={n}, p={P}, n_max={N_MAX}, one force evaluation per step, static tree",
+                   "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "mode": "ACCURATE", "eps": eps,
+                   "l2": "flushed (256 MB write) before every step, outside its timed interval",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "bodies/s", "h2d_bytes_per_step": 3 * 8 * n,
+                "d2h_bytes_per_step": 2 * 8 * n},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                     "frac": achieved / peak32 if peak32 else None, "traffic": None,
+                     "kernel": "k_l2p_p2p32 (fused L2P + P2P)",
+                     "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)"},
+        "gpu_launches": int(sum(r["launches"] * (r["steps"] + 1) for r in res.values())),
+        "clocks": clocks,
+        "forms": {k: {"bodies_per_s": n / (float(np.mean(r["ms"])) * 1e-3), "ms_per_step": float(np.mean(r["ms"])),
+                      "err_median": r["err_median"], "err_p99": r["err_p99"], "plan_s": r["plan_s"],
+                      "far_pairs": r["far"], "near_leaf_pairs": r["near"], "p2p_interactions": r["inter"],
+                      "pass_ms": dict(zip(["total", "prepare", "p2m", "m2m", "m2l", "l2l", "l2p_p2p"], r["passes"]))}
+                  for k, r in res.items()},
+        "mixed_vs_fp64": {"speedup": float(np.mean(res["fp64"]["ms"])) / float(np.mean(mix["ms"])),
+                          "median_rel_diff": float(np.median(d))},
+        "tree": {"nodes": nn, "leaves": nl, "levels": nlev, "build_s_incl_host_copies": setup_tree_s},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local, pg = _dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, rank, world, pg)
+        return run_ours(args, rank, world, local, pg)
+    finally:
+        if pg is not None:
+            pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

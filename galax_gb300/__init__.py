@@ -94,6 +94,7 @@ def lib():
         "gx_last_timings": (C.c_int, [_VP, _D]),
         "gx_bench_forces": (C.c_int, [_VP, C.c_int32, C.c_int32, _D, C.c_int32, _D]),
         "gx_last_launch_count": (C.c_int, [_VP, _I64]),
+        "gx_probe_fp32_tflops": (C.c_int, [_VP, _D]),
         "gx_host_alloc": (_VP, [C.c_size_t]),
         "gx_host_free": (None, [_VP]),
     }
@@ -382,6 +383,11 @@ class GpuContext:
         c = C.c_int64()
         self._check(lib().gx_last_launch_count(self._h, C.byref(c)))
         return c.value
+
+    def probe_fp32_tflops(self) -> float:
+        out = C.c_double()
+        self._check(lib().gx_probe_fp32_tflops(self._h, C.byref(out)))
+        return out.value
 
     def bench_forces(self, reps: int, flush_l2: bool = True, which: int = 0):
         ms = np.zeros(reps)

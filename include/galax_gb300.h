@@ -151,6 +151,10 @@ int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each
 /* Number of kernels the last force evaluation launched. */
 int gx_last_launch_count(gx_ctx *ctx, int64_t *count);
 
+/* FP32 FMA throughput of this GPU in TFLOP/s (best of 5 timed launches of a
+ * kernel of independent FMA chains): the ceiling used for the FP32 P2P pass. */
+int gx_probe_fp32_tflops(gx_ctx *ctx, double *tflops);
+
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost);
  * NULL on failure. */
 void *gx_host_alloc(size_t bytes);
