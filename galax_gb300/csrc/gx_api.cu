@@ -124,7 +124,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->m, &ctx->ax, &ctx->ay, &ctx->vdata, &ctx->vlen, &ctx->udata, &ctx->ulen, &ctx->p2p_off,
                       &ctx->p2p_idx, &ctx->ref_voff, &ctx->ref_did, &ctx->ref_G, &ctx->radius, &ctx->far_off, &ctx->far_idx,
                       &ctx->near_off, &ctx->near_idx, &ctx->M, &ctx->L, &ctx->Lf, &ctx->Mf32, &ctx->Lf32,
-                      &ctx->Lff32, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
+                      &ctx->Lff32, &ctx->pos32, &ctx->part, &ctx->items_ref.leaf, &ctx->items_ref.qb, &ctx->items_ref.nq, &ctx->items_ref.off, &ctx->items_acc.leaf, &ctx->items_acc.qb, &ctx->items_acc.nq, &ctx->items_acc.off, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
                       &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush};
     for (DevBuf *b : bufs) free_buf(*b);
     for (auto &e : ctx->ev)
@@ -230,6 +230,7 @@ int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, doub
     if (ctx->cfg.max_nodes && (uint64_t)ctx->n_nodes > ctx->cfg.max_nodes)
         return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "tree node count exceeds max_nodes");
     GX_TRY(gx_lists_build_ref(ctx));
+    ctx->max_leaf = std::min<int64_t>(n_max, n);
     // Tree::build permutes the caller's arrays (lib.rs:204); so do we.
     if (!(flags & GX_BUILD_BALANCED)) GX_TRY(gx_download_bodies(ctx, x, y, vx, vy, m, ax, ay));
     ctx->have_tree = true;
@@ -304,6 +305,8 @@ int gx_upload_tree(gx_ctx *ctx, int64_t n_nodes, int64_t n_bodies, const double 
     ctx->level_start = n_nodes > 0 ? ls : std::vector<int64_t>(1, 0);
     if (ctx->have_bodies && ctx->n_bodies != n_bodies) ctx->have_bodies = false;
     ctx->n_bodies = n_bodies;
+    ctx->max_leaf = 0;
+    for (int64_t i = 0; i < nl; i++) ctx->max_leaf = std::max(ctx->max_leaf, body_end[i] - body_start[i]);
     ctx->have_tree = true;
     return GX_OK;
 }
@@ -363,9 +366,15 @@ static int ensure_plan(gx_ctx *ctx) {
     if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree: call gx_build_tree or gx_upload_tree first");
     if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no bodies");
     if (ctx->mode == GX_MODE_ACCURATE) {
-        if (!ctx->plan_acc_valid || ctx->plan_theta != ctx->theta) GX_TRY(gx_plan_accurate(ctx));
+        if (!ctx->plan_acc_valid || ctx->plan_theta != ctx->theta) {
+            GX_TRY(gx_plan_accurate(ctx));
+            GX_TRY(gx_plan_items(ctx, true));
+        }
     } else {
-        if (!ctx->plan_ref_valid || ctx->plan_p != ctx->p || ctx->plan_eps != ctx->eps) GX_TRY(gx_plan_ref(ctx));
+        if (!ctx->plan_ref_valid || ctx->plan_p != ctx->p || ctx->plan_eps != ctx->eps) {
+            GX_TRY(gx_plan_ref(ctx));
+            GX_TRY(gx_plan_items(ctx, false));
+        }
     }
     return GX_OK;
 }

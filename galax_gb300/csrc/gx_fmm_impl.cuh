@@ -22,12 +22,30 @@
 
 namespace {
 
-__host__ __device__ constexpr double cfact(int n) { return n <= 1 ? 1.0 : (double)n * cfact(n - 1); }
+// Factorials and binomials: constant-folded when the loops around them are
+// unrolled, evaluated by short loops otherwise.  Deliberately not recursive: a
+// recursive device function has no static stack bound, and with the large local
+// arrays of the high-order kernels that overflows the per-thread stack.
+__host__ __device__ constexpr double cfact(int n) {
+    double r = 1.0;
+    for (int i = 2; i <= n; i++) r *= (double)i;
+    return r;
+}
 __host__ __device__ constexpr double cinvfact(int n) { return 1.0 / cfact(n); }
 __host__ __device__ constexpr double cbinom(int n, int k) {
-    return (k < 0 || k > n) ? 0.0 : ((k == 0 || k == n) ? 1.0 : cbinom(n - 1, k - 1) + cbinom(n - 1, k));
+    if (k < 0 || k > n) return 0.0;
+    double r = 1.0;  // C(n-k+i, i) after step i: every intermediate value is an integer
+    for (int i = 1; i <= k; i++) r = r * (double)(n - k + i) / (double)i;
+    return r;
 }
 __host__ __device__ constexpr int nc2(int q) { return (q + 1) * (q + 2) / 2; }  // entries with k+l <= q
+
+// Loops over expansion indices are fully unrolled (coefficient arrays stay in
+// registers) for orders up to 5; above that the bound is made a runtime value
+// (a zero the compiler cannot see through) so the loops stay rolled and the
+// translation units compile in seconds.
+__constant__ int g_rt_zero = 0;
+__device__ __forceinline__ int gx_rt_order(int P) { return P <= 5 ? P : P + g_rt_zero; }
 
 template <class T>
 __device__ __forceinline__ T warp_sum_t(T v) {
@@ -36,12 +54,53 @@ __device__ __forceinline__ T warp_sum_t(T v) {
     return v;
 }
 
+// FP32 reciprocal square root as the single PTX instruction rsqrt.approx.ftz.f32:
+// the arguments here are r^2 + eps^2 > 0, far from the denormal range, so the
+// denormal handling the library function adds around it is dead weight.
+__device__ __forceinline__ float rsqrt_fast(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 template <class T>
 __device__ __forceinline__ T rsqrt_t(T v);
 template <>
 __device__ __forceinline__ double rsqrt_t<double>(double v) { return rsqrt(v); }
 template <>
-__device__ __forceinline__ float rsqrt_t<float>(float v) { return rsqrtf(v); }
+__device__ __forceinline__ float rsqrt_t<float>(float v) { return rsqrt_fast(v); }
+
+// Expansion rows are padded to a multiple of 16 bytes (16 floats / 16 doubles at
+// p = 4) so that a node's coefficients load as float4 / double2 vectors.
+template <class T>
+__host__ __device__ constexpr int row_stride(int nc) {
+    return sizeof(T) == 4 ? (nc + 3) / 4 * 4 : (nc + 1) / 2 * 2;
+}
+
+template <int N, class T>
+__device__ __forceinline__ void load_row(const T *__restrict__ p, T *out);
+template <int N>
+__device__ __forceinline__ void load_row(const float *__restrict__ p, float *out) {
+    constexpr int NS = row_stride<float>(N);
+#pragma unroll
+    for (int k = 0; k < NS / 4; k++) {
+        float4 v = __ldg(reinterpret_cast<const float4 *>(p) + k);
+        if (4 * k + 0 < N) out[4 * k + 0] = v.x;
+        if (4 * k + 1 < N) out[4 * k + 1] = v.y;
+        if (4 * k + 2 < N) out[4 * k + 2] = v.z;
+        if (4 * k + 3 < N) out[4 * k + 3] = v.w;
+    }
+}
+template <int N>
+__device__ __forceinline__ void load_row(const double *__restrict__ p, double *out) {
+    constexpr int NS = row_stride<double>(N);
+#pragma unroll
+    for (int k = 0; k < NS / 2; k++) {
+        double2 v = __ldg(reinterpret_cast<const double2 *>(p) + k);
+        if (2 * k + 0 < N) out[2 * k + 0] = v.x;
+        if (2 * k + 1 < N) out[2 * k + 1] = v.y;
+    }
+}
 
 // ---------------------------------------------------------------- prepare
 // compute_fmm_force's input sanitising (lib.rs:1474-1482) and the zeroing of a.
@@ -69,80 +128,88 @@ template <int P, class T>
 __global__ void __launch_bounds__(128) k_p2m(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
                                              const double *__restrict__ m, const double *__restrict__ comx,
                                              const double *__restrict__ comy, const int32_t *__restrict__ bs,
-                                             const int32_t *__restrict__ be, T *__restrict__ M) {
+                                             const int32_t *__restrict__ be, T *__restrict__ M,
+                                             float4 *__restrict__ pos) {
     constexpr int NC = nc2(P);
-    constexpr int UF = P <= 5 ? 64 : 1;
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (leaf >= nl) return;
     int32_t b0 = bs[leaf], b1 = be[leaf];
     double cxl = comx[leaf], cyl = comy[leaf];
     T acc[NC];
-#pragma unroll UF
-    for (int k = 0; k < NC; k++) acc[k] = T(0);
+#pragma unroll
+    for (int k = 0; k < NCr; k++) acc[k] = T(0);
     for (int32_t b = b0 + lane; b < b1; b += 32) {
         T dx = (T)(x[b] - cxl), dy = (T)(y[b] - cyl), mm = (T)m[b];
+        if (pos) pos[b] = make_float4((float)dx, (float)dy, (float)m[b], 0.f);
         T px[P + 1], py[P + 1];
         px[0] = T(1);
         py[0] = T(1);
-#pragma unroll UF
-        for (int k = 1; k <= P; k++) {
+#pragma unroll
+        for (int k = 1; k <= PP; k++) {
             px[k] = px[k - 1] * dx;
             py[k] = py[k - 1] * dy;
         }
-#pragma unroll UF
-        for (int i = 0; i <= P; i++)
-#pragma unroll UF
-            for (int j = 0; j <= P - i; j++)
+#pragma unroll
+        for (int i = 0; i <= PP; i++)
+#pragma unroll
+            for (int j = 0; j <= PP - i; j++)
                 acc[gx_mi(i, j)] += mm * px[i] * py[j] * (T)(cinvfact(i) * cinvfact(j));
     }
-#pragma unroll UF
-    for (int k = 0; k < NC; k++) {
+#pragma unroll
+    for (int k = 0; k < NCr; k++) {
         T v = warp_sum_t<T>(acc[k]);
-        if (lane == (k & 31)) M[leaf * NC + k] = isfinite(v) ? v : T(0);
+        if (lane == (k & 31)) M[leaf * NS + k] = isfinite(v) ? v : T(0);
     }
 }
 
 // ---------------------------------------------------------------- M2M
+// One thread per parent: M_P[I,J] = sum_children sum_{i<=I, j<=J} M_c[i,j] dx^(I-i) dy^(J-j) / ((I-i)!(J-j)!)
 template <int P, class T>
 __global__ void __launch_bounds__(128) k_m2m(int64_t s, int64_t e, const int4 *__restrict__ child,
                                              const double *__restrict__ comx, const double *__restrict__ comy,
                                              T *__restrict__ M) {
     constexpr int NC = nc2(P);
-    constexpr int UF = P <= 5 ? 64 : 1;
-    int64_t node = s + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    int lane = threadIdx.x & 31;
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    int64_t node = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= e) return;
     int4 c4 = child[node];
     int cc[4] = {c4.x, c4.y, c4.z, c4.w};
     double pcx = comx[node], pcy = comy[node];
-    for (int o = lane; o < NC; o += 32) {
-        // decode o -> (oi, oj): o = n(n+1)/2 + oj with n = oi + oj
-        int nn = 0;
-        while ((nn + 1) * (nn + 2) / 2 <= o) nn++;
-        int oj = o - nn * (nn + 1) / 2, oi = nn - oj;
-        T sum = T(0);
-        for (int k = 0; k < 4; k++) {
-            int c = cc[k];
-            if (c < 0) continue;
-            T dx = (T)(comx[c] - pcx), dy = (T)(comy[c] - pcy);
-            T px[P + 1], py[P + 1];
-            px[0] = T(1);
-            py[0] = T(1);
-#pragma unroll UF
-            for (int q = 1; q <= P; q++) {
-                px[q] = px[q - 1] * dx;
-                py[q] = py[q - 1] * dy;
-            }
-            const T *Mc = M + (int64_t)c * NC;
-            T part = T(0);
-            for (int i = 0; i <= oi; i++)
-                for (int j = 0; j <= oj; j++)
-                    part += Mc[gx_mi(i, j)] * px[oi - i] * py[oj - j] * (T)(cinvfact(oi - i) * cinvfact(oj - j));
-            sum += part;
+    T out[NC];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) out[k] = T(0);
+    for (int q = 0; q < 4; q++) {
+        int c = cc[q];
+        if (c < 0) continue;
+        T dx = (T)(comx[c] - pcx), dy = (T)(comy[c] - pcy);
+        T px[P + 1], py[P + 1];
+        px[0] = T(1);
+        py[0] = T(1);
+#pragma unroll
+        for (int k = 1; k <= PP; k++) {
+            px[k] = px[k - 1] * dx * (T)(1.0 / k);  // dx^k / k!
+            py[k] = py[k - 1] * dy * (T)(1.0 / k);
         }
-        M[node * NC + o] = sum;
+        T mc[NC];
+        load_row<NC>(M + (int64_t)c * NS, mc);
+#pragma unroll
+        for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+            for (int oj = 0; oj <= PP - oi; oj++)
+#pragma unroll
+                for (int i = 0; i <= oi; i++)
+#pragma unroll
+                    for (int j = 0; j <= oj; j++) out[gx_mi(oi, oj)] += mc[gx_mi(i, j)] * px[oi - i] * py[oj - j];
     }
+#pragma unroll
+    for (int k = 0; k < NCr; k++) M[node * NS + k] = out[k];
 }
 
 template <class T>
@@ -157,15 +224,17 @@ __global__ void k_scrub(int64_t n, T *v) {
 // The kernel of the reference is G = -1/R, so G^(k,l) = -A[k,l].
 template <int P, class T>
 __device__ __forceinline__ void derivs_scaled(T dx, T dy, T eps2, T *A) {
-    constexpr int Q = 2 * P;
-    constexpr int UF = P <= 5 ? 64 : 1;
+    const int PP = gx_rt_order(P);
+    const int Q = 2 * PP;
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
     T r2 = dx * dx + dy * dy + eps2;
     T ir = rsqrt_t<T>(r2);
     T ir2 = ir * ir;
     A[0] = ir;
-#pragma unroll UF
+#pragma unroll
     for (int n = 1; n <= Q; n++) {
-#pragma unroll UF
+#pragma unroll
         for (int k = 0; k <= n; k++) {
             int l = n - k;
             T s1 = T(0), s2 = T(0);
@@ -186,43 +255,44 @@ __global__ void __launch_bounds__(128) k_m2l_ref(int64_t nn, const uint32_t *__r
                                                  const int32_t *__restrict__ did, const double *__restrict__ G,
                                                  const double *__restrict__ M, double *__restrict__ L) {
     constexpr int NC = nc2(P);
-    constexpr int UF = P <= 5 ? 64 : 1;
+    constexpr int NS = row_stride<double>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
     constexpr int S = 2 * P + 1;
     int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (node >= nn) return;
     int len = vlen[node];
     double acc[NC];
-#pragma unroll UF
-    for (int k = 0; k < NC; k++) acc[k] = 0.0;
+#pragma unroll
+    for (int k = 0; k < NCr; k++) acc[k] = 0.0;
     for (int s = lane; s < len; s += 32) {
         uint32_t src = vdata[node * GX_LIST_CAP + s];
         const double *g = G + (int64_t)did[voff[node] + s] * (S * S);
-        const double *Ms = M + (int64_t)src * NC;
         double ms[NC];
-#pragma unroll UF
-        for (int k = 0; k < NC; k++) ms[k] = Ms[k];
-#pragma unroll UF
-        for (int i = 0; i <= P; i++)
-#pragma unroll UF
-            for (int j = 0; j <= P - i; j++) {
+        load_row<NC>(M + (int64_t)src * NS, ms);
+#pragma unroll
+        for (int i = 0; i <= PP; i++)
+#pragma unroll
+            for (int j = 0; j <= PP - i; j++) {
                 double mv = ms[gx_mi(i, j)];
                 if (mv == 0.0) continue;  // lib.rs:1252: zero source terms are skipped
                 double sm = ((i + j) & 1) ? -mv : mv;
-#pragma unroll UF
-                for (int oi = 0; oi <= P; oi++)
-#pragma unroll UF
-                    for (int oj = 0; oj <= P - oi; oj++)
+#pragma unroll
+                for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+                    for (int oj = 0; oj <= PP - oi; oj++)
                         acc[gx_mi(oi, oj)] += sm * g[gx_kdi(i + oi, j + oj, P)];
             }
     }
-#pragma unroll UF
-    for (int oi = 0; oi <= P; oi++)
-#pragma unroll UF
-        for (int oj = 0; oj <= P - oi; oj++) {
+#pragma unroll
+    for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+        for (int oj = 0; oj <= PP - oi; oj++) {
             int k = gx_mi(oi, oj);
             double v = warp_sum_t<double>(acc[k]);
-            if (lane == (k & 31)) L[node * NC + k] = v * (cinvfact(oi) * cinvfact(oj));
+            if (lane == (k & 31)) L[node * NS + k] = v * (cinvfact(oi) * cinvfact(oj));
         }
 }
 
@@ -234,7 +304,10 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
                                                    const double *__restrict__ comx, const double *__restrict__ comy,
                                                    double eps2d, const T *__restrict__ M, T *__restrict__ L) {
     constexpr int NC = nc2(P);
-    constexpr int UF = P <= 5 ? 64 : 1;
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
     constexpr int ND = nc2(2 * P);
     int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
@@ -244,47 +317,64 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
     double tcx = comx[node], tcy = comy[node];
     T eps2 = (T)eps2d;
     T acc[NC];
-#pragma unroll UF
-    for (int k = 0; k < NC; k++) acc[k] = T(0);
+#pragma unroll
+    for (int k = 0; k < NCr; k++) acc[k] = T(0);
     for (int s = lane; s < len; s += 32) {
         int64_t src = (int64_t)idx[st + s];
         T dx = (T)(tcx - comx[src]), dy = (T)(tcy - comy[src]);
         T A[ND];
         derivs_scaled<P, T>(dx, dy, eps2, A);
-        const T *Ms = M + src * NC;
         T ms[NC];
-#pragma unroll UF
-        for (int k = 0; k < NC; k++) ms[k] = Ms[k];
-#pragma unroll UF
-        for (int i = 0; i <= P; i++)
-#pragma unroll UF
-            for (int j = 0; j <= P - i; j++) {
+        load_row<NC>(M + src * NS, ms);
+#pragma unroll
+        for (int i = 0; i <= PP; i++)
+#pragma unroll
+            for (int j = 0; j <= PP - i; j++) {
                 T sm = ((i + j) & 1) ? -ms[gx_mi(i, j)] : ms[gx_mi(i, j)];
-#pragma unroll UF
-                for (int oi = 0; oi <= P; oi++)
-#pragma unroll UF
-                    for (int oj = 0; oj <= P - oi; oj++) acc[gx_mi(oi, oj)] += sm * A[gx_mi(i + oi, j + oj)];
+#pragma unroll
+                for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+                    for (int oj = 0; oj <= PP - oi; oj++) acc[gx_mi(oi, oj)] += sm * A[gx_mi(i + oi, j + oj)];
             }
     }
     // G = -A: L[T] = -(1/T!) sum_S M'[S] A[S+T]
-#pragma unroll UF
-    for (int oi = 0; oi <= P; oi++)
-#pragma unroll UF
-        for (int oj = 0; oj <= P - oi; oj++) {
+#pragma unroll
+    for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+        for (int oj = 0; oj <= PP - oi; oj++) {
             int k = gx_mi(oi, oj);
             T v = warp_sum_t<T>(acc[k]);
-            if (lane == (k & 31)) L[node * NC + k] = v * (T)(-cinvfact(oi) * cinvfact(oj));
+            if (lane == (k & 31)) L[node * NS + k] = v * (T)(-cinvfact(oi) * cinvfact(oj));
         }
 }
 
 // ---------------------------------------------------------------- L2L
+// L_c[I,J] += sum_{i>=I, j>=J} L_P[i,j] C(i,I) C(j,J) dx^(i-I) dy^(j-J), one thread per child.
 template <int P, class T>
-__device__ __forceinline__ T l2l_term(const T *LP, int oi, int oj, const T *px, const T *py) {
-    T sum = T(0);
-    for (int i = oi; i <= P; i++)
-        for (int j = oj; j <= P - i; j++)
-            sum += LP[gx_mi(i, j)] * (T)(cbinom(i, oi) * cbinom(j, oj)) * px[i - oi] * py[j - oj];
-    return sum;
+__device__ __forceinline__ void l2l_shift(const T *__restrict__ LP, T dx, T dy, T *out) {
+    const int PP = gx_rt_order(P);
+    T px[P + 1], py[P + 1];
+    px[0] = T(1);
+    py[0] = T(1);
+#pragma unroll
+    for (int q = 1; q <= PP; q++) {
+        px[q] = px[q - 1] * dx;
+        py[q] = py[q - 1] * dy;
+    }
+    T lp[nc2(P)];
+    load_row<nc2(P)>(LP, lp);
+#pragma unroll
+    for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+        for (int oj = 0; oj <= PP - oi; oj++) {
+            T sum = T(0);
+#pragma unroll
+            for (int i = oi; i <= PP; i++)
+#pragma unroll
+                for (int j = oj; j <= PP - i; j++)
+                    sum += lp[gx_mi(i, j)] * (T)(cbinom(i, oi) * cbinom(j, oj)) * px[i - oi] * py[j - oj];
+            out[gx_mi(oi, oj)] += sum;
+        }
 }
 
 // REF: Lout[leaf] = L[leaf] + shift(L[parent(leaf)])
@@ -293,28 +383,19 @@ __global__ void __launch_bounds__(128) k_l2l_ref_leaves(int64_t nl, const int32_
                                                         const double *__restrict__ comx, const double *__restrict__ comy,
                                                         const T *__restrict__ L, T *__restrict__ Lout) {
     constexpr int NC = nc2(P);
-    int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    int64_t leaf = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (leaf >= nl) return;
     int32_t par = parent[leaf];
-    T px[P + 1], py[P + 1];
-    px[0] = T(1);
-    py[0] = T(1);
-    if (par >= 0) {
-        T dx = (T)(comx[leaf] - comx[par]), dy = (T)(comy[leaf] - comy[par]);
-        for (int q = 1; q <= P; q++) {
-            px[q] = px[q - 1] * dx;
-            py[q] = py[q - 1] * dy;
-        }
-    }
-    for (int o = lane; o < NC; o += 32) {
-        int nn = 0;
-        while ((nn + 1) * (nn + 2) / 2 <= o) nn++;
-        int oj = o - nn * (nn + 1) / 2, oi = nn - oj;
-        T v = L[leaf * NC + o];
-        if (par >= 0) v += l2l_term<P, T>(L + (int64_t)par * NC, oi, oj, px, py);
-        Lout[leaf * NC + o] = v;
-    }
+    T out[NC];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) out[k] = L[leaf * NS + k];
+    if (par >= 0)
+        l2l_shift<P, T>(L + (int64_t)par * NS, (T)(comx[leaf] - comx[par]), (T)(comy[leaf] - comy[par]), out);
+#pragma unroll
+    for (int k = 0; k < NCr; k++) Lout[leaf * NS + k] = out[k];
 }
 
 // top-down: L[x] += shift(L[parent(x)]) for the nodes of one level
@@ -323,175 +404,286 @@ __global__ void __launch_bounds__(128) k_l2l_level(int64_t s, int64_t e, const i
                                                    const double *__restrict__ comx, const double *__restrict__ comy,
                                                    T *__restrict__ L) {
     constexpr int NC = nc2(P);
-    int64_t x = s + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    int lane = threadIdx.x & 31;
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= e) return;
     int32_t par = parent[x];
     if (par < 0) return;
-    T px[P + 1], py[P + 1];
-    px[0] = T(1);
-    py[0] = T(1);
-    T dx = (T)(comx[x] - comx[par]), dy = (T)(comy[x] - comy[par]);
-    for (int q = 1; q <= P; q++) {
-        px[q] = px[q - 1] * dx;
-        py[q] = py[q - 1] * dy;
-    }
-    for (int o = lane; o < NC; o += 32) {
-        int nn = 0;
-        while ((nn + 1) * (nn + 2) / 2 <= o) nn++;
-        int oj = o - nn * (nn + 1) / 2, oi = nn - oj;
-        L[x * NC + o] += l2l_term<P, T>(L + (int64_t)par * NC, oi, oj, px, py);
-    }
+    T out[NC];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) out[k] = L[x * NS + k];
+    l2l_shift<P, T>(L + (int64_t)par * NS, (T)(comx[x] - comx[par]), (T)(comy[x] - comy[par]), out);
+#pragma unroll
+    for (int k = 0; k < NCr; k++) L[x * NS + k] = out[k];
 }
 
 // ---------------------------------------------------------------- L2P + P2P
-// FP64: a_i = -grad(local) + sum_j m_j (x_j - x_i) / (r^2+eps^2)^(3/2)
-template <int P>
-__global__ void __launch_bounds__(128) k_l2p_p2p64(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
-                                                   const double *__restrict__ m, const double *__restrict__ comx,
-                                                   const double *__restrict__ comy, const int32_t *__restrict__ bs,
-                                                   const int32_t *__restrict__ be, const double *__restrict__ Lf,
-                                                   const int64_t *__restrict__ off, const int32_t *__restrict__ cnt,
-                                                   const int32_t *__restrict__ src_idx, double eps2,
-                                                   double *__restrict__ ax, double *__restrict__ ay) {
-    constexpr int NC = nc2(P);
-    constexpr int UF = P <= 5 ? 64 : 1;
-    __shared__ double sx[4][32], sy[4][32], sm[4][32];
+// One warp per target leaf, one lane per target body (chunks of 32 for larger
+// leaves).  The source-leaf list is read 32 entries at a time (one coalesced load)
+// and broadcast by shuffles; each source leaf (<= 32 bodies) is loaded one body per
+// lane, staged in shared memory and read back as a broadcast, and the next leaf's
+// load is issued before the current leaf is computed, so its latency is hidden.
+// The target leaf itself is handled in a separate branch (i == j is skipped there),
+// keeping the common loop free of the self test.
+
+// L2P (lib.rs:1321-1345) for one body at (du, dv) from the leaf COM
+template <int P, class T>
+__device__ __forceinline__ void l2p_eval(const T *__restrict__ Ll, T du, T dv, T &fx, T &fy) {
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
+    T px[P + 1], py[P + 1];
+    px[0] = T(1);
+    py[0] = T(1);
+#pragma unroll
+    for (int q = 1; q <= PP; q++) {
+        px[q] = px[q - 1] * du;
+        py[q] = py[q - 1] * dv;
+    }
+    fx = T(0);
+    fy = T(0);
+#pragma unroll
+    for (int a = 0; a <= PP; a++)
+#pragma unroll
+        for (int b = 0; b <= PP - a; b++) {
+            T c = Ll[gx_mi(a, b)];
+            if (a >= 1) fx += c * (T)a * px[a - 1] * py[b];
+            if (b >= 1) fy += c * (T)b * px[a] * py[b - 1];
+        }
+}
+
+// Work items: the source list of every target leaf is cut into items of at most
+// P2P_K source leaves; one warp per item writes per-body partial accelerations to
+// its own slot, so the work per warp is bounded however uneven the lists are
+// (Plummer core leaves have hundreds of near leaves, halo leaves a few).  A second
+// kernel evaluates L2P and adds the partials of each leaf in item order, so the
+// result does not depend on scheduling.
+
+// FP64 partials: sum_j m_j (x_j - x_i) / (r^2+eps^2)^(3/2)
+__global__ void __launch_bounds__(128) k_p2p64_items(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                     const int64_t *__restrict__ item_qb, const int32_t *__restrict__ item_nq,
+                                                     const double *__restrict__ x, const double *__restrict__ y,
+                                                     const double *__restrict__ m, const int32_t *__restrict__ bs,
+                                                     const int32_t *__restrict__ be, const int32_t *__restrict__ src_idx,
+                                                     double eps2, int tchunks, double2 *__restrict__ part) {
+    __shared__ double3 sb[4][32];
     int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (leaf >= nl) return;
+    int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (it >= n_items) return;
+    int32_t leaf = item_leaf[it];
+    int64_t qb = item_qb[it];
+    int nq = item_nq[it];
     int32_t t0 = bs[leaf], t1 = be[leaf];
-    double lcx = comx[leaf], lcy = comy[leaf];
-    const double *Ll = Lf + leaf * NC;
-    int64_t q0 = off[leaf];
-    int64_t q1 = cnt ? q0 + cnt[leaf] : off[leaf + 1];
-    for (int32_t tc = t0; tc < t1; tc += 32) {
-        int32_t i = tc + lane;
+    int sl = lane < nq ? src_idx[qb + lane] : -1;
+    int sbeg = sl >= 0 ? bs[sl] : 0, send = sl >= 0 ? be[sl] : 0;
+    auto fetch = [&](int k, int sc) -> double3 {
+        int s0 = __shfl_sync(0xffffffffu, sbeg, k) + sc, s1 = __shfl_sync(0xffffffffu, send, k);
+        int j = s0 + lane;
+        return (j < s1) ? make_double3(x[j], y[j], m[j]) : make_double3(0.0, 0.0, 0.0);
+    };
+    for (int tc = 0; tc < tchunks; tc++) {
+        int32_t i = t0 + tc * 32 + lane;
         bool valid = i < t1;
         double xi = valid ? x[i] : 0.0, yi = valid ? y[i] : 0.0;
-        // L2P (lib.rs:1321-1345)
-        double fx = 0.0, fy = 0.0;
-        {
-            double du = xi - lcx, dv = yi - lcy;
-            double px[P + 1], py[P + 1];
-            px[0] = 1.0;
-            py[0] = 1.0;
-#pragma unroll UF
-            for (int q = 1; q <= P; q++) {
-                px[q] = px[q - 1] * du;
-                py[q] = py[q - 1] * dv;
-            }
-#pragma unroll UF
-            for (int a = 0; a <= P; a++)
-#pragma unroll UF
-                for (int b = 0; b <= P - a; b++) {
-                    double c = Ll[gx_mi(a, b)];
-                    if (a >= 1) fx += c * (double)a * px[a - 1] * py[b];
-                    if (b >= 1) fy += c * (double)b * px[a] * py[b - 1];
-                }
-        }
-        double accx = -fx, accy = -fy;
-        for (int64_t q = q0; q < q1; q++) {
-            int32_t sl = src_idx[q];
-            int32_t s0 = bs[sl], s1 = be[sl];
-            for (int32_t sc = s0; sc < s1; sc += 32) {
-                int32_t j = sc + lane;
-                __syncwarp();
-                if (j < s1) {
-                    sx[w][lane] = x[j];
-                    sy[w][lane] = y[j];
-                    sm[w][lane] = m[j];
-                }
-                __syncwarp();
-                int nsrc = min(32, s1 - sc);
-                for (int k = 0; k < nsrc; k++) {
-                    double dx = sx[w][k] - xi, dy = sy[w][k] - yi;
-                    double r2 = dx * dx + dy * dy + eps2;
-                    double ir = rsqrt(r2);
-                    double f = sm[w][k] * (ir * ir * ir);
-                    if (sc + k == i) f = 0.0;
-                    accx += f * dx;
-                    accy += f * dy;
+        double accx = 0.0, accy = 0.0;
+        if (t0 + tc * 32 < t1) {
+            double3 cur = fetch(0, 0);
+            for (int k = 0; k < nq; k++) {
+                int s0 = __shfl_sync(0xffffffffu, sbeg, k), s1 = __shfl_sync(0xffffffffu, send, k);
+                int srcl = __shfl_sync(0xffffffffu, sl, k);
+                for (int sc = 0; sc < s1 - s0; sc += 32) {
+                    double3 nxt;
+                    if (sc + 32 < s1 - s0) nxt = fetch(k, sc + 32);
+                    else nxt = (k + 1 < nq) ? fetch(k + 1, 0) : make_double3(0.0, 0.0, 0.0);
+                    __syncwarp();
+                    sb[w][lane] = cur;
+                    __syncwarp();
+                    int ns = min(32, s1 - s0 - sc);
+                    if (srcl == leaf) {
+                        for (int kk = 0; kk < ns; kk++) {
+                            double3 bb = sb[w][kk];
+                            double dx = bb.x - xi, dy = bb.y - yi;
+                            double ir = rsqrt(dx * dx + dy * dy + eps2);
+                            double f = bb.z * (ir * ir * ir);
+                            if (s0 + sc + kk == i) f = 0.0;
+                            accx += f * dx;
+                            accy += f * dy;
+                        }
+                    } else {
+#pragma unroll 4
+                        for (int kk = 0; kk < ns; kk++) {
+                            double3 bb = sb[w][kk];
+                            double dx = bb.x - xi, dy = bb.y - yi;
+                            double ir = rsqrt(dx * dx + dy * dy + eps2);
+                            double f = bb.z * (ir * ir * ir);
+                            accx += f * dx;
+                            accy += f * dy;
+                        }
+                    }
+                    cur = nxt;
                 }
             }
         }
-        if (valid) {
-            ax[i] = accx;
-            ay[i] = accy;
-        }
+        part[(it * tchunks + tc) * 32 + lane] = make_double2(accx, accy);
     }
 }
 
-// MIXED: FP32 arithmetic on coordinates relative to the target leaf's COM
-// (offsets formed in FP64, rounded once), FP32 accumulation, FP64 result.
-template <int P>
-__global__ void __launch_bounds__(128) k_l2p_p2p32(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
-                                                   const double *__restrict__ m, const double *__restrict__ comx,
-                                                   const double *__restrict__ comy, const int32_t *__restrict__ bs,
-                                                   const int32_t *__restrict__ be, const float *__restrict__ Lf,
-                                                   const int64_t *__restrict__ off, const int32_t *__restrict__ cnt,
-                                                   const int32_t *__restrict__ src_idx, float eps2,
-                                                   double *__restrict__ ax, double *__restrict__ ay) {
-    constexpr int NC = nc2(P);
-    constexpr int UF = P <= 5 ? 64 : 1;
+// FP32 partials on coordinates relative to the target leaf's COM.  Bodies come packed
+// as (x - com_leaf, y - com_leaf, m) in FP32 (written by P2M); a source leaf is moved
+// into the target's frame by one FP32 shift per leaf pair, formed in FP64 and rounded once.
+__global__ void __launch_bounds__(128) k_p2p32_items(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                     const int64_t *__restrict__ item_qb, const int32_t *__restrict__ item_nq,
+                                                     const float4 *__restrict__ pos, const double *__restrict__ comx,
+                                                     const double *__restrict__ comy, const int32_t *__restrict__ bs,
+                                                     const int32_t *__restrict__ be, const int32_t *__restrict__ src_idx,
+                                                     float eps2, int tchunks, float2 *__restrict__ part) {
     __shared__ float4 sb[4][32];
     int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (it >= n_items) return;
+    int32_t leaf = item_leaf[it];
+    int64_t qb = item_qb[it];
+    int nq = item_nq[it];
+    int32_t t0 = bs[leaf], t1 = be[leaf];
+    double tcx = comx[leaf], tcy = comy[leaf];
+    int sl = lane < nq ? src_idx[qb + lane] : -1;
+    int sbeg = 0, send = 0;
+    float shx = 0.f, shy = 0.f;
+    if (sl >= 0) {
+        sbeg = bs[sl];
+        send = be[sl];
+        shx = (float)(comx[sl] - tcx);
+        shy = (float)(comy[sl] - tcy);
+    }
+    auto fetch = [&](int k, int sc) -> float4 {
+        int s0 = __shfl_sync(0xffffffffu, sbeg, k) + sc, s1 = __shfl_sync(0xffffffffu, send, k);
+        float gx = __shfl_sync(0xffffffffu, shx, k), gy = __shfl_sync(0xffffffffu, shy, k);
+        int j = s0 + lane;
+        float4 v = (j < s1) ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        v.x += gx;
+        v.y += gy;
+        return v;
+    };
+    for (int tc = 0; tc < tchunks; tc++) {
+        int32_t i = t0 + tc * 32 + lane;
+        bool valid = i < t1;
+        float4 me = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float xi = me.x, yi = me.y;
+        float ax0 = 0.f, ay0 = 0.f, ax1 = 0.f, ay1 = 0.f;
+        if (t0 + tc * 32 < t1) {
+            float4 cur = fetch(0, 0);
+            for (int k = 0; k < nq; k++) {
+                int s0 = __shfl_sync(0xffffffffu, sbeg, k), s1 = __shfl_sync(0xffffffffu, send, k);
+                int srcl = __shfl_sync(0xffffffffu, sl, k);
+                for (int sc = 0; sc < s1 - s0; sc += 32) {
+                    float4 nxt;
+                    if (sc + 32 < s1 - s0) nxt = fetch(k, sc + 32);
+                    else nxt = (k + 1 < nq) ? fetch(k + 1, 0) : make_float4(0.f, 0.f, 0.f, 0.f);
+                    __syncwarp();
+                    sb[w][lane] = cur;
+                    __syncwarp();
+                    int ns = min(32, s1 - s0 - sc);
+                    if (srcl == leaf) {
+                        for (int kk = 0; kk < ns; kk++) {
+                            float4 bb = sb[w][kk];
+                            float dx = bb.x - xi, dy = bb.y - yi;
+                            float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                            float f = bb.z * (ir * ir * ir);
+                            f = (s0 + sc + kk == i) ? 0.f : f;
+                            ax0 = fmaf(f, dx, ax0);
+                            ay0 = fmaf(f, dy, ay0);
+                        }
+                    } else if (ns == 32) {
+#pragma unroll 8
+                        for (int kk = 0; kk < 32; kk += 2) {
+                            float4 b0 = sb[w][kk], b1 = sb[w][kk + 1];
+                            float dx0 = b0.x - xi, dy0 = b0.y - yi, dx1 = b1.x - xi, dy1 = b1.y - yi;
+                            float ir0 = rsqrt_fast(fmaf(dx0, dx0, fmaf(dy0, dy0, eps2)));
+                            float ir1 = rsqrt_fast(fmaf(dx1, dx1, fmaf(dy1, dy1, eps2)));
+                            float f0 = b0.z * (ir0 * ir0 * ir0), f1 = b1.z * (ir1 * ir1 * ir1);
+                            ax0 = fmaf(f0, dx0, ax0);
+                            ay0 = fmaf(f0, dy0, ay0);
+                            ax1 = fmaf(f1, dx1, ax1);
+                            ay1 = fmaf(f1, dy1, ay1);
+                        }
+                    } else {
+                        for (int kk = 0; kk < ns; kk++) {
+                            float4 bb = sb[w][kk];
+                            float dx = bb.x - xi, dy = bb.y - yi;
+                            float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                            float f = bb.z * (ir * ir * ir);
+                            ax0 = fmaf(f, dx, ax0);
+                            ay0 = fmaf(f, dy, ay0);
+                        }
+                    }
+                    cur = nxt;
+                }
+            }
+        }
+        part[(it * tchunks + tc) * 32 + lane] = make_float2(ax0 + ax1, ay0 + ay1);
+    }
+}
+
+// L2P (lib.rs:1321-1345) + the ordered sum of the leaf's P2P partials:  a = -grad(local) + near
+template <int P>
+__global__ void __launch_bounds__(128) k_l2p_reduce64(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
+                                                      const double *__restrict__ comx, const double *__restrict__ comy,
+                                                      const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                                      const double *__restrict__ Lf, const int64_t *__restrict__ item_off,
+                                                      int tchunks, const double2 *__restrict__ part,
+                                                      double *__restrict__ ax, double *__restrict__ ay) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<double>(NC);
+    int lane = threadIdx.x & 31;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nl) return;
     int32_t t0 = bs[leaf], t1 = be[leaf];
-    double lcx = comx[leaf], lcy = comy[leaf];
-    const float *Ll = Lf + leaf * NC;
-    int64_t q0 = off[leaf];
-    int64_t q1 = cnt ? q0 + cnt[leaf] : off[leaf + 1];
-    for (int32_t tc = t0; tc < t1; tc += 32) {
-        int32_t i = tc + lane;
-        bool valid = i < t1;
-        float xi = valid ? (float)(x[i] - lcx) : 0.f, yi = valid ? (float)(y[i] - lcy) : 0.f;
-        float fx = 0.f, fy = 0.f;
-        {
-            float px[P + 1], py[P + 1];
-            px[0] = 1.f;
-            py[0] = 1.f;
-#pragma unroll UF
-            for (int q = 1; q <= P; q++) {
-                px[q] = px[q - 1] * xi;
-                py[q] = py[q - 1] * yi;
-            }
-#pragma unroll UF
-            for (int a = 0; a <= P; a++)
-#pragma unroll UF
-                for (int b = 0; b <= P - a; b++) {
-                    float c = Ll[gx_mi(a, b)];
-                    if (a >= 1) fx += c * (float)a * px[a - 1] * py[b];
-                    if (b >= 1) fy += c * (float)b * px[a] * py[b - 1];
-                }
+    int64_t i0 = item_off[leaf], i1 = item_off[leaf + 1];
+    for (int tc = 0; tc < tchunks && t0 + tc * 32 < t1; tc++) {
+        int32_t i = t0 + tc * 32 + lane;
+        if (i >= t1) continue;
+        double fx, fy;
+        l2p_eval<P, double>(Lf + leaf * NS, x[i] - comx[leaf], y[i] - comy[leaf], fx, fy);
+        double sx = -fx, sy = -fy;
+        for (int64_t it = i0; it < i1; it++) {
+            double2 v = part[(it * tchunks + tc) * 32 + lane];
+            sx += v.x;
+            sy += v.y;
         }
-        float accx = 0.f, accy = 0.f;
-        for (int64_t q = q0; q < q1; q++) {
-            int32_t sl = src_idx[q];
-            int32_t s0 = bs[sl], s1 = be[sl];
-            for (int32_t sc = s0; sc < s1; sc += 32) {
-                int32_t j = sc + lane;
-                __syncwarp();
-                if (j < s1) sb[w][lane] = make_float4((float)(x[j] - lcx), (float)(y[j] - lcy), (float)m[j], 0.f);
-                __syncwarp();
-                int nsrc = min(32, s1 - sc);
-                for (int k = 0; k < nsrc; k++) {
-                    float4 b = sb[w][k];
-                    float dx = b.x - xi, dy = b.y - yi;
-                    float r2 = fmaf(dx, dx, fmaf(dy, dy, eps2));
-                    float ir = rsqrtf(r2);
-                    float f = b.z * (ir * ir * ir);
-                    f = (sc + k == i) ? 0.f : f;
-                    accx = fmaf(f, dx, accx);
-                    accy = fmaf(f, dy, accy);
-                }
-            }
+        ax[i] = sx;
+        ay[i] = sy;
+    }
+}
+
+template <int P>
+__global__ void __launch_bounds__(128) k_l2p_reduce32(int64_t nl, const float4 *__restrict__ pos,
+                                                      const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                                      const float *__restrict__ Lf, const int64_t *__restrict__ item_off,
+                                                      int tchunks, const float2 *__restrict__ part,
+                                                      double *__restrict__ ax, double *__restrict__ ay) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<float>(NC);
+    int lane = threadIdx.x & 31;
+    int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (leaf >= nl) return;
+    int32_t t0 = bs[leaf], t1 = be[leaf];
+    int64_t i0 = item_off[leaf], i1 = item_off[leaf + 1];
+    for (int tc = 0; tc < tchunks && t0 + tc * 32 < t1; tc++) {
+        int32_t i = t0 + tc * 32 + lane;
+        if (i >= t1) continue;
+        float4 me = pos[i];
+        float fx, fy;
+        l2p_eval<P, float>(Lf + leaf * NS, me.x, me.y, fx, fy);
+        double sx = -(double)fx, sy = -(double)fy;
+        for (int64_t it = i0; it < i1; it++) {
+            float2 v = part[(it * tchunks + tc) * 32 + lane];
+            sx += (double)v.x;
+            sy += (double)v.y;
         }
-        if (valid) {
-            ax[i] = (double)accx - (double)fx;
-            ay[i] = (double)accy - (double)fy;
-        }
+        ax[i] = sx;
+        ay[i] = sy;
     }
 }
 
@@ -521,131 +713,111 @@ int run_forces(gx_ctx *ctx, bool timed) {
     tm.mark();  // 1
     if (nn == 0) {
         GX_CUDA(ctx, cudaGetLastError());
+        ctx->last_launches = ctx->launches - launches0;
         return GX_OK;
     }
     const double *X = dptr<double>(ctx->x), *Y = dptr<double>(ctx->y), *Mb = dptr<double>(ctx->m);
     const double *comx = dptr<double>(ctx->comx), *comy = dptr<double>(ctx->comy);
     const int32_t *bs = dptr<int32_t>(ctx->bs), *be = dptr<int32_t>(ctx->be), *parent = dptr<int32_t>(ctx->parent);
     const int4 *child = dptr<int4>(ctx->child);
-    const unsigned gw = (unsigned)((nl * 32 + 127) / 128);
+    const unsigned gw = (unsigned)((nl * 32 + 127) / 128);  // warp per leaf
     const double eps2 = ctx->eps * ctx->eps;
+    const gx_ctx::Items &I = mode == GX_MODE_ACCURATE ? ctx->items_acc : ctx->items_ref;
+    const int tchunks = (int)std::max<int64_t>(1, (ctx->max_leaf + 31) / 32);
+    const int32_t *src_idx = mode == GX_MODE_ACCURATE ? dptr<int32_t>(ctx->near_idx) : dptr<int32_t>(ctx->p2p_idx);
+    const unsigned gi = (unsigned)((I.n * 32 + 127) / 128);  // warp per item
 
-    if (!mixed) {
-        GX_TRY(gx_ensure(ctx, ctx->M, sizeof(double) * NC * (size_t)nn));
-        GX_TRY(gx_ensure(ctx, ctx->L, sizeof(double) * NC * (size_t)nn));
-        GX_TRY(gx_ensure(ctx, ctx->Lf, sizeof(double) * NC * (size_t)nl));
-        double *M = dptr<double>(ctx->M), *L = dptr<double>(ctx->L), *Lf = dptr<double>(ctx->Lf);
-        k_p2m<P, double><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, M);
+    auto passes = [&](auto tag) -> int {
+        using T = decltype(tag);
+        DevBuf &Mb_ = mixed ? ctx->Mf32 : ctx->M;
+        DevBuf &Lb_ = mixed ? ctx->Lf32 : ctx->L;
+        DevBuf &Lfb_ = mixed ? ctx->Lff32 : ctx->Lf;
+        constexpr int NS = row_stride<T>(NC);
+        GX_TRY(gx_ensure(ctx, Mb_, sizeof(T) * NS * (size_t)nn));
+        GX_TRY(gx_ensure(ctx, Lb_, sizeof(T) * NS * (size_t)nn));
+        GX_TRY(gx_ensure(ctx, Lfb_, sizeof(T) * NS * (size_t)nl));
+        T *M = dptr<T>(Mb_), *L = dptr<T>(Lb_), *Lf = dptr<T>(Lfb_);
+        float4 *pos = nullptr;
+        if (mixed) {
+            GX_TRY(gx_ensure(ctx, ctx->pos32, sizeof(float4) * (size_t)n));
+            pos = dptr<float4>(ctx->pos32);
+        }
+        // P2M (+ FP32 body packing in the mixed form)
+        k_p2m<P, T><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, M, pos);
         ctx->launches++;
         tm.mark();  // 2
+        // M2M, bottom-up by level
         for (int lv = 1; lv < ctx->n_levels; lv++) {
             int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
-            k_m2m<P, double><<<(unsigned)(((e - s) * 32 + 127) / 128), 128, 0, st>>>(s, e, child, comx, comy, M);
+            k_m2m<P, T><<<gx_blocks(e - s, 128), 128, 0, st>>>(s, e, child, comx, comy, M);
             ctx->launches++;
         }
         if (ctx->n_levels > 1) {
-            k_scrub<double><<<gx_blocks(NC * nn, 256), 256, 0, st>>>(NC * nn, M);
+            k_scrub<T><<<gx_blocks(NS * nn, 256), 256, 0, st>>>(NS * nn, M);
             ctx->launches++;
         }
         tm.mark();  // 3
+        // M2L
         const unsigned gn = (unsigned)((nn * 32 + 127) / 128);
-        if (mode == GX_MODE_REF) {
+        if (mode == GX_MODE_REF && !mixed) {
             k_m2l_ref<P><<<gn, 128, 0, st>>>(nn, dptr<uint32_t>(ctx->vdata), dptr<uint8_t>(ctx->vlen),
                                              dptr<int64_t>(ctx->ref_voff), dptr<int32_t>(ctx->ref_did),
-                                             dptr<double>(ctx->ref_G), M, L);
-        } else if (mode == GX_MODE_EXACT) {
-            k_m2l_exact<P, double, uint32_t><<<gn, 128, 0, st>>>(nn, dptr<uint32_t>(ctx->vdata), nullptr, nullptr,
-                                                                 dptr<uint8_t>(ctx->vlen), GX_LIST_CAP, comx, comy,
-                                                                 eps2, M, L);
-        } else {
+                                             dptr<double>(ctx->ref_G), reinterpret_cast<const double *>(M),
+                                             reinterpret_cast<double *>(L));
+        } else if (mode == GX_MODE_ACCURATE) {
             const int64_t *fs = dptr<int64_t>(ctx->far_off);
-            k_m2l_exact<P, double, int32_t><<<gn, 128, 0, st>>>(nn, dptr<int32_t>(ctx->far_idx), fs,
-                                                                reinterpret_cast<const int32_t *>(fs + nn), nullptr, 0,
-                                                                comx, comy, eps2, M, L);
+            k_m2l_exact<P, T, int32_t><<<gn, 128, 0, st>>>(nn, dptr<int32_t>(ctx->far_idx), fs,
+                                                           reinterpret_cast<const int32_t *>(fs + nn), nullptr, 0, comx,
+                                                           comy, eps2, M, L);
+        } else {
+            k_m2l_exact<P, T, uint32_t><<<gn, 128, 0, st>>>(nn, dptr<uint32_t>(ctx->vdata), nullptr, nullptr,
+                                                            dptr<uint8_t>(ctx->vlen), GX_LIST_CAP, comx, comy, eps2, M,
+                                                            L);
         }
         ctx->launches++;
         tm.mark();  // 4
-        const double *Lleaf = L;
+        // L2L
+        const T *Lleaf = L;
         if (mode == GX_MODE_REF) {
-            k_l2l_ref_leaves<P, double><<<gw, 128, 0, st>>>(nl, parent, comx, comy, L, Lf);
+            k_l2l_ref_leaves<P, T><<<gx_blocks(nl, 128), 128, 0, st>>>(nl, parent, comx, comy, L, Lf);
             ctx->launches++;
             Lleaf = Lf;
         } else {
             for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
                 int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
-                k_l2l_level<P, double><<<(unsigned)(((e - s) * 32 + 127) / 128), 128, 0, st>>>(s, e, parent, comx, comy, L);
+                k_l2l_level<P, T><<<gx_blocks(e - s, 128), 128, 0, st>>>(s, e, parent, comx, comy, L);
                 ctx->launches++;
             }
         }
         tm.mark();  // 5
-        if (mode == GX_MODE_ACCURATE) {
-            const int64_t *ns = dptr<int64_t>(ctx->near_off);
-            k_l2p_p2p64<P><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, Lleaf, ns,
-                                               reinterpret_cast<const int32_t *>(ns + nn), dptr<int32_t>(ctx->near_idx),
-                                               eps2, dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+        // P2P work items, then L2P + ordered sum of the partials
+        if (mixed) {
+            GX_TRY(gx_ensure(ctx, ctx->part, sizeof(float2) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
+            float2 *part = dptr<float2>(ctx->part);
+            if (I.n > 0)
+                k_p2p32_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
+                                                  pos, comx, comy, bs, be, src_idx, (float)eps2, tchunks, part);
+            k_l2p_reduce32<P><<<gw, 128, 0, st>>>(nl, pos, bs, be, reinterpret_cast<const float *>(Lleaf),
+                                                  dptr<int64_t>(I.off), tchunks, part, dptr<double>(ctx->ax),
+                                                  dptr<double>(ctx->ay));
         } else {
-            k_l2p_p2p64<P><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, Lleaf, dptr<int64_t>(ctx->p2p_off),
-                                               nullptr, dptr<int32_t>(ctx->p2p_idx), eps2, dptr<double>(ctx->ax),
-                                               dptr<double>(ctx->ay));
+            GX_TRY(gx_ensure(ctx, ctx->part, sizeof(double2) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
+            double2 *part = dptr<double2>(ctx->part);
+            if (I.n > 0)
+                k_p2p64_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
+                                                  X, Y, Mb, bs, be, src_idx, eps2, tchunks, part);
+            k_l2p_reduce64<P><<<gw, 128, 0, st>>>(nl, X, Y, comx, comy, bs, be, reinterpret_cast<const double *>(Lleaf),
+                                                  dptr<int64_t>(I.off), tchunks, part, dptr<double>(ctx->ax),
+                                                  dptr<double>(ctx->ay));
         }
-        ctx->launches++;
+        ctx->launches += 2;
         tm.mark();  // 6
+        return GX_OK;
+    };
+    if (mixed) {
+        GX_TRY(passes(float{}));
     } else {
-        GX_TRY(gx_ensure(ctx, ctx->Mf32, sizeof(float) * NC * (size_t)nn));
-        GX_TRY(gx_ensure(ctx, ctx->Lf32, sizeof(float) * NC * (size_t)nn));
-        GX_TRY(gx_ensure(ctx, ctx->Lff32, sizeof(float) * NC * (size_t)nl));
-        float *M = dptr<float>(ctx->Mf32), *L = dptr<float>(ctx->Lf32), *Lf = dptr<float>(ctx->Lff32);
-        k_p2m<P, float><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, M);
-        ctx->launches++;
-        tm.mark();
-        for (int lv = 1; lv < ctx->n_levels; lv++) {
-            int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
-            k_m2m<P, float><<<(unsigned)(((e - s) * 32 + 127) / 128), 128, 0, st>>>(s, e, child, comx, comy, M);
-            ctx->launches++;
-        }
-        if (ctx->n_levels > 1) {
-            k_scrub<float><<<gx_blocks(NC * nn, 256), 256, 0, st>>>(NC * nn, M);
-            ctx->launches++;
-        }
-        tm.mark();
-        const unsigned gn = (unsigned)((nn * 32 + 127) / 128);
-        if (mode == GX_MODE_ACCURATE) {
-            const int64_t *fs = dptr<int64_t>(ctx->far_off);
-            k_m2l_exact<P, float, int32_t><<<gn, 128, 0, st>>>(nn, dptr<int32_t>(ctx->far_idx), fs,
-                                                               reinterpret_cast<const int32_t *>(fs + nn), nullptr, 0,
-                                                               comx, comy, eps2, M, L);
-        } else {
-            k_m2l_exact<P, float, uint32_t><<<gn, 128, 0, st>>>(nn, dptr<uint32_t>(ctx->vdata), nullptr, nullptr,
-                                                                dptr<uint8_t>(ctx->vlen), GX_LIST_CAP, comx, comy, eps2,
-                                                                M, L);
-        }
-        ctx->launches++;
-        tm.mark();
-        const float *Lleaf = L;
-        if (mode == GX_MODE_REF) {
-            k_l2l_ref_leaves<P, float><<<gw, 128, 0, st>>>(nl, parent, comx, comy, L, Lf);
-            ctx->launches++;
-            Lleaf = Lf;
-        } else {
-            for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
-                int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
-                k_l2l_level<P, float><<<(unsigned)(((e - s) * 32 + 127) / 128), 128, 0, st>>>(s, e, parent, comx, comy, L);
-                ctx->launches++;
-            }
-        }
-        tm.mark();
-        if (mode == GX_MODE_ACCURATE) {
-            const int64_t *ns = dptr<int64_t>(ctx->near_off);
-            k_l2p_p2p32<P><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, Lleaf, ns,
-                                               reinterpret_cast<const int32_t *>(ns + nn), dptr<int32_t>(ctx->near_idx),
-                                               (float)eps2, dptr<double>(ctx->ax), dptr<double>(ctx->ay));
-        } else {
-            k_l2p_p2p32<P><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, Lleaf, dptr<int64_t>(ctx->p2p_off),
-                                               nullptr, dptr<int32_t>(ctx->p2p_idx), (float)eps2,
-                                               dptr<double>(ctx->ax), dptr<double>(ctx->ay));
-        }
-        ctx->launches++;
-        tm.mark();
+        GX_TRY(passes(double{}));
     }
     GX_CUDA(ctx, cudaGetLastError());
     ctx->last_launches = ctx->launches - launches0;

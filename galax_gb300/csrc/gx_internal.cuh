@@ -39,7 +39,7 @@ int gx_cuda_check(gx_ctx *ctx, cudaError_t e, const char *what);
 // Grow-only device allocation; contents are not preserved on growth.
 int gx_ensure(gx_ctx *ctx, DevBuf &b, size_t bytes);
 template <class T>
-inline T *dptr(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
+inline T *dptr(const DevBuf &b) { return reinterpret_cast<T *>(b.p); }
 
 // Device status word bits (read back at pass boundaries).
 enum : unsigned {
@@ -89,10 +89,19 @@ struct gx_ctx {
     DevBuf radius;                   // accurate mode node radii
     DevBuf far_off, far_idx, near_off, near_idx;
     int64_t n_far_pairs = 0, n_near_pairs = 0, n_p2p_inter = 0;
+    // P2P work items (source lists cut into pieces of at most 32 leaves), per plan
+    struct Items {
+        DevBuf leaf, qb, nq, off;  // int32, int64, int32, int64[n_leaves+1]
+        int64_t n = 0;
+        bool valid = false;
+    } items_ref, items_acc;
+    DevBuf part;                   // per-item partial accelerations
+    int64_t max_leaf = 0;          // largest leaf body count
 
     // expansions
     DevBuf M, L, Lf;
     DevBuf Mf32, Lf32, Lff32;
+    DevBuf pos32;  // mixed form: bodies as FP32 (x - com_leaf, y - com_leaf, m, 0)
 
     // scratch
     DevBuf scratch_a, scratch_b, scratch_c, scratch_d, scratch_e, scratch_f, scratch_g;
@@ -114,6 +123,7 @@ int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bou
 int gx_lists_build_ref(gx_ctx *ctx);
 int gx_plan_ref(gx_ctx *ctx);
 int gx_plan_accurate(gx_ctx *ctx);
+int gx_plan_items(gx_ctx *ctx, bool accurate);
 // gx_fmm.cu
 int gx_forces_device(gx_ctx *ctx, bool timed);
 int gx_poly_table_host(int p, double eps, std::vector<double> &out);

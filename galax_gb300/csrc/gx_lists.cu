@@ -838,6 +838,31 @@ int gx_plan_accurate(gx_ctx *ctx) {
 }
 
 namespace {
+constexpr int P2P_K = 32;  // source leaves per P2P work item
+
+// per leaf: number of items; start/count from either list layout
+__global__ void k_items_count(int64_t nl, const int64_t *start, const int32_t *cnt, int64_t *nitems) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a > nl) return;
+    if (a == nl) { nitems[a] = 0; return; }
+    int64_t c = cnt ? cnt[a] : start[a + 1] - start[a];
+    nitems[a] = (c + P2P_K - 1) / P2P_K;
+}
+
+__global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int64_t *off, int32_t *leaf,
+                             int64_t *qb, int32_t *nq) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nl) return;
+    int64_t s0 = start[a];
+    int64_t c = cnt ? cnt[a] : start[a + 1] - start[a];
+    for (int64_t k = 0; k * P2P_K < c; k++) {
+        int64_t it = off[a] + k;
+        leaf[it] = (int32_t)a;
+        qb[it] = s0 + k * P2P_K;
+        nq[it] = (int32_t)min((int64_t)P2P_K, c - k * P2P_K);
+    }
+}
+
 __global__ void k_add_offsets(const int64_t *o, int64_t *dst, int64_t c, int64_t add) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < c) dst[i] = o[i] + add;
@@ -895,4 +920,39 @@ int gx_tree_balance(gx_ctx *ctx, int64_t n_max, const double bounds[4]) {
         splits.assign(have.begin(), have.end());
     }
     return gx_tree_rebuild_with_splits(ctx, n_max, bounds, splits);
+}
+
+// P2P work items of the current plan (REF gather lists or ACCURATE near lists).
+int gx_plan_items(gx_ctx *ctx, bool accurate) {
+    gx_ctx::Items &I = accurate ? ctx->items_acc : ctx->items_ref;
+    I.valid = false;
+    int64_t nl = ctx->n_leaves, nn = ctx->n_nodes;
+    const int64_t *start;
+    const int32_t *cnt;
+    if (accurate) {
+        start = dptr<int64_t>(ctx->near_off);
+        cnt = reinterpret_cast<const int32_t *>(start + nn);
+    } else {
+        start = dptr<int64_t>(ctx->p2p_off);
+        cnt = nullptr;
+    }
+    GX_TRY(gx_ensure(ctx, I.off, sizeof(int64_t) * (size_t)(nl + 1)));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nl + 1)));
+    int64_t *nit = dptr<int64_t>(ctx->scratch_c);
+    k_items_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, start, cnt, nit);
+    GX_TRY(gx_exclusive_scan_i64(ctx, nit, dptr<int64_t>(I.off), nl + 1));
+    int64_t tot = 0;
+    GX_CUDA(ctx, cudaMemcpyAsync(&tot, dptr<int64_t>(I.off) + nl, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    GX_TRY(gx_ensure(ctx, I.leaf, sizeof(int32_t) * (size_t)(tot + 1)));
+    GX_TRY(gx_ensure(ctx, I.qb, sizeof(int64_t) * (size_t)(tot + 1)));
+    GX_TRY(gx_ensure(ctx, I.nq, sizeof(int32_t) * (size_t)(tot + 1)));
+    k_items_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, start, cnt, dptr<int64_t>(I.off), dptr<int32_t>(I.leaf),
+                                                              dptr<int64_t>(I.qb), dptr<int32_t>(I.nq));
+    ctx->launches += 2;
+    GX_CUDA(ctx, cudaGetLastError());
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    I.n = tot;
+    I.valid = true;
+    return GX_OK;
 }

@@ -1,0 +1,81 @@
+"""The oracle's accelerated list and constrained-tree builders equal the literal
+O(n^2) restatements of the reference (InteractionLists::build lib.rs:947-1025,
+build_p2p_lists lib.rs:1358-1392, neighbors_geometric lib.rs:382-423)."""
+import numpy as np
+import pytest
+
+from galax_gb300 import presets
+
+
+@pytest.mark.parametrize("preset,n,n_max", [("uniform", 8000, 32), ("plummer", 20000, 32), ("galaxy", 6001, 16),
+                                            ("disk", 15000, 8), ("plummer", 3000, 1)])
+def test_accelerated_lists_equal_literal(oracle, preset, n, n_max):
+    b = presets.make(preset, n, seed=31)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, n_max, presets.BOUNDS[preset])
+    va, vl = oracle.vlist_build(t, True), oracle.vlist_build(t, False)
+    ua, ul = oracle.ulist_build(t, True), oracle.ulist_build(t, False)
+    assert np.array_equal(va.lengths, vl.lengths) and np.array_equal(va.data, vl.data)
+    assert np.array_equal(ua.lengths, ul.lengths) and np.array_equal(ua.data, ul.data)
+
+
+def test_accelerated_lists_with_nonfinite_nodes(oracle):
+    b = presets.uniform(2000, seed=32)
+    b.x[10] = np.nan
+    b.y[20] = np.inf
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, 16, presets.BOUNDS["uniform"])
+    va, vl = oracle.vlist_build(t, True), oracle.vlist_build(t, False)
+    ua, ul = oracle.ulist_build(t, True), oracle.ulist_build(t, False)
+    assert np.array_equal(va.data, vl.data) and np.array_equal(ua.data, ul.data)
+
+
+@pytest.mark.parametrize("preset,n,n_max", [("uniform", 1500, 16), ("plummer", 2000, 16)])
+def test_constrained_accel_equals_literal(oracle, preset, n, n_max):
+    b = presets.make(preset, n, seed=33)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    oracle.tree_build(ob, n_max, presets.BOUNDS[preset])  # Morton-sort first, as the CLI does
+    t1 = oracle.tree_build_constrained(ob, n_max, presets.BOUNDS[preset], accel=True)
+    t2 = oracle.tree_build_constrained(ob, n_max, presets.BOUNDS[preset], accel=False)
+    assert t1.n_nodes == t2.n_nodes
+    for f in ("cx", "cy", "hw", "body_start", "body_end", "child", "parent"):
+        assert np.array_equal(getattr(t1, f), getattr(t2, f))
+
+
+def test_ref_cache_first_inserter(oracle):
+    """m2l's derivative cache (lib.rs:1209-1247): pairs whose truncated offsets agree
+    share the derivatives of the first pair in (target id, slot) order."""
+    b = presets.uniform(3000, seed=34)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, 32, presets.BOUNDS["uniform"])
+    v = oracle.vlist_build(t)
+    pk, kd = oracle.m2l_ref_keys(v, t)
+    off, idx = v.csr()
+    tgt = np.repeat(np.arange(t.n_nodes), v.lengths.astype(np.int64))
+    dx = t.comx[tgt] - t.comx[idx]
+    dy = t.comy[tgt] - t.comy[idx]
+    keys = np.stack([np.trunc(dx), np.trunc(dy)], 1)
+    first = {}
+    for q, k in enumerate(map(tuple, keys)):
+        first.setdefault(k, q)
+    assert len(first) == kd.shape[0]
+    for q, k in enumerate(map(tuple, keys)):
+        f = first[k]
+        assert kd[pk[q], 0] == dx[f] and kd[pk[q], 1] == dy[f]
+
+
+def test_accurate_lists_cover_every_pair_once(oracle):
+    """ACCURATE mode: far pairs plus near leaf pairs count every body pair exactly once."""
+    b = presets.plummer(3000, seed=35)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, 16, presets.BOUNDS["plummer"])
+    R = oracle.node_radii(ob, t)
+    far, near = oracle.mac_lists_build(t, R, 0.5)
+    cover = np.zeros((3000, 3000), np.int32)
+    for a in range(t.n_nodes):
+        for s in far.idx[far.off[a]:far.off[a + 1]]:
+            cover[t.body_start[a]:t.body_end[a], t.body_start[s]:t.body_end[s]] += 1
+        if t.is_leaf[a]:
+            for s in near.idx[near.off[a]:near.off[a + 1]]:
+                cover[t.body_start[a]:t.body_end[a], t.body_start[s]:t.body_end[s]] += 1
+    assert np.all(cover == 1)
