@@ -95,6 +95,7 @@ def lib():
         "gx_bench_forces": (C.c_int, [_VP, C.c_int32, C.c_int32, _D, C.c_int32, _D]),
         "gx_last_launch_count": (C.c_int, [_VP, _I64]),
         "gx_probe_fp32_tflops": (C.c_int, [_VP, _D]),
+        "gx_n2_sampled_static": (C.c_int, [_VP, _VP, _VP, C.c_int64, C.c_double, _I64, C.c_int64, _D, _D, _VP]),
         "gx_host_alloc": (_VP, [C.c_size_t]),
         "gx_host_free": (None, [_VP]),
     }
@@ -117,6 +118,29 @@ def _f64(a) -> np.ndarray:
     if a.dtype != np.float64 or not a.flags.c_contiguous:
         raise TypeError("expected a C-contiguous float64 array")
     return a
+
+
+N2_STATIC_MAX_SAMPLES = 4096
+
+
+def n2_sampled_static(x_dev: int, y_dev: int, m_dev: int, n: int, eps: float, idx, stream: int = 0):
+    """Exact FP64 softened forces on sampled targets from the caller's device arrays
+    (addresses of n float64 values each), without a context and without allocating
+    device memory: for callers that cannot allocate when they want the check (device
+    memory owned by another runtime's caching allocator, or a stream being captured
+    into a CUDA graph).  At most N2_STATIC_MAX_SAMPLES targets per call; the first
+    call on a device should come before any stream capture; calls that overlap on
+    the GPU race on the shared staging array."""
+    idx = np.ascontiguousarray(np.asarray(idx, np.int64))
+    ax = np.zeros(idx.size)
+    ay = np.zeros(idx.size)
+    rc = lib().gx_n2_sampled_static(x_dev, y_dev, m_dev, int(n), float(eps), _p(idx, _I64), idx.size, _p(ax), _p(ay),
+                                    stream or None)
+    if rc == 6:
+        raise GpuError(rc, f"{idx.size} samples exceed the static staging array ({N2_STATIC_MAX_SAMPLES})")
+    if rc != 0:
+        raise GpuError(rc, "gx_n2_sampled_static failed")
+    return ax, ay
 
 
 class HostArray:

@@ -5,6 +5,8 @@
 //  * diagnostics (galax-core/src/lib.rs:1638-1683): KE, FMM PE, momentum, Lz as
 //    deterministic two-stage block reductions (fixed grid, fixed tree order);
 //  * validate_fmm's exact sum (lib.rs:1537-1553) for sampled targets.
+#include <mutex>
+
 #include "gx_internal.cuh"
 
 namespace {
@@ -168,5 +170,72 @@ int gx_n2_device(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, dou
     GX_CUDA(ctx, cudaMemcpyAsync(ax, dax, sizeof(double) * n_idx, cudaMemcpyDeviceToHost, ctx->stream));
     GX_CUDA(ctx, cudaMemcpyAsync(ay, day, sizeof(double) * n_idx, cudaMemcpyDeviceToHost, ctx->stream));
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
+// ---------------------------------------------------------------- allocation-free variant
+// gx_n2_sampled_static: the sampled exact sum without a context and without any
+// device allocation.  Some callers cannot allocate device memory at the moment
+// they want a force check: a simulation whose device memory is owned by another
+// runtime's caching allocator (which may already hold nearly all of HBM, so a
+// cudaMalloc would fail or fragment it), or code running while a stream is being
+// captured into a CUDA graph, where cudaMalloc/cudaFree would break the capture.
+// Their device arrays are passed in; the per-sample indices and results are
+// staged through the file-scope array below instead of context scratch.
+//
+// The array is GX_N2_STATIC_MAX_SAMPLES * 24 bytes (96 KiB); every GPU that loads
+// this library holds it until the process exits.  All calls on a device share it
+// and it keeps the last call's contents: each call overwrites every slot it reads
+// (indices, then one result per sample), so nothing has to start at zero, but
+// calls that overlap on the GPU (other streams, other host threads) race on it.
+namespace {
+static __device__ __align__(256) unsigned char g_n2_static_scratch[GX_N2_STATIC_MAX_SAMPLES *
+                                                                   (sizeof(int64_t) + 2 * sizeof(double))];
+// Device address of the array per device ordinal, found once per device with that
+// device current (the host-side symbol is a stand-in, not a device address).
+constexpr int kMaxDevices = 64;
+void *g_n2_static_addr[kMaxDevices] = {};
+std::mutex g_n2_static_mu;
+}  // namespace
+
+extern "C" int gx_n2_sampled_static(const double *x, const double *y, const double *m, int64_t n, double eps,
+                                    const int64_t *idx, int64_t n_idx, double *ax, double *ay, void *stream) {
+    if (n < 0 || n_idx < 0 || !(eps >= 0.0)) return GX_ERR_INVALID_ARG;
+    if (n_idx > GX_N2_STATIC_MAX_SAMPLES) return GX_ERR_CAP_EXCEEDED;
+    if (n_idx == 0) return GX_OK;
+    if (!x || !y || !m || !idx || !ax || !ay) return GX_ERR_INVALID_ARG;
+    for (int64_t k = 0; k < n_idx; k++)
+        if (idx[k] < 0 || idx[k] >= n) return GX_ERR_INVALID_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GX_ERR_INIT;
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_n2_static_mu);
+        if (!g_n2_static_addr[dev]) {
+            void *p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_n2_static_scratch) != cudaSuccess || !p) {
+                cudaGetLastError();
+                return GX_ERR_KERNEL_LOAD;
+            }
+            g_n2_static_addr[dev] = p;
+        }
+        base = g_n2_static_addr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int64_t *didx = static_cast<int64_t *>(base);
+    double *dax = reinterpret_cast<double *>(didx + GX_N2_STATIC_MAX_SAMPLES);
+    double *day = dax + GX_N2_STATIC_MAX_SAMPLES;
+    if (cudaMemcpyAsync(didx, idx, sizeof(int64_t) * n_idx, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        cudaGetLastError();
+        return GX_ERR_CUDA;
+    }
+    k_n2_sampled<<<(unsigned)n_idx, RED_THREADS, 0, st>>>(n, x, y, m, eps * eps, didx, dax, day);
+    if (cudaGetLastError() != cudaSuccess) return GX_ERR_CUDA;
+    if (cudaMemcpyAsync(ax, dax, sizeof(double) * n_idx, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(ay, day, sizeof(double) * n_idx, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        return GX_ERR_CUDA;
+    }
     return GX_OK;
 }

@@ -139,6 +139,24 @@ int gx_diagnostics(gx_ctx *ctx, double out[5]);
  * resident bodies for the targets idx[0..n_idx). */
 int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, double *ay);
 
+/* The same sampled exact sum without a context and without allocating: for
+ * callers that cannot allocate device memory when they want the check (their
+ * device memory belongs to another runtime's caching allocator, or a stream is
+ * being captured into a CUDA graph).  No counterpart in the reference.
+ * x, y, m are the caller's device arrays of n bodies; idx (host, n_idx entries,
+ * each in [0, n)) and the host outputs ax, ay are staged through a file-scope
+ * device array of GX_N2_STATIC_MAX_SAMPLES slots (96 KiB, held by every GPU that
+ * loads the library until exit); more samples return GX_ERR_CAP_EXCEEDED.  The
+ * first call on a device looks up that array's device address (once per device,
+ * with the device current): make that first call before any stream capture.
+ * Calls share the array and it keeps the last call's contents (each call
+ * overwrites all it reads); calls that overlap on the GPU race.  stream is a
+ * cudaStream_t (NULL = the legacy default stream); the call returns after the
+ * stream has finished the work. */
+#define GX_N2_STATIC_MAX_SAMPLES 4096
+int gx_n2_sampled_static(const double *x, const double *y, const double *m, int64_t n, double eps,
+                         const int64_t *idx, int64_t n_idx, double *ax, double *ay, void *stream);
+
 /* Device time of the last force evaluation per pass, in ms:
  * {total, prepare, p2m, m2m, m2l, l2l, l2p+p2p}; returns 7 entries. */
 int gx_last_timings(gx_ctx *ctx, double out[7]);
