@@ -302,7 +302,8 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
                                                    const int64_t *__restrict__ start, const int32_t *__restrict__ cnt,
                                                    const uint8_t *__restrict__ cnt8, int64_t fixed_stride,
                                                    const double *__restrict__ comx, const double *__restrict__ comy,
-                                                   double eps2d, const T *__restrict__ M, T *__restrict__ L) {
+                                                   const float4 *__restrict__ comhl, double eps2d,
+                                                   const T *__restrict__ M, T *__restrict__ L) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
@@ -315,13 +316,23 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
     int64_t st = start ? start[node] : node * fixed_stride;
     int len = cnt ? cnt[node] : (int)cnt8[node];
     double tcx = comx[node], tcy = comy[node];
+    float4 thl = comhl ? comhl[node] : make_float4(0.f, 0.f, 0.f, 0.f);
     T eps2 = (T)eps2d;
     T acc[NC];
 #pragma unroll
     for (int k = 0; k < NCr; k++) acc[k] = T(0);
     for (int s = lane; s < len; s += 32) {
         int64_t src = (int64_t)idx[st + s];
-        T dx = (T)(tcx - comx[src]), dy = (T)(tcy - comy[src]);
+        T dx, dy;
+        if (sizeof(T) == 4 && comhl) {
+            // COMs as FP32 (hi, lo) pairs: the offset is exact to FP32 rounding without FP64 work
+            float4 shl = comhl[src];
+            dx = (T)((thl.x - shl.x) + (thl.y - shl.y));
+            dy = (T)((thl.z - shl.z) + (thl.w - shl.w));
+        } else {
+            dx = (T)(tcx - comx[src]);
+            dy = (T)(tcy - comy[src]);
+        }
         T A[ND];
         derivs_scaled<P, T>(dx, dy, eps2, A);
         T ms[NC];
@@ -375,6 +386,46 @@ __device__ __forceinline__ void l2l_shift(const T *__restrict__ LP, T dx, T dy, 
                     sum += lp[gx_mi(i, j)] * (T)(cbinom(i, oi) * cbinom(j, oj)) * px[i - oi] * py[j - oj];
             out[gx_mi(oi, oj)] += sum;
         }
+}
+
+// Top-down modes: only the leaves' locals are consumed (by L2P), and translating a
+// local expansion is exact for polynomials, so shifting every ancestor's M2L local
+// straight to the leaf equals the level-by-level L2L chain.  One warp per leaf, one
+// lane per ancestor (from the ancestor table anc[level * nl + leaf]), then a warp
+// reduction: a single launch instead of one per level.  Ancestors without far
+// interactions (has_far = 0) hold a zero local and are skipped.
+template <int P, class T>
+__global__ void __launch_bounds__(128) k_l2l_direct(int64_t nl, int n_levels, const int32_t *__restrict__ anc,
+                                                    const uint8_t *__restrict__ has_far, const double *__restrict__ comx,
+                                                    const double *__restrict__ comy, const T *__restrict__ L,
+                                                    T *__restrict__ Lout) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    int lane = threadIdx.x & 31;
+    int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (leaf >= nl) return;
+    T out[NC];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) out[k] = T(0);
+    for (int j = lane; j < n_levels; j += 32) {
+        int32_t a = anc[(int64_t)j * nl + leaf];
+        if (a < 0 || !has_far[a]) continue;
+        if (a == (int32_t)leaf) {
+            T own[NC];
+            load_row<NC>(L + leaf * NS, own);
+#pragma unroll
+            for (int k = 0; k < NCr; k++) out[k] += own[k];
+        } else {
+            l2l_shift<P, T>(L + (int64_t)a * NS, (T)(comx[leaf] - comx[a]), (T)(comy[leaf] - comy[a]), out);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NCr; k++) {
+        T v = warp_sum_t<T>(out[k]);
+        if (lane == (k & 31)) Lout[leaf * NS + k] = v;
+    }
 }
 
 // REF: Lout[leaf] = L[leaf] + shift(L[parent(leaf)])
@@ -596,7 +647,7 @@ __global__ void __launch_bounds__(128) k_p2p32_items(int64_t n_items, const int3
                             ay0 = fmaf(f, dy, ay0);
                         }
                     } else if (ns == 32) {
-#pragma unroll 8
+#pragma unroll
                         for (int kk = 0; kk < 32; kk += 2) {
                             float4 b0 = sb[w][kk], b1 = sb[w][kk + 1];
                             float dx0 = b0.x - xi, dy0 = b0.y - yi, dx1 = b1.x - xi, dy1 = b1.y - yi;
@@ -768,11 +819,12 @@ int run_forces(gx_ctx *ctx, bool timed) {
             const int64_t *fs = dptr<int64_t>(ctx->far_off);
             k_m2l_exact<P, T, int32_t><<<gn, 128, 0, st>>>(nn, dptr<int32_t>(ctx->far_idx), fs,
                                                            reinterpret_cast<const int32_t *>(fs + nn), nullptr, 0, comx,
-                                                           comy, eps2, M, L);
+                                                           comy, mixed ? dptr<float4>(ctx->comhl) : nullptr, eps2, M,
+                                                           L);
         } else {
             k_m2l_exact<P, T, uint32_t><<<gn, 128, 0, st>>>(nn, dptr<uint32_t>(ctx->vdata), nullptr, nullptr,
-                                                            dptr<uint8_t>(ctx->vlen), GX_LIST_CAP, comx, comy, eps2, M,
-                                                            L);
+                                                            dptr<uint8_t>(ctx->vlen), GX_LIST_CAP, comx, comy,
+                                                            mixed ? dptr<float4>(ctx->comhl) : nullptr, eps2, M, L);
         }
         ctx->launches++;
         tm.mark();  // 4
@@ -783,11 +835,12 @@ int run_forces(gx_ctx *ctx, bool timed) {
             ctx->launches++;
             Lleaf = Lf;
         } else {
-            for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
-                int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
-                k_l2l_level<P, T><<<gx_blocks(e - s, 128), 128, 0, st>>>(s, e, parent, comx, comy, L);
-                ctx->launches++;
-            }
+            k_l2l_direct<P, T><<<gw, 128, 0, st>>>(nl, ctx->n_levels, dptr<int32_t>(ctx->anc),
+                                                   dptr<uint8_t>(mode == GX_MODE_ACCURATE ? ctx->has_far_acc
+                                                                                          : ctx->has_far_ref),
+                                                   comx, comy, L, Lf);
+            ctx->launches++;
+            Lleaf = Lf;
         }
         tm.mark();  // 5
         // P2P work items, then L2P + ordered sum of the partials

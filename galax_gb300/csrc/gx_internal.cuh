@@ -87,6 +87,9 @@ struct gx_ctx {
     DevBuf ref_G;                    // n_keys x (2p+1)^2 doubles
     int64_t n_ref_keys = 0, n_v_pairs = 0;
     DevBuf radius;                   // accurate mode node radii
+    DevBuf anc;                      // per leaf, its ancestor at every level (level-major), -1 above the root
+    DevBuf has_far_ref, has_far_acc; // per node: 1 if its M2L list is non-empty
+    DevBuf comhl;                    // per node COM as FP32 (x_hi, x_lo, y_hi, y_lo)
     DevBuf far_off, far_idx, near_off, near_idx;
     int64_t n_far_pairs = 0, n_near_pairs = 0, n_p2p_inter = 0;
     // P2P work items (source lists cut into pieces of at most 32 leaves), per plan
@@ -97,6 +100,7 @@ struct gx_ctx {
     } items_ref, items_acc;
     DevBuf part;                   // per-item partial accelerations
     int64_t max_leaf = 0;          // largest leaf body count
+    bool aux_valid = false;        // anc / comhl built for the current tree
 
     // expansions
     DevBuf M, L, Lf;
@@ -124,6 +128,7 @@ int gx_lists_build_ref(gx_ctx *ctx);
 int gx_plan_ref(gx_ctx *ctx);
 int gx_plan_accurate(gx_ctx *ctx);
 int gx_plan_items(gx_ctx *ctx, bool accurate);
+int gx_plan_tree_aux(gx_ctx *ctx);
 // gx_fmm.cu
 int gx_forces_device(gx_ctx *ctx, bool timed);
 int gx_poly_table_host(int p, double eps, std::vector<double> &out);

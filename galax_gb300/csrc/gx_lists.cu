@@ -515,6 +515,16 @@ __global__ void k_balance_splits(LevelSet ls, int64_t nl, const double *cx, cons
     mid_out[lid] = mid;
 }
 
+__global__ void k_flag_u8(int64_t nn, const uint8_t *len, uint8_t *flag) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) flag[i] = len[i] > 0;
+}
+
+__global__ void k_flag_i32(int64_t nn, const int32_t *cnt, uint8_t *flag) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nn) flag[i] = cnt[i] > 0;
+}
+
 }  // namespace
 
 // Builds a BVH over nodes [s, e) into `storage` (grown as needed).
@@ -725,6 +735,9 @@ int gx_plan_ref(gx_ctx *ctx) {
         GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         ctx->n_ref_keys = nk;
     }
+    GX_TRY(gx_ensure(ctx, ctx->has_far_ref, (size_t)nn));
+    k_flag_u8<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, dptr<uint8_t>(ctx->vlen), dptr<uint8_t>(ctx->has_far_ref));
+    ctx->launches++;
     GX_TRY(check_status(ctx));
     ctx->plan_ref_valid = true;
     ctx->plan_p = ctx->p;
@@ -829,6 +842,9 @@ int gx_plan_accurate(gx_ctx *ctx) {
         }
     }
     ctx->n_far_pairs = far_tot;
+    GX_TRY(gx_ensure(ctx, ctx->has_far_acc, (size_t)nn));
+    k_flag_i32<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, fcnt, dptr<uint8_t>(ctx->has_far_acc));
+    ctx->launches++;
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->plan_acc_valid = true;
     ctx->plan_p = ctx->p;
@@ -839,6 +855,26 @@ int gx_plan_accurate(gx_ctx *ctx) {
 
 namespace {
 constexpr int P2P_K = 32;  // source leaves per P2P work item
+
+// ancestor table: anc[level * nl + leaf] = the leaf's ancestor at that level
+__global__ void k_ancestors(int64_t nl, int n_levels, const int32_t *parent, int32_t *anc) {
+    int64_t leaf = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= nl) return;
+    int32_t a = (int32_t)leaf;
+    for (int j = 0; j < n_levels; j++) {
+        anc[(int64_t)j * nl + leaf] = a;
+        if (a >= 0) a = parent[a];
+    }
+}
+
+// COM as FP32 (hi, lo): hi = fl(c), lo = fl(c - hi)
+__global__ void k_comhl(int64_t nn, const double *comx, const double *comy, float4 *out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    float xh = (float)comx[i], yh = (float)comy[i];
+    out[i] = make_float4(xh, (float)(comx[i] - (double)xh), yh, (float)(comy[i] - (double)yh));
+}
+
 
 // per leaf: number of items; start/count from either list layout
 __global__ void k_items_count(int64_t nl, const int64_t *start, const int32_t *cnt, int64_t *nitems) {
@@ -954,5 +990,24 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     I.n = tot;
     I.valid = true;
+    return GX_OK;
+}
+
+// Per-tree auxiliary arrays: the leaves' ancestor table (direct L2L) and the FP32
+// hi/lo node COMs (mixed-precision M2L offsets).
+int gx_plan_tree_aux(gx_ctx *ctx) {
+    int64_t nl = ctx->n_leaves, nn = ctx->n_nodes;
+    int L = ctx->n_levels;
+    GX_TRY(gx_ensure(ctx, ctx->anc, sizeof(int32_t) * (size_t)(nl > 0 ? nl : 1) * (size_t)(L > 0 ? L : 1)));
+    GX_TRY(gx_ensure(ctx, ctx->comhl, sizeof(float4) * (size_t)(nn > 0 ? nn : 1)));
+    if (nl > 0) {
+        k_ancestors<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, L, dptr<int32_t>(ctx->parent), dptr<int32_t>(ctx->anc));
+        k_comhl<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, dptr<double>(ctx->comx), dptr<double>(ctx->comy),
+                                                             dptr<float4>(ctx->comhl));
+        ctx->launches += 2;
+        GX_CUDA(ctx, cudaGetLastError());
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    ctx->aux_valid = true;
     return GX_OK;
 }

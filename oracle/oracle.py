@@ -408,12 +408,10 @@ def cli_softening(b: Bodies) -> float:
 
 
 def cli_dt(ax: np.ndarray, ay: np.ndarray) -> float:
-    """dt = 0.5/sqrt(max|a|) else 0.01 (galax-cli/src/main.rs:232-244)."""
-    amax = 0.0
-    for a, b in zip(ax, ay):
-        v = (a * a + b * b) ** 0.5
-        if v > amax:
-            amax = v
+    """dt = 0.5/sqrt(max|a|) else 0.01 (galax-cli/src/main.rs:232-244); the fold over
+    f64::max ignores NaN."""
+    a = np.sqrt(np.asarray(ax) * np.asarray(ax) + np.asarray(ay) * np.asarray(ay))
+    amax = float(np.nanmax(np.concatenate([a, [0.0]])))
     return 0.5 / amax ** 0.5 if amax > 1e-30 else 0.01
 
 

@@ -1,0 +1,118 @@
+"""Device-resident leapfrog, diagnostics and the sampled exact sum against the oracle.
+
+simulate / leapfrog_kdk (galax-integrate/src/lib.rs:158-237), diagnostics
+(galax-core/src/lib.rs:1638-1683), validate_fmm's exact sum (lib.rs:1537-1553)
+and compute_n2_force (lib.rs:1685-1721).
+"""
+import numpy as np
+import pytest
+
+from helpers import oracle_case, rel_vec_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)) / np.maximum(np.abs(np.asarray(b)), 1e-300)
+
+
+def test_config1_uniform_10k_ten_steps(G, oracle):
+    """Uniform 10k in [0,100]^2, p=4, n_max=32, CLI softening, dt = 0.5/sqrt(max|a|),
+    10 KDK steps with the static tree; diagnostics every step."""
+    from galax_gb300 import presets
+    n, p = 10_000, 4
+    b = presets.uniform(n, seed=0)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS["uniform"], p)
+    ref = ob.copy()
+    oracle.compute_fmm_force(ref, t, v, u, p, eps, oracle.MODE_REF)  # initial forces (galax-cli/src/main.rs:230)
+    dt = oracle.cli_dt(ref.ax, ref.ay)
+    diag_ref = oracle.simulate(ref, t, v, u, p, eps, dt, 10, 1, oracle.MODE_REF)
+
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=p, eps64=eps))
+    gb = b.copy()
+    ctx.build_tree(gb, 32, presets.BOUNDS["uniform"])
+    assert np.array_equal(gb.x, ob.x)
+    ctx.upload_bodies(gb)
+    ctx.forces_resident()
+    g0 = G.Bodies.new(n)
+    ctx.download_bodies(g0)
+    assert presets.cli_dt(g0.ax, g0.ay) == pytest.approx(dt, rel=1e-12)
+    diag = ctx.kdk_run(10, dt, 1)
+    out = G.Bodies.new(n)
+    ctx.download_bodies(out)
+    ctx.close()
+    scale = np.max(np.abs(ref.x))
+    assert np.max(np.abs(out.x - ref.x)) / scale < 1e-10 and np.max(np.abs(out.y - ref.y)) / scale < 1e-10
+    vs = np.max(np.hypot(ref.vx, ref.vy))
+    assert np.max(np.abs(out.vx - ref.vx)) / vs < 1e-10 and np.max(np.abs(out.vy - ref.vy)) / vs < 1e-10
+    assert rel_vec_err(out.ax, out.ay, ref.ax, ref.ay).max() < 1e-10
+    assert diag.shape == diag_ref.shape == (10, 6)
+    assert np.array_equal(diag[:, 0], diag_ref[:, 0])
+    for col in (1, 2, 5):  # KE, FMM PE, Lz
+        assert _rel(diag[:, col], diag_ref[:, col]).max() < 1e-10
+    pscale = np.sum(ref.mass * np.hypot(ref.vx, ref.vy))
+    assert np.max(np.abs(diag[:, 3:5] - diag_ref[:, 3:5])) / pscale < 1e-10
+
+
+def test_diagnostics_known_values(G):
+    """galax-integrate/src/lib.rs:33-54."""
+    b = G.Bodies(np.array([0.0, 3.0]), np.array([0.0, 0.0]), np.array([2.0, -1.0]), np.array([1.0, 2.0]),
+                 np.array([5.0, 3.0]), np.array([0.5, -0.3]), np.array([0.0, 0.1]))
+    ctx = G.GpuContext(G.GpuConfig(max_n=2, p=4, eps64=0.1))
+    ctx.upload_bodies(b)
+    ke, pe, px, py, lz = ctx.diagnostics()
+    ctx.close()
+    assert abs(ke - 20.0) < 1e-14 and abs(px - 7.0) < 1e-14 and abs(py - 11.0) < 1e-14 and abs(lz - 18.0) < 1e-14
+    # FMM PE: -1/2 sum m |a| max(r, 1)
+    e = -0.5 * (5.0 * 0.5 * 1.0 + 3.0 * np.hypot(0.3, 0.1) * 3.0)
+    assert abs(pe - e) < 1e-14
+
+
+def test_single_body_drift(G):
+    """galax-integrate/src/lib.rs:9-30 on the device."""
+    b = G.Bodies.from_arrays([0.0], [0.0], [1.0], [10.0], [5.0])
+    ctx = G.GpuContext(G.GpuConfig(max_n=1, p=2, eps64=0.1))
+    ctx.build_tree(b, 32, (-100.0, 100.0, -100.0, 100.0))
+    ctx.upload_bodies(b)
+    ctx.kdk_run(1, 0.1, 0)
+    out = G.Bodies.new(1)
+    ctx.download_bodies(out)
+    ctx.close()
+    assert out.vx[0] == 10.0 and out.vy[0] == 5.0
+    assert abs(out.x[0] - 1.0) < 1e-14 and abs(out.y[0] - 0.5) < 1e-14
+
+
+@pytest.mark.parametrize("preset,n", [("plummer", 20_000), ("galaxy", 5_001)])
+def test_sampled_n2_matches_oracle(G, oracle, preset, n):
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=12)
+    eps = 0.05
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, p=4, eps64=eps))
+    ctx.upload_bodies(b)
+    idx = np.random.default_rng(3).choice(n, 500, replace=False)
+    ax, ay = ctx.n2_sampled(idx)
+    rx, ry = oracle.n2_sampled(b.x, b.y, b.mass, eps, idx)
+    assert rel_vec_err(ax, ay, rx, ry).max() < 1e-12
+    full = ctx.n2_debug(G.Bodies.from_arrays(b.x[:3000], b.y[:3000], b.mass[:3000]))
+    ob = oracle.Bodies.from_arrays(b.x[:3000], b.y[:3000], b.mass[:3000])
+    oracle.n2_force(ob, eps)
+    assert rel_vec_err(full[0], full[1], ob.ax, ob.ay).max() < 1e-12
+    ctx.close()
+
+
+def test_accurate_mixed_kdk_conserves_momentum(G):
+    """The mixed ACCURATE form over 20 steps of the galaxy preset: total momentum stays
+    near zero relative to sum m|v| (the reference has no device check of this)."""
+    from galax_gb300 import presets
+    n = 20_001
+    b = presets.galaxy(n, seed=13)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=4, eps64=0.05))
+    ctx.build_tree(b, 32, presets.BOUNDS["galaxy"])
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    ctx.upload_bodies(b)
+    ctx.forces_resident()
+    diag = ctx.kdk_run(20, 1e-3, 10)
+    ctx.close()
+    pscale = np.sum(b.mass * np.hypot(b.vx, b.vy))
+    assert diag.shape == (2, 6)
+    assert np.all(np.abs(diag[:, 3:5]) / pscale < 1e-3)
