@@ -102,7 +102,7 @@ def test_sampled_n2_matches_oracle(G, oracle, preset, n):
 
 def test_accurate_mixed_kdk_conserves_momentum(G):
     """The mixed ACCURATE form over 20 steps of the galaxy preset: total momentum stays
-    near zero relative to sum m|v| (the reference has no device check of this)."""
+    at its initial value relative to sum m|v| (the reference has no device check of this)."""
     from galax_gb300 import presets
     n = 20_001
     b = presets.galaxy(n, seed=13)
@@ -114,5 +114,6 @@ def test_accurate_mixed_kdk_conserves_momentum(G):
     diag = ctx.kdk_run(20, 1e-3, 10)
     ctx.close()
     pscale = np.sum(b.mass * np.hypot(b.vx, b.vy))
+    p0 = np.array([np.sum(b.mass * b.vx), np.sum(b.mass * b.vy)])
     assert diag.shape == (2, 6)
-    assert np.all(np.abs(diag[:, 3:5]) / pscale < 1e-3)
+    assert np.all(np.abs(diag[:, 3:5] - p0) / pscale < 1e-5)
