@@ -96,6 +96,9 @@ def lib():
         "gx_last_launch_count": (C.c_int, [_VP, _I64]),
         "gx_probe_fp32_tflops": (C.c_int, [_VP, _D]),
         "gx_n2_sampled_static": (C.c_int, [_VP, _VP, _VP, C.c_int64, C.c_double, _I64, C.c_int64, _D, _D, _VP]),
+        "gx_force_vjp": (C.c_int, [_VP, _D, _D, _D, _D, _D]),
+        "gx_rollout_forward": (C.c_int, [_VP, C.c_int64, C.c_double, C.c_int64]),
+        "gx_rollout_backward": (C.c_int, [_VP, _D, _D, _D, _D, _D, _D, _D, _D, _D, _I64]),
         "gx_host_alloc": (_VP, [C.c_size_t]),
         "gx_host_free": (None, [_VP]),
     }
@@ -407,6 +410,36 @@ class GpuContext:
         c = C.c_int64()
         self._check(lib().gx_last_launch_count(self._h, C.byref(c)))
         return c.value
+
+    # -- reverse mode (ACCURATE)
+    def _resident_n(self, *arrays) -> int:
+        """The resident body count; every cotangent array must have that length."""
+        n = self.tree_info()[3]
+        for a in arrays:
+            if len(a) != n:
+                raise ValueError(f"cotangent of length {len(a)} for {n} resident bodies")
+        return n
+
+    def force_vjp(self, lam_x, lam_y):
+        """(g_x, g_y, g_m) = lam . d(a)/d(x, y, m) at the resident bodies."""
+        n = self._resident_n(lam_x, lam_y)
+        gx, gy, gm = np.zeros(n), np.zeros(n), np.zeros(n)
+        self._check(lib().gx_force_vjp(self._h, _p(_f64(np.ascontiguousarray(lam_x, np.float64))),
+                                       _p(_f64(np.ascontiguousarray(lam_y, np.float64))), _p(gx), _p(gy), _p(gm)))
+        return gx, gy, gm
+
+    def rollout_forward(self, n_steps: int, dt: float, checkpoint_every: int) -> None:
+        self._check(lib().gx_rollout_forward(self._h, int(n_steps), float(dt), int(checkpoint_every)))
+
+    def rollout_backward(self, lx, ly, lvx, lvy):
+        """Gradients at step 0: (g_x, g_y, g_vx, g_vy, g_m, peak_device_bytes)."""
+        n = self._resident_n(lx, ly, lvx, lvy)
+        out = [np.zeros(n) for _ in range(5)]
+        pk = C.c_int64()
+        f = lambda a: _p(_f64(np.ascontiguousarray(a, np.float64)))
+        self._check(lib().gx_rollout_backward(self._h, f(lx), f(ly), f(lvx), f(lvy), *[_p(o) for o in out],
+                                              C.byref(pk)))
+        return (*out, pk.value)
 
     def probe_fp32_tflops(self) -> float:
         out = C.c_double()

@@ -125,7 +125,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->p2p_idx, &ctx->ref_voff, &ctx->ref_did, &ctx->ref_G, &ctx->radius, &ctx->anc, &ctx->has_far_ref, &ctx->has_far_acc, &ctx->comhl, &ctx->far_off, &ctx->far_idx,
                       &ctx->near_off, &ctx->near_idx, &ctx->M, &ctx->L, &ctx->Lf, &ctx->Mf32, &ctx->Lf32,
                       &ctx->Lff32, &ctx->pos32, &ctx->part, &ctx->items_ref.leaf, &ctx->items_ref.qb, &ctx->items_ref.nq, &ctx->items_ref.off, &ctx->items_acc.leaf, &ctx->items_acc.qb, &ctx->items_acc.nq, &ctx->items_acc.off, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
-                      &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush};
+                      &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush, &ctx->adj_lx, &ctx->adj_ly, &ctx->adj_lvx, &ctx->adj_lvy, &ctx->adj_lm, &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm, &ctx->adj_lax, &ctx->adj_lay, &ctx->adj_lf, &ctx->adj_dL, &ctx->adj_dM, &ctx->adj_dMleaf, &ctx->ckpt, &ctx->seg};
     for (DevBuf *b : bufs) free_buf(*b);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -214,7 +214,7 @@ int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, doub
     if (n < 0 || n_max <= 0 || !bounds) return gx_fail(ctx, GX_ERR_INVALID_ARG, "bad n, n_max or bounds");
     if (n > 0 && (!x || !y || !m)) return gx_fail(ctx, GX_ERR_INVALID_ARG, "x, y and m are required");
     ctx->have_tree = false;
-    ctx->plan_ref_valid = ctx->plan_acc_valid = ctx->aux_valid = false;
+    ctx->plan_ref_valid = ctx->plan_acc_valid = ctx->aux_valid = ctx->roll_valid = false;
     GX_TRY(upload_bodies_impl(ctx, n, x, y, vx, vy, m, ax, ay));
     ctx->n_bodies = n;
     GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
@@ -251,7 +251,7 @@ int gx_upload_tree(gx_ctx *ctx, int64_t n_nodes, int64_t n_bodies, const double 
     if (ctx->cfg.max_nodes && (uint64_t)n_nodes > ctx->cfg.max_nodes)
         return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "n_nodes exceeds max_nodes");
     ctx->have_tree = false;
-    ctx->plan_ref_valid = ctx->plan_acc_valid = ctx->aux_valid = false;
+    ctx->plan_ref_valid = ctx->plan_acc_valid = ctx->aux_valid = ctx->roll_valid = false;
     // levels = height (compute_levels, lib.rs:426-438); Tree::build appends each
     // round contiguously, which the device passes rely on.
     std::vector<int32_t> lev((size_t)n_nodes);
@@ -379,6 +379,8 @@ static int ensure_plan(gx_ctx *ctx) {
     }
     return GX_OK;
 }
+
+int gx_ensure_plan_public(gx_ctx *ctx) { return ensure_plan(ctx); }
 
 int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64_t *n_p2p_interactions) {
     GX_TRY(check_ctx(ctx));

@@ -22,22 +22,31 @@
 
 namespace {
 
-// Factorials and binomials: constant-folded when the loops around them are
-// unrolled, evaluated by short loops otherwise.  Deliberately not recursive: a
-// recursive device function has no static stack bound, and with the large local
-// arrays of the high-order kernels that overflows the per-thread stack.
-__host__ __device__ constexpr double cfact(int n) {
-    double r = 1.0;
-    for (int i = 2; i <= n; i++) r *= (double)i;
-    return r;
+// Factorials and binomials come from a constant-memory table, filled by static
+// initialization from a constexpr builder: a table read is one constant-bank
+// operand whether or not the loop around it is unrolled (FP64 arithmetic is slow
+// on this part, so these must never be evaluated at run time).  The builder is
+// iterative: a recursive device function has no static stack bound.
+struct GxTables {
+    double fact[34];
+    double invfact[34];
+    double binom[17][17];
+};
+__host__ __device__ constexpr GxTables gx_make_tables() {
+    GxTables t{};
+    t.fact[0] = 1.0;
+    for (int i = 1; i < 34; i++) t.fact[i] = t.fact[i - 1] * (double)i;
+    for (int i = 0; i < 34; i++) t.invfact[i] = 1.0 / t.fact[i];
+    for (int n = 0; n < 17; n++) {
+        t.binom[n][0] = 1.0;
+        for (int k = 1; k <= n; k++) t.binom[n][k] = t.binom[n - 1][k - 1] + (k < n ? t.binom[n - 1][k] : 0.0);
+    }
+    return t;
 }
-__host__ __device__ constexpr double cinvfact(int n) { return 1.0 / cfact(n); }
-__host__ __device__ constexpr double cbinom(int n, int k) {
-    if (k < 0 || k > n) return 0.0;
-    double r = 1.0;  // C(n-k+i, i) after step i: every intermediate value is an integer
-    for (int i = 1; i <= k; i++) r = r * (double)(n - k + i) / (double)i;
-    return r;
-}
+__constant__ GxTables c_tab = gx_make_tables();
+__device__ __forceinline__ double cfact(int n) { return c_tab.fact[n]; }
+__device__ __forceinline__ double cinvfact(int n) { return c_tab.invfact[n]; }
+__device__ __forceinline__ double cbinom(int n, int k) { return (k < 0 || k > n) ? 0.0 : c_tab.binom[n][k]; }
 __host__ __device__ constexpr int nc2(int q) { return (q + 1) * (q + 2) / 2; }  // entries with k+l <= q
 
 // Loops over expansion indices are fully unrolled (coefficient arrays stay in
@@ -727,14 +736,14 @@ __global__ void __launch_bounds__(128) k_l2p_reduce32(int64_t nl, const float4 *
         float4 me = pos[i];
         float fx, fy;
         l2p_eval<P, float>(Lf + leaf * NS, me.x, me.y, fx, fy);
-        double sx = -(double)fx, sy = -(double)fy;
+        float sx = 0.f, sy = 0.f;
         for (int64_t it = i0; it < i1; it++) {
             float2 v = part[(it * tchunks + tc) * 32 + lane];
-            sx += (double)v.x;
-            sy += (double)v.y;
+            sx += v.x;
+            sy += v.y;
         }
-        ax[i] = sx;
-        ay[i] = sy;
+        ax[i] = (double)sx - (double)fx;
+        ay[i] = (double)sy - (double)fy;
     }
 }
 

@@ -107,6 +107,14 @@ struct gx_ctx {
     DevBuf Mf32, Lf32, Lff32;
     DevBuf pos32;  // mixed form: bodies as FP32 (x - com_leaf, y - com_leaf, m, 0)
 
+    // adjoint: cotangents, VJP outputs, transposed expansions, checkpoints
+    DevBuf adj_lx, adj_ly, adj_lvx, adj_lvy, adj_lm, adj_gx, adj_gy, adj_gm, adj_lax, adj_lay, adj_lf;
+    DevBuf adj_dL, adj_dM, adj_dMleaf;
+    DevBuf ckpt, seg;
+    int64_t roll_steps = 0, roll_k = 1;
+    double roll_dt = 0.0;
+    bool roll_valid = false;
+
     // scratch
     DevBuf scratch_a, scratch_b, scratch_c, scratch_d, scratch_e, scratch_f, scratch_g;
     DevBuf status;     // unsigned, device status word

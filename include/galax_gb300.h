@@ -157,6 +157,24 @@ int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, do
 int gx_n2_sampled_static(const double *x, const double *y, const double *m, int64_t n, double eps,
                          const int64_t *idx, int64_t n_idx, double *ax, double *ay, void *stream);
 
+/* Reverse mode (GX_MODE_ACCURATE).  Not in the reference: its north star asks for a
+ * backward() of the force operator.  gx_force_vjp returns, for cotangents lam of
+ * the accelerations of the resident bodies, g_x = sum lam . da/dx and
+ * g_m = sum lam . da/dm (host arrays, tree order), the exact transpose of the
+ * frozen-tree evaluation (L2P^T with the Hessian of the local expansion, L2L^T,
+ * M2L^T, M2M^T, P2M^T, Hessian-vector P2P), computed in FP64.  p in {1..6, 8}. */
+int gx_force_vjp(gx_ctx *ctx, const double *lam_x, const double *lam_y, double *gx, double *gy, double *gm);
+/* Leapfrog rollout from the resident state (simulate, galax-integrate/src/lib.rs:204-237)
+ * keeping (x, y, vx, vy) every checkpoint_every steps; the resident state ends at
+ * step n_steps. */
+int gx_rollout_forward(gx_ctx *ctx, int64_t n_steps, double dt, int64_t checkpoint_every);
+/* Reverse leapfrog of the last gx_rollout_forward: given dL/d(x, y, vx, vy) at the
+ * final step, returns dL/d(x, y, vx, vy) at step 0 and dL/dm.  Segments between
+ * checkpoints are recomputed (deterministically, so bit for bit); *peak_bytes (may be
+ * NULL) receives the device bytes of the checkpoint, segment and adjoint buffers. */
+int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const double *lvx, const double *lvy,
+                        double *gx0, double *gy0, double *gvx0, double *gvy0, double *gm, int64_t *peak_bytes);
+
 /* Device time of the last force evaluation per pass, in ms:
  * {total, prepare, p2m, m2m, m2l, l2l, l2p+p2p}; returns 7 entries. */
 int gx_last_timings(gx_ctx *ctx, double out[7]);

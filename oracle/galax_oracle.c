@@ -1488,3 +1488,84 @@ void gxo_compute_fmm_force_mac(double *x, double *y, double *m, double *ax, doub
     }
     free(mult); free(loc);
 }
+
+/* ------------------------------------------------------------ N^2 adjoint
+ * Not in the reference (it has no gradients): the exact FP64 vector-Jacobian product
+ * of the softened N^2 accelerations (compute_n2_force, lib.rs:1685-1721) and the
+ * reverse leapfrog over it, used as the reference gradient of the GPU adjoint.
+ *   a_i = sum_{k != i} m_k K(x_k - x_i),  K(d) = d (|d|^2+eps^2)^(-3/2)
+ *   g_x,i = sum_k J(x_k - x_i) (m_i lam_k - m_k lam_i),  J = I/r^3 - 3 d d^T/r^5
+ *   g_m,i = -sum_k lam_k . (x_k - x_i)/r^3 */
+void gxo_n2_vjp(const double *x, const double *y, const double *m, int64_t n, double eps, const double *lx,
+                const double *ly, double *gx, double *gy, double *gm) {
+    double s2 = eps * eps;
+#pragma omp parallel for schedule(static) num_threads(gxo_get_threads())
+    for (int64_t i = 0; i < n; i++) {
+        double ax = 0.0, ay = 0.0, am = 0.0;
+        for (int64_t k = 0; k < n; k++) {
+            if (k == i) continue;
+            double dx = x[k] - x[i], dy = y[k] - y[i];
+            double r2 = dx * dx + dy * dy + s2;
+            double ir = 1.0 / sqrt(r2);
+            double ir3 = ir * ir * ir, ir5 = ir3 * ir * ir;
+            double wx = m[i] * lx[k] - m[k] * lx[i], wy = m[i] * ly[k] - m[k] * ly[i];
+            double dw = dx * wx + dy * wy;
+            ax += ir3 * wx - 3.0 * ir5 * dx * dw;
+            ay += ir3 * wy - 3.0 * ir5 * dy * dw;
+            am -= (lx[k] * dx + ly[k] * dy) * ir3;
+        }
+        gx[i] = ax;
+        gy[i] = ay;
+        gm[i] = am;
+    }
+}
+
+/* Gradient at step 0 of a scalar loss of the final state for the N^2 leapfrog
+ * (leapfrog_kdk_n2, galax-integrate/src/lib.rs:241-255) from the final-state
+ * cotangents; all states are kept (small n). */
+void gxo_n2_rollout_grad(const double *x0, const double *y0, const double *vx0, const double *vy0, const double *m,
+                         int64_t n, double eps, double dt, int64_t T, const double *lxT, const double *lyT,
+                         const double *lvxT, const double *lvyT, double *gx, double *gy, double *gvx, double *gvy,
+                         double *gm) {
+    double h = 0.5 * dt;
+    double *X = (double *)malloc(sizeof(double) * n * (T + 1)), *Y = (double *)malloc(sizeof(double) * n * (T + 1));
+    double *vx = (double *)malloc(sizeof(double) * n), *vy = (double *)malloc(sizeof(double) * n);
+    double *ax = (double *)malloc(sizeof(double) * n), *ay = (double *)malloc(sizeof(double) * n);
+    memcpy(X, x0, sizeof(double) * n);
+    memcpy(Y, y0, sizeof(double) * n);
+    memcpy(vx, vx0, sizeof(double) * n);
+    memcpy(vy, vy0, sizeof(double) * n);
+    gxo_n2_force(X, Y, m, n, eps, ax, ay);
+    for (int64_t s = 0; s < T; s++) {
+        double *xp = X + s * n, *yp = Y + s * n, *xn = X + (s + 1) * n, *yn = Y + (s + 1) * n;
+        for (int64_t i = 0; i < n; i++) {
+            vx[i] += ax[i] * h;
+            vy[i] += ay[i] * h;
+            xn[i] = xp[i] + vx[i] * dt;
+            yn[i] = yp[i] + vy[i] * dt;
+        }
+        gxo_n2_force(xn, yn, m, n, eps, ax, ay);
+        for (int64_t i = 0; i < n; i++) {
+            vx[i] += ax[i] * h;
+            vy[i] += ay[i] * h;
+        }
+    }
+    double *lax = (double *)malloc(sizeof(double) * n), *lay = (double *)malloc(sizeof(double) * n);
+    double *tx = (double *)malloc(sizeof(double) * n), *ty = (double *)malloc(sizeof(double) * n);
+    double *tm = (double *)malloc(sizeof(double) * n);
+    memcpy(gx, lxT, sizeof(double) * n);
+    memcpy(gy, lyT, sizeof(double) * n);
+    memcpy(gvx, lvxT, sizeof(double) * n);
+    memcpy(gvy, lvyT, sizeof(double) * n);
+    memset(gm, 0, sizeof(double) * n);
+    for (int64_t s = T - 1; s >= -1; s--) {
+        double c = (s == T - 1) ? h : dt;
+        if (s == -1) c = h;
+        for (int64_t i = 0; i < n; i++) { lax[i] = c * gvx[i]; lay[i] = c * gvy[i]; }
+        gxo_n2_vjp(X + (s + 1) * n, Y + (s + 1) * n, m, n, eps, lax, lay, tx, ty, tm);
+        for (int64_t i = 0; i < n; i++) { gx[i] += tx[i]; gy[i] += ty[i]; gm[i] += tm[i]; }
+        if (s >= 0)
+            for (int64_t i = 0; i < n; i++) { gvx[i] += dt * gx[i]; gvy[i] += dt * gy[i]; }
+    }
+    free(X); free(Y); free(vx); free(vy); free(ax); free(ay); free(lax); free(lay); free(tx); free(ty); free(tm);
+}

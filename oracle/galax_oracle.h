@@ -144,6 +144,14 @@ void gxo_csr_free(gxo_csr *c);
 void gxo_compute_fmm_force_mac(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
                                const gxo_csr *far, const gxo_csr *near, int64_t p, double eps);
 
+/* ---- N^2 adjoint (not in the reference; the reference gradient of the GPU adjoint) ---- */
+void gxo_n2_vjp(const double *x, const double *y, const double *m, int64_t n, double eps, const double *lx,
+                const double *ly, double *gx, double *gy, double *gm);
+void gxo_n2_rollout_grad(const double *x0, const double *y0, const double *vx0, const double *vy0, const double *m,
+                         int64_t n, double eps, double dt, int64_t T, const double *lxT, const double *lyT,
+                         const double *lvxT, const double *lvyT, double *gx, double *gy, double *gvx, double *gvy,
+                         double *gm);
+
 void gxo_set_threads(int n);
 int gxo_get_threads(void);
 

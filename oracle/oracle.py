@@ -472,3 +472,32 @@ def mac_lists_build(t: Tree, radius: np.ndarray, theta: float):
 def compute_fmm_force_mac(b: Bodies, t: Tree, far: Csr, near: Csr, p: int, eps: float) -> None:
     _mac_setup().gxo_compute_fmm_force_mac(_d(b.x), _d(b.y), _d(b.mass), _d(b.ax), _d(b.ay), t.ptr, far.ptr, near.ptr,
                                            int(p), float(eps))
+
+
+# ------------------------------------------------------------ N^2 adjoint
+def _adj_setup():
+    L = lib()
+    if getattr(L, "_adj_ready", False):
+        return L
+    L.gxo_n2_vjp.argtypes = [_D, _D, _D, C.c_int64, C.c_double, _D, _D, _D, _D, _D]
+    L.gxo_n2_rollout_grad.argtypes = [_D] * 5 + [C.c_int64, C.c_double, C.c_double, C.c_int64] + [_D] * 9
+    L._adj_ready = True
+    return L
+
+
+def n2_vjp(x, y, m, eps, lx, ly):
+    x, y, m, lx, ly = (_arr(a) for a in (x, y, m, lx, ly))
+    n = x.size
+    gx, gy, gm = np.zeros(n), np.zeros(n), np.zeros(n)
+    _adj_setup().gxo_n2_vjp(_d(x), _d(y), _d(m), n, float(eps), _d(lx), _d(ly), _d(gx), _d(gy), _d(gm))
+    return gx, gy, gm
+
+
+def n2_rollout_grad(x0, y0, vx0, vy0, m, eps, dt, n_steps, lx, ly, lvx, lvy):
+    a = [_arr(v) for v in (x0, y0, vx0, vy0, m)]
+    t = [_arr(v) for v in (lx, ly, lvx, lvy)]
+    n = a[0].size
+    out = [np.zeros(n) for _ in range(5)]
+    _adj_setup().gxo_n2_rollout_grad(*[_d(v) for v in a], n, float(eps), float(dt), int(n_steps),
+                                     *[_d(v) for v in t], *[_d(o) for o in out])
+    return out

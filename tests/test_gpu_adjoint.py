@@ -1,0 +1,155 @@
+"""Reverse mode: the force VJP and the checkpointed reverse leapfrog (ACCURATE, FP64).
+
+Not in the reference (galax has no gradients); checked against central finite
+differences of the GPU forward with the tree frozen (h = 1e-6) and against the
+oracle's exact FP64 N^2 adjoint (gxo_n2_vjp / gxo_n2_rollout_grad).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(G, b, bounds, eps, p=4, theta=0.5):
+    n = len(b)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=p, eps64=eps))
+    ctx.build_tree(b, 32, bounds)  # permutes b into tree order
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_FP64, theta)
+    ctx.upload_bodies(b)
+    ctx.forces_resident()  # builds the plan (lists, radii) once: the tree is frozen from here
+    return ctx
+
+
+def _forces(ctx, x, y, m):
+    ax, ay = np.zeros(x.size), np.zeros(x.size)
+    ctx.compute_forces(x, y, m, ax, ay)
+    return ax, ay
+
+
+@pytest.mark.parametrize("preset,n,p", [("plummer", 20_000, 4), ("uniform", 8_000, 2), ("galaxy", 6_001, 6)])
+def test_force_vjp_matches_finite_differences(G, preset, n, p):
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=51)
+    ctx = _ctx(G, b, presets.BOUNDS[preset], 0.05, p=p)
+    rng = np.random.default_rng(1)
+    lx, ly = rng.standard_normal(n), rng.standard_normal(n)
+    gx, gy, gm = ctx.force_vjp(lx, ly)
+    scale = np.std(b.x)
+    for _ in range(3):
+        dx, dy, dm = rng.standard_normal(n), rng.standard_normal(n), rng.standard_normal(n) * b.mass
+        h = 1e-6 * scale
+        ap = _forces(ctx, b.x + h * dx, b.y + h * dy, b.mass + h * dm / scale)
+        am = _forces(ctx, b.x - h * dx, b.y - h * dy, b.mass - h * dm / scale)
+        fd = (np.dot(lx, ap[0] - am[0]) + np.dot(ly, ap[1] - am[1])) / (2 * h)
+        an = np.dot(gx, dx) + np.dot(gy, dy) + np.dot(gm, dm) / scale
+        assert abs(fd - an) <= 1e-6 * abs(fd), (fd, an)
+    ctx.close()
+
+
+def test_force_vjp_close_to_exact_n2_adjoint(G, oracle):
+    """The VJP of the FMM approximates the VJP of the exact sum to FMM accuracy."""
+    from galax_gb300 import presets
+    n = 10_000
+    b = presets.plummer(n, seed=52)
+    ctx = _ctx(G, b, presets.BOUNDS["plummer"], 0.05)
+    rng = np.random.default_rng(2)
+    lx, ly = rng.standard_normal(n), rng.standard_normal(n)
+    gx, gy, gm = ctx.force_vjp(lx, ly)
+    rx, ry, rm = oracle.n2_vjp(b.x, b.y, b.mass, 0.05, lx, ly)
+    ctx.close()
+    ex = np.linalg.norm(np.hypot(gx - rx, gy - ry)) / np.linalg.norm(np.hypot(rx, ry))
+    em = np.linalg.norm(gm - rm) / np.linalg.norm(rm)
+    assert ex < 2e-3 and em < 2e-3, (ex, em)
+
+
+def _rot(theta):
+    c, s = np.cos(theta), np.sin(theta)
+    return np.array([[c, -s], [s, c]])
+
+
+def _loss_and_grads(x0, y0, xT, yT, R):
+    """L = sum |x_T - R x_0|^2 (the rollout loss of the benchmark's adjoint config)."""
+    tx = R[0, 0] * x0 + R[0, 1] * y0
+    ty = R[1, 0] * x0 + R[1, 1] * y0
+    rx, ry = xT - tx, yT - ty
+    L = float(np.sum(rx * rx + ry * ry))
+    # dL/dx_T and the direct dL/dx_0 = -2 R^T (x_T - R x_0)
+    return L, 2 * rx, 2 * ry, -2 * (R[0, 0] * rx + R[1, 0] * ry), -2 * (R[0, 1] * rx + R[1, 1] * ry)
+
+
+def _rollout(ctx, G, b, n_steps, dt):
+    ctx.upload_bodies(b)
+    ctx.forces_resident()
+    ctx.kdk_run(n_steps, dt, 0)
+    out = G.Bodies.new(len(b))
+    ctx.download_bodies(out)
+    return out
+
+
+@pytest.mark.parametrize("k", [1, 4, 20])
+def test_rollout_gradient_matches_finite_differences(G, k):
+    from galax_gb300 import presets
+    n, T, dt = 4_001, 20, 2e-3
+    b = presets.galaxy(n, seed=53)
+    ctx = _ctx(G, b, presets.BOUNDS["galaxy"], 0.05)
+    R = _rot(0.3)
+    ctx.upload_bodies(b)
+    ctx.rollout_forward(T, dt, k)
+    fin = G.Bodies.new(n)
+    ctx.download_bodies(fin)
+    L, lxT, lyT, dx0, dy0 = _loss_and_grads(b.x, b.y, fin.x, fin.y, R)
+    gx, gy, gvx, gvy, gm, peak = ctx.rollout_backward(lxT, lyT, np.zeros(n), np.zeros(n))
+    gx, gy = gx + dx0, gy + dy0
+    assert peak > 0
+    rng = np.random.default_rng(3)
+    for _ in range(3):
+        d = [rng.standard_normal(n) for _ in range(4)] + [rng.standard_normal(n) * b.mass]
+        h = 1e-6
+        def L_at(sign):
+            p = G.Bodies.from_arrays(b.x + sign * h * d[0], b.y + sign * h * d[1], b.mass + sign * h * d[4],
+                                     b.vx + sign * h * d[2], b.vy + sign * h * d[3])
+            f = _rollout(ctx, G, p, T, dt)
+            return _loss_and_grads(p.x, p.y, f.x, f.y, R)[0]
+        fd = (L_at(1) - L_at(-1)) / (2 * h)
+        an = np.dot(gx, d[0]) + np.dot(gy, d[1]) + np.dot(gvx, d[2]) + np.dot(gvy, d[3]) + np.dot(gm, d[4])
+        assert abs(fd - an) <= 1e-5 * abs(fd), (fd, an)
+    ctx.close()
+
+
+def test_checkpoint_interval_does_not_change_the_gradient(G):
+    """Recomputed segments are bit-identical to the forward pass."""
+    from galax_gb300 import presets
+    n, T, dt = 3_001, 12, 2e-3
+    b = presets.galaxy(n, seed=54)
+    ctx = _ctx(G, b, presets.BOUNDS["galaxy"], 0.05)
+    res = []
+    for k in (1, 5, 12):
+        ctx.upload_bodies(b)
+        ctx.rollout_forward(T, dt, k)
+        fin = G.Bodies.new(n)
+        ctx.download_bodies(fin)
+        res.append(ctx.rollout_backward(fin.x, fin.y, fin.vx, np.zeros(n))[:5])
+    ctx.close()
+    for r in res[1:]:
+        for a, c in zip(r, res[0]):
+            assert np.array_equal(a, c)
+
+
+def test_rollout_gradient_close_to_exact_n2_adjoint(G, oracle):
+    """The FMM rollout gradient against the exact FP64 N^2 reverse leapfrog (2000 bodies)."""
+    from galax_gb300 import presets
+    n, T, dt = 2_000, 10, 2e-3
+    b = presets.galaxy(n, seed=55)
+    ctx = _ctx(G, b, presets.BOUNDS["galaxy"], 0.05)
+    R = _rot(-0.7)
+    ctx.upload_bodies(b)
+    ctx.rollout_forward(T, dt, 3)
+    fin = G.Bodies.new(n)
+    ctx.download_bodies(fin)
+    L, lxT, lyT, dx0, dy0 = _loss_and_grads(b.x, b.y, fin.x, fin.y, R)
+    g = ctx.rollout_backward(lxT, lyT, np.zeros(n), np.zeros(n))
+    ctx.close()
+    r = oracle.n2_rollout_grad(b.x, b.y, b.vx, b.vy, b.mass, 0.05, dt, T, lxT, lyT, np.zeros(n), np.zeros(n))
+    for k in range(5):
+        err = np.linalg.norm(g[k] - r[k]) / np.linalg.norm(r[k])
+        assert err < 1e-3, (k, err)
