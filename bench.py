@@ -169,6 +169,125 @@ def run_reference(args, rank, world, pg):
     return 0
 
 
+def _rot(theta):
+    c, s = np.cos(theta), np.sin(theta)
+    return np.array([[c, -s], [s, c]])
+
+
+def _rollout_loss(x0, y0, xT, yT, R):
+    """L = sum |x_T - R x_0|^2 and its partials dL/dx_T, dL/dx_0 (direct term)."""
+    tx = R[0, 0] * x0 + R[0, 1] * y0
+    ty = R[1, 0] * x0 + R[1, 1] * y0
+    rx, ry = xT - tx, yT - ty
+    return (float(np.sum(rx * rx + ry * ry)), 2 * rx, 2 * ry, -2 * (R[0, 0] * rx + R[1, 0] * ry),
+            -2 * (R[0, 1] * rx + R[1, 1] * ry))
+
+
+def _adjoint_run(G, ctx, b, T, dt, k, R):
+    """One forward rollout and its reverse pass; returns times, gradients and peak bytes."""
+    n = len(b)
+    ctx.upload_bodies(b)
+    t0 = time.perf_counter()
+    ctx.rollout_forward(T, dt, k)
+    t_fwd = time.perf_counter() - t0
+    fin = G.Bodies.new(n)
+    ctx.download_bodies(fin)
+    L, lxT, lyT, dx0, dy0 = _rollout_loss(b.x, b.y, fin.x, fin.y, R)
+    z = np.zeros(n)
+    t0 = time.perf_counter()
+    gx, gy, gvx, gvy, gm, peak = ctx.rollout_backward(lxT, lyT, z, z)
+    t_bwd = time.perf_counter() - t0
+    return t_fwd, t_bwd, (gx + dx0, gy + dy0, gvx, gvy, gm), peak, L
+
+
+def _loss_only(G, ctx, b, T, dt, R):
+    n = len(b)
+    ctx.upload_bodies(b)
+    ctx.forces_resident()
+    ctx.kdk_run(T, dt, 0)
+    fin = G.Bodies.new(n)
+    ctx.download_bodies(fin)
+    return _rollout_loss(b.x, b.y, fin.x, fin.y, R)[0]
+
+
+def _grad_rel(g, r):
+    return float(max(np.linalg.norm(a - c) / max(np.linalg.norm(c), 1e-300) for a, c in zip(g, r)))
+
+
+def run_adjoint(G, presets, ctx1m, b1m, args):
+    """Reverse-mode rollouts: galaxy N=200,001 x 100 steps (FP64 and mixed; central
+    finite differences of the FP64 rollout along seeded directions) and Plummer N=1M x
+    500 steps at dt=1e-3 (mixed; checkpoint interval sweep, gradient against the FP64
+    GPU adjoint on a 20-step prefix).  The comparison with the exact FP64 N^2 adjoint
+    on a 2000-body subset is a test (tests/test_gpu_adjoint.py)."""
+    out = {}
+    # ---- galaxy, N = 200,001, 100 steps
+    n, T = 200_001, 100
+    bg = presets.galaxy(n, seed=args.seed + 4)
+    cg = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 24, p=P, eps64=0.1))
+    cg.build_tree(bg, N_MAX, presets.BOUNDS["galaxy"])
+    eps = presets.cli_softening(bg.x, bg.y)
+    cg.set_params(P, eps)
+    cg.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
+    cg.upload_bodies(bg)
+    cg.forces_resident()
+    a0 = G.Bodies.new(n)
+    cg.download_bodies(a0)
+    dt = presets.cli_dt(a0.ax, a0.ay)
+    R = _rot(float(np.random.default_rng(args.seed + 5).uniform(0, 2 * np.pi)))
+    k = 10
+    gal = {"workload": f"galaxy N={n}, p={P}, n_max={N_MAX}, {T} steps, dt={dt:.4g} (CLI rule), "
+                       f"checkpoint every {k} steps", "eps": eps}
+    grads = {}
+    for name, prec in (("fp64", G.PREC_FP64), ("mixed", G.PREC_MIXED)):
+        cg.set_mode(G.MODE_ACCURATE, prec, THETA)
+        _adjoint_run(G, cg, bg, 5, dt, k, R)  # warm-up
+        tf, tb, g, peak, L = _adjoint_run(G, cg, bg, T, dt, k, R)
+        grads[name] = g
+        gal[name] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak}
+    gal["mixed"]["grad_rel_err_vs_fp64"] = _grad_rel(grads["mixed"], grads["fp64"])
+    # central finite differences of the FP64 rollout, h = 1e-6, seeded directions
+    cg.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
+    rng = np.random.default_rng(args.seed + 6)
+    fd = []
+    h = 1e-6
+    for _ in range(args.fd_dirs):
+        d = [rng.standard_normal(n) for _ in range(4)] + [rng.standard_normal(n) * bg.mass]
+        def L_at(sg):
+            pb = G.Bodies.from_arrays(bg.x + sg * h * d[0], bg.y + sg * h * d[1], bg.mass + sg * h * d[4],
+                                      bg.vx + sg * h * d[2], bg.vy + sg * h * d[3])
+            return _loss_only(G, cg, pb, T, dt, R)
+        num = (L_at(1) - L_at(-1)) / (2 * h)
+        g = grads["fp64"]
+        an = sum(float(np.dot(g[q], d[q])) for q in range(5))
+        fd.append(abs(num - an) / abs(num))
+    gal["fp64"]["fd_rel_err_max"] = float(max(fd)) if fd else None
+    gal["fp64"]["fd_directions"] = args.fd_dirs
+    cg.close()
+    out["galaxy_200k"] = gal
+
+    # ---- Plummer 1M, 500 steps at dt = 1e-3, mixed, checkpoint sweep
+    T, dt = args.adj_steps, 1e-3
+    Rp = _rot(float(np.random.default_rng(args.seed + 8).uniform(0, 2 * np.pi)))
+    ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
+    sweep = {}
+    for k in args.adj_k:
+        _adjoint_run(G, ctx1m, b1m, 3, dt, k, Rp)  # warm-up (allocations)
+        tf, tb, g, peak, L = _adjoint_run(G, ctx1m, b1m, T, dt, k, Rp)
+        sweep[str(k)] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak}
+    # gradient of a 20-step prefix: mixed against FP64 (the FP64 form is ~50x slower)
+    Tp = 20
+    _, _, gm20, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp)
+    ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
+    _, _, g64, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp)
+    ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
+    out["plummer_1m"] = {"workload": f"plummer N={len(b1m)}, p={P}, n_max={N_MAX}, {T} steps, dt={dt}, mixed",
+                         "checkpoint_sweep": sweep,
+                         "grad_rel_err_mixed_vs_fp64_20_steps": _grad_rel(gm20, g64)}
+    return out
+
+
+
 def run_ours(args, rank, world, local, pg):
     import galax_gb300 as G
     from galax_gb300 import build as gbuild
@@ -242,6 +361,9 @@ def run_ours(args, rank, world, local, pg):
     e2e_ms = _max_over_ranks(pg, float(np.mean(e2e_t)) * 1e3)
     peak32 = ctx.probe_fp32_tflops()
 
+    adjoint = None
+    if not args.no_adjoint and world == 1:
+        adjoint = run_adjoint(G, presets, ctx, gb, args)
     mix = res["mixed"]
     ms_step = _max_over_ranks(pg, float(np.mean(mix["ms"])))
     kms = float(np.mean(mix["kms"]))
@@ -282,7 +404,13 @@ def run_ours(args, rank, world, local, pg):
                           "median_rel_diff": float(np.median(d))},
         "tree": {"nodes": nn, "leaves": nl, "levels": nlev, "build_s_incl_host_copies": setup_tree_s},
         "cpu_baseline": cpu,
+        "adjoint": adjoint if adjoint is not None else "not run (--no-adjoint, or N>1 replicas: see the N=1 line)",
     }
+    if adjoint is not None:
+        sw = adjoint["plummer_1m"]["checkpoint_sweep"]
+        kk = "22" if "22" in sw else next(iter(sw))
+        line["adjoint_over_forward"] = {"value": sw[kk]["adjoint_over_forward"], "checkpoint_every": int(kk),
+                                        "workload": adjoint["plummer_1m"]["workload"]}
     print(json.dumps(line), flush=True)
     ctx.close()
     return 0
@@ -297,6 +425,10 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-steps", type=int, default=500)
+    ap.add_argument("--adj-k", type=lambda s: [int(v) for v in s.split(",")], default=[10, 22, 50, 1])
+    ap.add_argument("--fd-dirs", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -7,60 +7,77 @@
 //   la = c lv with c = h (each interior a_{n+1} feeds two half kicks) or h/2 at n+1 = T
 //   (gx, gm) = VJP_F(x_{n+1}; la);  lx += gx;  lm += gm
 //   lv += h lx;  (lx, lv) now hold dL/dx_n, dL/dv_n
-// and finally VJP_F(x_0; h/2 lv_0).  States are recomputed from checkpoints taken
-// every k steps; the kernels are deterministic, so the recomputed states are the
-// forward ones bit for bit.
+// and finally VJP_F(x_0; h/2 lv_0).  The forward keeps a checkpoint every k steps
+// (positions, velocities, accelerations and the leaf locals of that evaluation); the
+// backward recomputes the k-1 interior states of each segment from its checkpoint
+// (k = 1 stores every state and recomputes nothing).  The kernels are deterministic,
+// so the recomputed states are the forward ones bit for bit.
 #include "gx_internal.cuh"
 
-int gx_run_force_vjp_1(gx_ctx *, const double *, const double *, double *, double *, double *);
-int gx_run_force_vjp_2(gx_ctx *, const double *, const double *, double *, double *, double *);
-int gx_run_force_vjp_3(gx_ctx *, const double *, const double *, double *, double *, double *);
-int gx_run_force_vjp_4(gx_ctx *, const double *, const double *, double *, double *, double *);
-int gx_run_force_vjp_5(gx_ctx *, const double *, const double *, double *, double *, double *);
-int gx_run_force_vjp_6(gx_ctx *, const double *, const double *, double *, double *, double *);
-int gx_run_force_vjp_8(gx_ctx *, const double *, const double *, double *, double *, double *);
+#define GX_VJP_DECL(PP)                                                                                 \
+    int gx_run_force_vjp_##PP(gx_ctx *, int, const double *, const double *, const void *, const double *, \
+                              const double *, double *, double *, double *);
+GX_VJP_DECL(1)
+GX_VJP_DECL(2)
+GX_VJP_DECL(3)
+GX_VJP_DECL(4)
+GX_VJP_DECL(5)
+GX_VJP_DECL(6)
+GX_VJP_DECL(8)
 
 namespace {
 
-int force_vjp(gx_ctx *ctx, const double *lx, const double *ly, double *gx, double *gy, double *gm) {
+// VJP at positions (X, Y) with the forward's leaf locals lf of those positions, in the
+// context's precision (FP32 rows for the mixed form, FP64 rows otherwise).
+int force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf, const double *lx, const double *ly,
+              double *gx, double *gy, double *gm) {
+    int f32 = ctx->prec == GX_PREC_MIXED;
     switch (ctx->p) {
-        case 1: return gx_run_force_vjp_1(ctx, lx, ly, gx, gy, gm);
-        case 2: return gx_run_force_vjp_2(ctx, lx, ly, gx, gy, gm);
-        case 3: return gx_run_force_vjp_3(ctx, lx, ly, gx, gy, gm);
-        case 4: return gx_run_force_vjp_4(ctx, lx, ly, gx, gy, gm);
-        case 5: return gx_run_force_vjp_5(ctx, lx, ly, gx, gy, gm);
-        case 6: return gx_run_force_vjp_6(ctx, lx, ly, gx, gy, gm);
-        case 8: return gx_run_force_vjp_8(ctx, lx, ly, gx, gy, gm);
+        case 1: return gx_run_force_vjp_1(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
+        case 2: return gx_run_force_vjp_2(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
+        case 3: return gx_run_force_vjp_3(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
+        case 4: return gx_run_force_vjp_4(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
+        case 5: return gx_run_force_vjp_5(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
+        case 6: return gx_run_force_vjp_6(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
+        case 8: return gx_run_force_vjp_8(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         default: return gx_fail(ctx, GX_ERR_INVALID_ARG, "the adjoint supports p in {1,2,3,4,5,6,8}");
     }
 }
 
-int row_stride_f64(int p) {
-    int nc = (p + 1) * (p + 2) / 2;
-    return (nc + 1) / 2 * 2;
+// bytes of one set of leaf locals in the context's precision, rounded up to 256
+size_t lf_bytes(const gx_ctx *ctx) {
+    int nc = (ctx->p + 1) * (ctx->p + 2) / 2;
+    size_t row = ctx->prec == GX_PREC_MIXED ? sizeof(float) * (size_t)((nc + 3) / 4 * 4)
+                                            : sizeof(double) * (size_t)((nc + 1) / 2 * 2);
+    size_t b = row * (size_t)(ctx->n_leaves > 0 ? ctx->n_leaves : 1);
+    return (b + 255) / 256 * 256;
 }
-int row_stride_f32(int p) {
-    int nc = (p + 1) * (p + 2) / 2;
-    return (nc + 3) / 4 * 4;
-}
-
-// FP32 leaf locals (mixed forward) -> FP64 rows for the VJP
-__global__ void k_widen_rows(int64_t nl, int nc, int ns32, int ns64, const float *in, double *out) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nl * nc) return;
-    int64_t leaf = i / nc;
-    int k = (int)(i % nc);
-    out[leaf * ns64 + k] = (double)in[leaf * ns32 + k];
-}
+// the leaf locals of the last forward evaluation
+const void *current_lf(const gx_ctx *ctx) { return ctx->prec == GX_PREC_MIXED ? ctx->Lff32.p : ctx->Lf.p; }
 
 __global__ void k_axpy(int64_t n, double a, const double *x, double *y) {  // y += a x
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = __dadd_rn(y[i], __dmul_rn(a, x[i]));
 }
 
-__global__ void k_scale(int64_t n, double a, const double *x, double *y) {  // y = a x
+// lx += gx; ly += gy; lm += gm; lvx += dt lx; lvy += dt ly (one reverse leapfrog step)
+__global__ void k_adj_step(int64_t n, double dt, const double *gx, const double *gy, const double *gm, double *lx,
+                           double *ly, double *lm, double *lvx, double *lvy) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = a * x[i];
+    if (i >= n) return;
+    double a = __dadd_rn(lx[i], gx[i]), b = __dadd_rn(ly[i], gy[i]);
+    lx[i] = a;
+    ly[i] = b;
+    lm[i] = __dadd_rn(lm[i], gm[i]);
+    lvx[i] = __dadd_rn(lvx[i], __dmul_rn(dt, a));
+    lvy[i] = __dadd_rn(lvy[i], __dmul_rn(dt, b));
+}
+
+__global__ void k_scale2(int64_t n, double c, const double *x, const double *y, double *ox, double *oy) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    ox[i] = __dmul_rn(c, x[i]);
+    oy[i] = __dmul_rn(c, y[i]);
 }
 
 __global__ void k_kick_drift_a(int64_t n, double h, double dt, double *x, double *y, double *vx, double *vy,
@@ -89,37 +106,20 @@ int check_mode(gx_ctx *ctx) {
     return GX_OK;
 }
 
-// Forward evaluation at the resident positions, then its FP64 leaf locals into dst
-// (stride row_stride_f64) for the VJP.
-int forward_with_locals(gx_ctx *ctx, double *dst_lf) {
-    GX_TRY(gx_forces_device(ctx, false));
-    int64_t nl = ctx->n_leaves;
-    int nc = (ctx->p + 1) * (ctx->p + 2) / 2, ns64 = row_stride_f64(ctx->p);
-    if (ctx->prec == GX_PREC_MIXED) {
-        k_widen_rows<<<gx_blocks(nl * nc, 256), 256, 0, ctx->stream>>>(nl, nc, row_stride_f32(ctx->p), ns64,
-                                                                       dptr<float>(ctx->Lff32), dst_lf);
-        ctx->launches++;
-    } else {
-        GX_CUDA(ctx, cudaMemcpyAsync(dst_lf, ctx->Lf.p, sizeof(double) * ns64 * (size_t)nl, cudaMemcpyDeviceToDevice,
-                                     ctx->stream));
-    }
-    return GX_OK;
-}
-
-// VJP at stored positions (px, py) with stored leaf locals lf.
-int vjp_at(gx_ctx *ctx, const double *px, const double *py, const double *lf, const double *lx, const double *ly,
-           double *gx, double *gy, double *gm) {
-    int64_t n = ctx->n_bodies, nl = ctx->n_leaves;
-    int ns64 = row_stride_f64(ctx->p);
-    if (px != dptr<double>(ctx->x))
-        GX_CUDA(ctx, cudaMemcpyAsync(ctx->x.p, px, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (py != dptr<double>(ctx->y))
-        GX_CUDA(ctx, cudaMemcpyAsync(ctx->y.p, py, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
-    GX_TRY(gx_ensure(ctx, ctx->Lf, sizeof(double) * ns64 * (size_t)(nl > 0 ? nl : 1)));
-    if (lf != dptr<double>(ctx->Lf))
-        GX_CUDA(ctx, cudaMemcpyAsync(ctx->Lf.p, lf, sizeof(double) * ns64 * (size_t)nl, cudaMemcpyDeviceToDevice,
-                                     ctx->stream));
-    return force_vjp(ctx, lx, ly, gx, gy, gm);
+// Checkpoint slot j holds the state after min(j K, T) steps: x, y, vx, vy, ax, ay
+// (FP64) and the leaf locals of its force evaluation.
+struct Slots {
+    char *base;
+    size_t stride, lfoff;
+    int64_t n;
+    double *x(int64_t j) const { return reinterpret_cast<double *>(base + (size_t)j * stride); }
+    double *arr(int64_t j, int k) const { return x(j) + (size_t)k * (size_t)n; }
+    void *lf(int64_t j) const { return base + (size_t)j * stride + lfoff; }
+};
+Slots ckpt_slots(gx_ctx *ctx) {
+    int64_t n = ctx->n_bodies > 0 ? ctx->n_bodies : 1;
+    size_t lfoff = (sizeof(double) * 6 * (size_t)n + 255) / 256 * 256;
+    return Slots{reinterpret_cast<char *>(ctx->ckpt.p), lfoff + lf_bytes(ctx), lfoff, n};
 }
 
 }  // namespace
@@ -132,18 +132,17 @@ int gx_force_vjp(gx_ctx *ctx, const double *lam_x, const double *lam_y, double *
     if (!lam_x || !lam_y || !gx || !gy || !gm) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null array");
     extern int gx_ensure_plan_public(gx_ctx *);
     GX_TRY(gx_ensure_plan_public(ctx));
-    int64_t n = ctx->n_bodies, nl = ctx->n_leaves;
+    int64_t n = ctx->n_bodies;
     size_t b = sizeof(double) * (size_t)(n > 0 ? n : 1);
     DevBuf *bufs[] = {&ctx->adj_lx, &ctx->adj_ly, &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm};
     for (DevBuf *d : bufs) GX_TRY(gx_ensure(ctx, *d, b));
-    GX_TRY(gx_ensure(ctx, ctx->adj_lf, sizeof(double) * row_stride_f64(ctx->p) * (size_t)(nl > 0 ? nl : 1)));
     if (n == 0) return GX_OK;
     GX_CUDA(ctx, cudaMemcpyAsync(ctx->adj_lx.p, lam_x, b, cudaMemcpyHostToDevice, ctx->stream));
     GX_CUDA(ctx, cudaMemcpyAsync(ctx->adj_ly.p, lam_y, b, cudaMemcpyHostToDevice, ctx->stream));
-    GX_TRY(forward_with_locals(ctx, dptr<double>(ctx->adj_lf)));
-    GX_TRY(vjp_at(ctx, dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->adj_lf), dptr<double>(ctx->adj_lx),
-                  dptr<double>(ctx->adj_ly), dptr<double>(ctx->adj_gx), dptr<double>(ctx->adj_gy),
-                  dptr<double>(ctx->adj_gm)));
+    GX_TRY(gx_forces_device(ctx, false));  // the locals of the resident positions
+    GX_TRY(force_vjp(ctx, dptr<double>(ctx->x), dptr<double>(ctx->y), current_lf(ctx), dptr<double>(ctx->adj_lx),
+                     dptr<double>(ctx->adj_ly), dptr<double>(ctx->adj_gx), dptr<double>(ctx->adj_gy),
+                     dptr<double>(ctx->adj_gm)));
     GX_CUDA(ctx, cudaMemcpyAsync(gx, ctx->adj_gx.p, b, cudaMemcpyDeviceToHost, ctx->stream));
     GX_CUDA(ctx, cudaMemcpyAsync(gy, ctx->adj_gy.p, b, cudaMemcpyDeviceToHost, ctx->stream));
     GX_CUDA(ctx, cudaMemcpyAsync(gm, ctx->adj_gm.p, b, cudaMemcpyDeviceToHost, ctx->stream));
@@ -157,35 +156,44 @@ int gx_rollout_forward(gx_ctx *ctx, int64_t n_steps, double dt, int64_t checkpoi
     if (n_steps < 0 || checkpoint_every <= 0) return gx_fail(ctx, GX_ERR_INVALID_ARG, "bad n_steps or interval");
     extern int gx_ensure_plan_public(gx_ctx *);
     GX_TRY(gx_ensure_plan_public(ctx));
-    int64_t n = ctx->n_bodies;
-    int64_t nck = n_steps / checkpoint_every + 1;
-    GX_TRY(gx_ensure(ctx, ctx->ckpt, sizeof(double) * 4 * (size_t)(n > 0 ? n : 1) * (size_t)nck));
-    double *ck = dptr<double>(ctx->ckpt);
-    double h = 0.5 * dt;
-    auto save = [&](int64_t slot) -> int {
-        DevBuf *src[4] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy};
-        for (int k = 0; k < 4; k++)
-            GX_CUDA(ctx, cudaMemcpyAsync(ck + ((size_t)slot * 4 + k) * (size_t)n, src[k]->p, sizeof(double) * n,
-                                         cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->roll_valid = false;
+    const int64_t n = ctx->n_bodies, T = n_steps, K = checkpoint_every;
+    const int64_t nseg = (T + K - 1) / K;
+    size_t lfb = lf_bytes(ctx);
+    {
+        int64_t nn = n > 0 ? n : 1;
+        size_t stride = (sizeof(double) * 6 * (size_t)nn + 255) / 256 * 256 + lfb;
+        GX_TRY(gx_ensure(ctx, ctx->ckpt, stride * (size_t)(nseg + 1)));
+    }
+    Slots S = ckpt_slots(ctx);
+    const double h = 0.5 * dt;
+    const unsigned g = gx_blocks(n, 256);
+    DevBuf *st[6] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->ax, &ctx->ay};
+    auto save = [&](int64_t j) -> int {
+        for (int k = 0; k < 6; k++)
+            GX_CUDA(ctx, cudaMemcpyAsync(S.arr(j, k), st[k]->p, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                         ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(S.lf(j), current_lf(ctx), lfb, cudaMemcpyDeviceToDevice, ctx->stream));
         return GX_OK;
     };
     GX_TRY(gx_forces_device(ctx, false));  // a_0
     GX_TRY(save(0));
-    for (int64_t s = 0; s < n_steps; s++) {
-        k_kick_drift_a<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(n, h, dt, dptr<double>(ctx->x), dptr<double>(ctx->y),
-                                                                   dptr<double>(ctx->vx), dptr<double>(ctx->vy),
-                                                                   dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+    for (int64_t s = 0; s < T; s++) {
+        k_kick_drift_a<<<g, 256, 0, ctx->stream>>>(n, h, dt, dptr<double>(ctx->x), dptr<double>(ctx->y),
+                                                   dptr<double>(ctx->vx), dptr<double>(ctx->vy), dptr<double>(ctx->ax),
+                                                   dptr<double>(ctx->ay));
         GX_TRY(gx_forces_device(ctx, false));
-        k_kick_a<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(n, h, dptr<double>(ctx->vx), dptr<double>(ctx->vy),
-                                                             dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+        k_kick_a<<<g, 256, 0, ctx->stream>>>(n, h, dptr<double>(ctx->vx), dptr<double>(ctx->vy),
+                                             dptr<double>(ctx->ax), dptr<double>(ctx->ay));
         ctx->launches += 2;
-        if ((s + 1) % checkpoint_every == 0) GX_TRY(save((s + 1) / checkpoint_every));
+        if ((s + 1) % K == 0 || s + 1 == T) GX_TRY(save((s + 1 + K - 1) / K));
     }
     GX_CUDA(ctx, cudaGetLastError());
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    ctx->roll_steps = n_steps;
+    ctx->roll_steps = T;
     ctx->roll_dt = dt;
-    ctx->roll_k = checkpoint_every;
+    ctx->roll_k = K;
+    ctx->roll_prec = ctx->prec;
     ctx->roll_valid = true;
     return GX_OK;
 }
@@ -195,30 +203,30 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
     if (!ctx) return GX_ERR_INVALID_ARG;
     GX_TRY(check_mode(ctx));
     if (!ctx->roll_valid) return gx_fail(ctx, GX_ERR_STATE, "gx_rollout_backward needs gx_rollout_forward first");
+    if (ctx->roll_prec != ctx->prec)
+        return gx_fail(ctx, GX_ERR_STATE, "the precision changed between gx_rollout_forward and gx_rollout_backward");
     if (!lx || !ly || !lvx || !lvy || !gx0 || !gy0 || !gvx0 || !gvy0 || !gm)
         return gx_fail(ctx, GX_ERR_INVALID_ARG, "null array");
-    int64_t n = ctx->n_bodies, nl = ctx->n_leaves, T = ctx->roll_steps, K = ctx->roll_k;
-    double dt = ctx->roll_dt, h = 0.5 * dt;
-    int ns64 = row_stride_f64(ctx->p);
-    size_t b = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    const int64_t n = ctx->n_bodies, T = ctx->roll_steps, K = ctx->roll_k;
+    const int64_t nseg = (T + K - 1) / K;
+    const double dt = ctx->roll_dt, h = 0.5 * dt;
+    const size_t b = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    const size_t lfb = lf_bytes(ctx);
     // adjoint state (lx, ly, lvx, lvy, lm), VJP outputs (gx, gy, gm), la
     DevBuf *bufs[] = {&ctx->adj_lx, &ctx->adj_ly, &ctx->adj_lvx, &ctx->adj_lvy, &ctx->adj_lm,
                       &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm, &ctx->adj_lax, &ctx->adj_lay};
     for (DevBuf *d : bufs) GX_TRY(gx_ensure(ctx, *d, b));
-    // segment storage: positions and FP64 leaf locals of up to K+1 states
-    size_t seg_pos = 2 * (size_t)(n > 0 ? n : 1), seg_lf = (size_t)ns64 * (size_t)(nl > 0 ? nl : 1);
-    GX_TRY(gx_ensure(ctx, ctx->seg, sizeof(double) * (seg_pos + seg_lf) * (size_t)(K + 1)));
-    if (peak_bytes)
-        *peak_bytes = (int64_t)(ctx->ckpt.bytes + ctx->seg.bytes + 10 * b + ctx->adj_dL.bytes + ctx->adj_dM.bytes +
-                                ctx->adj_dMleaf.bytes);
+    // recomputed interior states of a segment: positions and leaf locals of up to K-1 states
+    const size_t seg_stride = (2 * b + 255) / 256 * 256 + lfb;
+    GX_TRY(gx_ensure(ctx, ctx->seg, seg_stride * (size_t)(K > 1 ? K - 1 : 1)));
+    Slots S = ckpt_slots(ctx);
+    char *seg = reinterpret_cast<char *>(ctx->seg.p);
+    auto seg_x = [&](int64_t j) { return reinterpret_cast<double *>(seg + (size_t)j * seg_stride); };
+    auto seg_l = [&](int64_t j) { return static_cast<void *>(seg + (size_t)j * seg_stride + (2 * b + 255) / 256 * 256); };
     double *LX = dptr<double>(ctx->adj_lx), *LY = dptr<double>(ctx->adj_ly), *LVX = dptr<double>(ctx->adj_lvx),
            *LVY = dptr<double>(ctx->adj_lvy), *LM = dptr<double>(ctx->adj_lm), *GX = dptr<double>(ctx->adj_gx),
            *GY = dptr<double>(ctx->adj_gy), *GM = dptr<double>(ctx->adj_gm), *LAX = dptr<double>(ctx->adj_lax),
            *LAY = dptr<double>(ctx->adj_lay);
-    double *seg = dptr<double>(ctx->seg), *ck = dptr<double>(ctx->ckpt);
-    auto seg_x = [&](int64_t j) { return seg + (size_t)j * (seg_pos + seg_lf); };
-    auto seg_y = [&](int64_t j) { return seg_x(j) + n; };
-    auto seg_l = [&](int64_t j) { return seg_x(j) + seg_pos; };
     if (n > 0) {
         GX_CUDA(ctx, cudaMemcpyAsync(LX, lx, b, cudaMemcpyHostToDevice, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(LY, ly, b, cudaMemcpyHostToDevice, ctx->stream));
@@ -227,55 +235,56 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
         GX_CUDA(ctx, cudaMemsetAsync(LM, 0, b, ctx->stream));
     }
     const unsigned g = gx_blocks(n, 256);
-    int64_t nseg = (T + K - 1) / K;
-    for (int64_t sgi = nseg - 1; sgi >= 0; sgi--) {
-        int64_t s0 = sgi * K, s1 = std::min(T, s0 + K);
-        // restore the checkpoint of step s0 and recompute the states s0 .. s1
-        DevBuf *dst[4] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy};
-        for (int k = 0; k < 4; k++)
-            GX_CUDA(ctx, cudaMemcpyAsync(dst[k]->p, ck + ((size_t)sgi * 4 + k) * (size_t)n, b, cudaMemcpyDeviceToDevice,
-                                         ctx->stream));
-        GX_TRY(forward_with_locals(ctx, seg_l(0)));  // a_{s0} and its locals
-        GX_CUDA(ctx, cudaMemcpyAsync(seg_x(0), ctx->x.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
-        GX_CUDA(ctx, cudaMemcpyAsync(seg_y(0), ctx->y.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
-        for (int64_t s = s0; s < s1; s++) {
-            k_kick_drift_a<<<g, 256, 0, ctx->stream>>>(n, h, dt, dptr<double>(ctx->x), dptr<double>(ctx->y),
-                                                       dptr<double>(ctx->vx), dptr<double>(ctx->vy),
-                                                       dptr<double>(ctx->ax), dptr<double>(ctx->ay));
-            int64_t j = s + 1 - s0;
-            GX_TRY(forward_with_locals(ctx, seg_l(j)));
-            k_kick_a<<<g, 256, 0, ctx->stream>>>(n, h, dptr<double>(ctx->vx), dptr<double>(ctx->vy),
-                                                 dptr<double>(ctx->ax), dptr<double>(ctx->ay));
-            ctx->launches += 2;
-            GX_CUDA(ctx, cudaMemcpyAsync(seg_x(j), ctx->x.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
-            GX_CUDA(ctx, cudaMemcpyAsync(seg_y(j), ctx->y.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
+    DevBuf *st[6] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->ax, &ctx->ay};
+    for (int64_t sgi = nseg - 1; sgi >= 0 && n > 0; sgi--) {
+        const int64_t s0 = sgi * K, s1 = std::min(T, s0 + K);
+        // recompute the interior states s0+1 .. s1-1 from the checkpoint of s0
+        if (s1 - s0 > 1) {
+            for (int k = 0; k < 6; k++)
+                GX_CUDA(ctx, cudaMemcpyAsync(st[k]->p, S.arr(sgi, k), b, cudaMemcpyDeviceToDevice, ctx->stream));
+            for (int64_t s = s0; s < s1 - 1; s++) {
+                k_kick_drift_a<<<g, 256, 0, ctx->stream>>>(n, h, dt, dptr<double>(ctx->x), dptr<double>(ctx->y),
+                                                           dptr<double>(ctx->vx), dptr<double>(ctx->vy),
+                                                           dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+                GX_TRY(gx_forces_device(ctx, false));
+                k_kick_a<<<g, 256, 0, ctx->stream>>>(n, h, dptr<double>(ctx->vx), dptr<double>(ctx->vy),
+                                                     dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+                ctx->launches += 2;
+                int64_t j = s - s0;  // state s+1 -> seg slot s - s0
+                GX_CUDA(ctx, cudaMemcpyAsync(seg_x(j), ctx->x.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
+                GX_CUDA(ctx, cudaMemcpyAsync(seg_x(j) + n, ctx->y.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
+                GX_CUDA(ctx, cudaMemcpyAsync(seg_l(j), current_lf(ctx), lfb, cudaMemcpyDeviceToDevice, ctx->stream));
+            }
         }
-        // reverse through the segment
+        // reverse through the segment: state s+1 for s = s1-1 .. s0
         for (int64_t s = s1 - 1; s >= s0; s--) {
-            int64_t j = s + 1 - s0;
-            double c = (s + 1 == T) ? h : dt;
-            k_scale<<<g, 256, 0, ctx->stream>>>(n, c, LVX, LAX);
-            k_scale<<<g, 256, 0, ctx->stream>>>(n, c, LVY, LAY);
-            GX_TRY(vjp_at(ctx, seg_x(j), seg_y(j), seg_l(j), LAX, LAY, GX, GY, GM));
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GX, LX);
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GY, LY);
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GM, LM);
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, dt, LX, LVX);
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, dt, LY, LVY);
-            ctx->launches += 7;
-        }
-        if (sgi == 0) {  // a_0 feeds the first half kick only
-            k_scale<<<g, 256, 0, ctx->stream>>>(n, h, LVX, LAX);
-            k_scale<<<g, 256, 0, ctx->stream>>>(n, h, LVY, LAY);
-            GX_TRY(vjp_at(ctx, seg_x(0), seg_y(0), seg_l(0), LAX, LAY, GX, GY, GM));
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GX, LX);
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GY, LY);
-            k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GM, LM);
-            ctx->launches += 5;
+            const double *px, *py;
+            const void *pl;
+            if (s + 1 == s1) {
+                px = S.arr(sgi + 1, 0);
+                py = S.arr(sgi + 1, 1);
+                pl = S.lf(sgi + 1);
+            } else {
+                px = seg_x(s - s0);
+                py = seg_x(s - s0) + n;
+                pl = seg_l(s - s0);
+            }
+            const double c = (s + 1 == T) ? h : dt;  // a_{s+1} feeds one half kick at T, two elsewhere
+            k_scale2<<<g, 256, 0, ctx->stream>>>(n, c, LVX, LVY, LAX, LAY);
+            GX_TRY(force_vjp(ctx, px, py, pl, LAX, LAY, GX, GY, GM));
+            k_adj_step<<<g, 256, 0, ctx->stream>>>(n, dt, GX, GY, GM, LX, LY, LM, LVX, LVY);
+            ctx->launches += 2;
         }
         GX_CUDA(ctx, cudaGetLastError());
     }
     if (n > 0) {
+        // a_0 feeds the first half kick only
+        k_scale2<<<g, 256, 0, ctx->stream>>>(n, h, LVX, LVY, LAX, LAY);
+        GX_TRY(force_vjp(ctx, S.arr(0, 0), S.arr(0, 1), S.lf(0), LAX, LAY, GX, GY, GM));
+        k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GX, LX);
+        k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GY, LY);
+        k_axpy<<<g, 256, 0, ctx->stream>>>(n, 1.0, GM, LM);
+        ctx->launches += 4;
         GX_CUDA(ctx, cudaMemcpyAsync(gx0, LX, b, cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(gy0, LY, b, cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(gvx0, LVX, b, cudaMemcpyDeviceToHost, ctx->stream));
@@ -283,6 +292,12 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
         GX_CUDA(ctx, cudaMemcpyAsync(gm, LM, b, cudaMemcpyDeviceToHost, ctx->stream));
     }
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (peak_bytes) {
+        size_t tot = ctx->ckpt.bytes + ctx->seg.bytes + ctx->adj_dL.bytes + ctx->adj_dM.bytes + ctx->adj_dMleaf.bytes +
+                     ctx->adj_lam32.bytes;
+        for (DevBuf *d : bufs) tot += d->bytes;
+        *peak_bytes = (int64_t)tot;
+    }
     return GX_OK;
 }
 

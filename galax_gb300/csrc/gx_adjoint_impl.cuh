@@ -13,7 +13,10 @@
 //   M2L^T as a gather over the (symmetric) far lists, M2M^T straight from every
 //   ancestor to the leaf, P2M^T, and the Hessian-vector product of P2P over the
 //   (symmetric) near lists.  Every operator is the exact transpose of the forward
-//   one, so the result agrees with finite differences of the forward evaluation.
+//   one, so in FP64 the result agrees with finite differences of the forward
+//   evaluation.  T = float is the mixed form: the same operators in FP32 on the
+//   forward's FP32 leaf locals, FP32 body offsets from the leaf COM and per-leaf-pair
+//   FP32 shifts (as the mixed forward), with the outputs accumulated in FP64.
 #pragma once
 #include "gx_fmm_impl.cuh"
 
@@ -25,96 +28,103 @@ __device__ __forceinline__ void pow_fact(T u, T *pf) {
     const int PP = gx_rt_order(P);
     pf[0] = T(1);
 #pragma unroll
-    for (int k = 1; k <= PP; k++) pf[k] = pf[k - 1] * u * (T)(1.0 / k);
+    for (int k = 1; k <= PP; k++) pf[k] = pf[k - 1] * u * tab_inv<T>(k);
 }
 
 // ---- A1: L2P^T and the Hessian term.  Warp per leaf, lane per body.
 //   g_x,j   = -H_Phi(u_j) lam_j
 //   dLf[T]  = -sum_j (lam_x T1 u^(T-e1) + lam_y T2 u^(T-e2))
-template <int P>
+// The FP32 form also packs the bodies (u, v, m) and cotangents for its P2P pass.
+template <int P, class T>
 __global__ void __launch_bounds__(128) k_adj_l2p(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
-                                                 const double *__restrict__ comx, const double *__restrict__ comy,
-                                                 const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
-                                                 const double *__restrict__ Lf, const double *__restrict__ lx,
-                                                 const double *__restrict__ ly, double *__restrict__ gx,
-                                                 double *__restrict__ gy, double *__restrict__ dL) {
+                                                 const double *__restrict__ m, const double *__restrict__ comx,
+                                                 const double *__restrict__ comy, const int32_t *__restrict__ bs,
+                                                 const int32_t *__restrict__ be, const T *__restrict__ Lf,
+                                                 const double *__restrict__ lx, const double *__restrict__ ly,
+                                                 double *__restrict__ gx, double *__restrict__ gy, T *__restrict__ dL,
+                                                 float4 *__restrict__ pos32, float2 *__restrict__ lam32) {
     constexpr int NC = nc2(P);
-    constexpr int NS = row_stride<double>(NC);
+    constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
     const int NCr = (PP + 1) * (PP + 2) / 2;
     int lane = threadIdx.x & 31;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nl) return;
-    double lf[NC];
+    T lf[NC];
     load_row<NC>(Lf + leaf * NS, lf);
-    double acc[NC];
+    T acc[NC];
 #pragma unroll
-    for (int k = 0; k < NCr; k++) acc[k] = 0.0;
+    for (int k = 0; k < NCr; k++) acc[k] = T(0);
+    const double cxl = comx[leaf], cyl = comy[leaf];
     for (int32_t i = bs[leaf] + lane; i < be[leaf]; i += 32) {
-        double u = x[i] - comx[leaf], v = y[i] - comy[leaf];
-        double pu[P + 1], pv[P + 1];
-        pu[0] = 1.0;
-        pv[0] = 1.0;
+        T u = (T)(x[i] - cxl), v = (T)(y[i] - cyl);
+        T pu[P + 1], pv[P + 1];
+        pu[0] = T(1);
+        pv[0] = T(1);
 #pragma unroll
         for (int q = 1; q <= PP; q++) {
             pu[q] = pu[q - 1] * u;
             pv[q] = pv[q - 1] * v;
         }
-        double lam_x = lx[i], lam_y = ly[i];
-        double hxx = 0.0, hxy = 0.0, hyy = 0.0;
+        T lam_x = (T)lx[i], lam_y = (T)ly[i];
+        if constexpr (sizeof(T) == 4) {
+            pos32[i] = make_float4(u, v, (float)m[i], 0.f);
+            lam32[i] = make_float2(lam_x, lam_y);
+        }
+        T hxx = T(0), hxy = T(0), hyy = T(0);
 #pragma unroll
         for (int a = 0; a <= PP; a++)
 #pragma unroll
             for (int b = 0; b <= PP - a; b++) {
-                double c = lf[gx_mi(a, b)];
-                if (a >= 2) hxx += c * (double)(a * (a - 1)) * pu[a - 2] * pv[b];
-                if (b >= 2) hyy += c * (double)(b * (b - 1)) * pu[a] * pv[b - 2];
-                if (a >= 1 && b >= 1) hxy += c * (double)(a * b) * pu[a - 1] * pv[b - 1];
-                double t = 0.0;
-                if (a >= 1) t += lam_x * (double)a * pu[a - 1] * pv[b];
-                if (b >= 1) t += lam_y * (double)b * pu[a] * pv[b - 1];
+                T c = lf[gx_mi(a, b)];
+                if (a >= 2) hxx += c * (T)(a * (a - 1)) * pu[a - 2] * pv[b];
+                if (b >= 2) hyy += c * (T)(b * (b - 1)) * pu[a] * pv[b - 2];
+                if (a >= 1 && b >= 1) hxy += c * (T)(a * b) * pu[a - 1] * pv[b - 1];
+                T t = T(0);
+                if (a >= 1) t += lam_x * (T)a * pu[a - 1] * pv[b];
+                if (b >= 1) t += lam_y * (T)b * pu[a] * pv[b - 1];
                 acc[gx_mi(a, b)] -= t;
             }
-        gx[i] = -(hxx * lam_x + hxy * lam_y);
-        gy[i] = -(hxy * lam_x + hyy * lam_y);
+        gx[i] = -(double)(hxx * lam_x + hxy * lam_y);
+        gy[i] = -(double)(hxy * lam_x + hyy * lam_y);
     }
 #pragma unroll
     for (int k = 0; k < NCr; k++) {
-        double s = warp_sum_t<double>(acc[k]);
+        T s = warp_sum_t<T>(acc[k]);
         if (lane == (k & 31)) dL[leaf * NS + k] = s;
     }
 }
 
 // ---- A2: L2L^T, one level of the upward pass: dL[P][U] = sum_c sum_{T<=U} dL[c][T] C(U,T) e^(U-T),
 // e = com_c - com_P.  The leaves' rows are already in place; internal rows are written here.
-template <int P>
+template <int P, class T>
 __global__ void __launch_bounds__(128) k_adj_l2l_up(int64_t s, int64_t e, const int4 *__restrict__ child,
                                                     const double *__restrict__ comx, const double *__restrict__ comy,
-                                                    double *__restrict__ dL) {
+                                                    T *__restrict__ dL) {
     constexpr int NC = nc2(P);
-    constexpr int NS = row_stride<double>(NC);
+    constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
     const int NCr = (PP + 1) * (PP + 2) / 2;
     int64_t node = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= e) return;
     int4 c4 = child[node];
     int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-    double out[NC];
+    T out[NC];
 #pragma unroll
-    for (int k = 0; k < NCr; k++) out[k] = 0.0;
+    for (int k = 0; k < NCr; k++) out[k] = T(0);
     for (int q = 0; q < 4; q++) {
         int c = cc[q];
         if (c < 0) continue;
-        double ex = comx[c] - comx[node], ey = comy[c] - comy[node];
-        double px[P + 1], py[P + 1];
-        px[0] = 1.0;
-        py[0] = 1.0;
+        T ex = (T)(comx[c] - comx[node]), ey = (T)(comy[c] - comy[node]);
+        T px[P + 1], py[P + 1];
+        px[0] = T(1);
+        py[0] = T(1);
 #pragma unroll
         for (int k = 1; k <= PP; k++) {
             px[k] = px[k - 1] * ex;
             py[k] = py[k - 1] * ey;
         }
-        double dc[NC];
+        T dc[NC];
         load_row<NC>(dL + (int64_t)c * NS, dc);
 #pragma unroll
         for (int ui = 0; ui <= PP; ui++)
@@ -124,8 +134,8 @@ __global__ void __launch_bounds__(128) k_adj_l2l_up(int64_t s, int64_t e, const 
                 for (int ti = 0; ti <= ui; ti++)
 #pragma unroll
                     for (int tj = 0; tj <= uj; tj++)
-                        out[gx_mi(ui, uj)] += dc[gx_mi(ti, tj)] * (cbinom(ui, ti) * cbinom(uj, tj)) * px[ui - ti] *
-                                              py[uj - tj];
+                        out[gx_mi(ui, uj)] += dc[gx_mi(ti, tj)] * (tab_binom<T>(ui, ti) * tab_binom<T>(uj, tj)) *
+                                              px[ui - ti] * py[uj - tj];
     }
 #pragma unroll
     for (int k = 0; k < NCr; k++) dL[node * NS + k] = out[k];
@@ -133,13 +143,15 @@ __global__ void __launch_bounds__(128) k_adj_l2l_up(int64_t s, int64_t e, const 
 
 // ---- A3: M2L^T as a gather over far(s) (far lists are symmetric):
 //   dM[s][S] = -(-1)^|S| sum_{t in far(s)} sum_T A(com_t - com_s)[S+T] dL[t][T] / T!
-template <int P>
-__global__ void __launch_bounds__(128) k_adj_m2l(int64_t nn, const int32_t *__restrict__ idx,
-                                                 const int64_t *__restrict__ start, const int32_t *__restrict__ cnt,
-                                                 const double *__restrict__ comx, const double *__restrict__ comy,
-                                                 double eps2, const double *__restrict__ dL, double *__restrict__ dM) {
+// The FP32 form forms com_t - com_s from the FP32 (hi, lo) COMs exactly as the
+// forward M2L forms it for the pair (t, s).
+template <int P, class T>
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1)
+    k_adj_m2l(int64_t nn, const int32_t *__restrict__ idx, const int64_t *__restrict__ start,
+              const int32_t *__restrict__ cnt, const double *__restrict__ comx, const double *__restrict__ comy,
+              const float4 *__restrict__ comhl, double eps2d, const T *__restrict__ dL, T *__restrict__ dM) {
     constexpr int NC = nc2(P);
-    constexpr int NS = row_stride<double>(NC);
+    constexpr int NS = row_stride<T>(NC);
     constexpr int ND = nc2(2 * P);
     const int PP = gx_rt_order(P);
     const int NCr = (PP + 1) * (PP + 2) / 2;
@@ -149,32 +161,46 @@ __global__ void __launch_bounds__(128) k_adj_m2l(int64_t nn, const int32_t *__re
     int64_t st = start[node];
     int len = cnt[node];
     double scx = comx[node], scy = comy[node];
-    double acc[NC];
+    float4 shl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (sizeof(T) == 4) shl = comhl[node];
+    const T eps2 = (T)eps2d;
+    T acc[NC];
 #pragma unroll
-    for (int k = 0; k < NCr; k++) acc[k] = 0.0;
+    for (int k = 0; k < NCr; k++) acc[k] = T(0);
+    int64_t t = lane < len ? (int64_t)idx[st + lane] : 0;
     for (int q = lane; q < len; q += 32) {
-        int64_t t = idx[st + q];
-        double A[ND];
-        derivs_scaled<P, double>(comx[t] - scx, comy[t] - scy, eps2, A);
-        double lt[NC];
+        int64_t nt = q + 32 < len ? (int64_t)idx[st + q + 32] : 0;
+        T lt[NC];
         load_row<NC>(dL + t * NS, lt);
+        T dx, dy;
+        if constexpr (sizeof(T) == 4) {
+            float4 thl = comhl[t];
+            dx = (thl.x - shl.x) + (thl.y - shl.y);
+            dy = (thl.z - shl.z) + (thl.w - shl.w);
+        } else {
+            dx = comx[t] - scx;
+            dy = comy[t] - scy;
+        }
+        T A[ND];
+        derivs_scaled<P, T>(dx, dy, eps2, A);
 #pragma unroll
         for (int ti = 0; ti <= PP; ti++)
 #pragma unroll
             for (int tj = 0; tj <= PP - ti; tj++) {
-                double w = lt[gx_mi(ti, tj)] * (cinvfact(ti) * cinvfact(tj));
+                T w = lt[gx_mi(ti, tj)] * tab_ifp<T>(ti, tj);
 #pragma unroll
                 for (int si = 0; si <= PP; si++)
 #pragma unroll
                     for (int sj = 0; sj <= PP - si; sj++) acc[gx_mi(si, sj)] += w * A[gx_mi(si + ti, sj + tj)];
             }
+        t = nt;
     }
 #pragma unroll
     for (int si = 0; si <= PP; si++)
 #pragma unroll
         for (int sj = 0; sj <= PP - si; sj++) {
             int k = gx_mi(si, sj);
-            double v = warp_sum_t<double>(acc[k]);
+            T v = warp_sum_t<T>(acc[k]);
             if (lane == (k & 31)) dM[node * NS + k] = ((si + sj) & 1) ? v : -v;
         }
 }
@@ -183,29 +209,29 @@ __global__ void __launch_bounds__(128) k_adj_m2l(int64_t nn, const int32_t *__re
 // moments shifted by d = com_leaf - com_a (SM(leaf->a), composed exactly along the
 // chain), so dM_leaf[S] = sum_a sum_{T>=S} dM_a[T] d^(T-S)/(T-S)!.  Warp per leaf,
 // lane per ancestor, warp reduction.
-template <int P>
+template <int P, class T>
 __global__ void __launch_bounds__(128) k_adj_m2m_direct(int64_t nl, int n_levels, const int32_t *__restrict__ anc,
                                                         const uint8_t *__restrict__ has_far,
                                                         const double *__restrict__ comx, const double *__restrict__ comy,
-                                                        const double *__restrict__ dM, double *__restrict__ dMleaf) {
+                                                        const T *__restrict__ dM, T *__restrict__ dMleaf) {
     constexpr int NC = nc2(P);
-    constexpr int NS = row_stride<double>(NC);
+    constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
     const int NCr = (PP + 1) * (PP + 2) / 2;
     int lane = threadIdx.x & 31;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nl) return;
-    double out[NC];
+    T out[NC];
 #pragma unroll
-    for (int k = 0; k < NCr; k++) out[k] = 0.0;
+    for (int k = 0; k < NCr; k++) out[k] = T(0);
     for (int j = lane; j < n_levels; j += 32) {
         int32_t a = anc[(int64_t)j * nl + leaf];
         if (a < 0 || !has_far[a]) continue;
-        double da[NC];
+        T da[NC];
         load_row<NC>(dM + (int64_t)a * NS, da);
-        double px[P + 1], py[P + 1];
-        pow_fact<P, double>(comx[leaf] - comx[a], px);
-        pow_fact<P, double>(comy[leaf] - comy[a], py);
+        T px[P + 1], py[P + 1];
+        pow_fact<P, T>((T)(comx[leaf] - comx[a]), px);
+        pow_fact<P, T>((T)(comy[leaf] - comy[a]), py);
 #pragma unroll
         for (int si = 0; si <= PP; si++)
 #pragma unroll
@@ -218,45 +244,47 @@ __global__ void __launch_bounds__(128) k_adj_m2m_direct(int64_t nl, int n_levels
     }
 #pragma unroll
     for (int k = 0; k < NCr; k++) {
-        double v = warp_sum_t<double>(out[k]);
+        T v = warp_sum_t<T>(out[k]);
         if (lane == (k & 31)) dMleaf[leaf * NS + k] = v;
     }
 }
 
 // ---- A5: P2M^T: g_m,j += sum_S dM[S] u^S/S!,  g_x,j += m_j sum_S dM[S] grad(u^S/S!).
-// Thread per body (the leaf id comes from the body -> leaf map).
-template <int P>
+// Warp per leaf, lane per body.
+template <int P, class T>
 __global__ void __launch_bounds__(128) k_adj_p2m(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
                                                  const double *__restrict__ m, const double *__restrict__ comx,
                                                  const double *__restrict__ comy, const int32_t *__restrict__ bs,
-                                                 const int32_t *__restrict__ be, const double *__restrict__ dMleaf,
+                                                 const int32_t *__restrict__ be, const T *__restrict__ dMleaf,
                                                  double *__restrict__ gx, double *__restrict__ gy,
                                                  double *__restrict__ gm) {
     constexpr int NC = nc2(P);
-    constexpr int NS = row_stride<double>(NC);
+    constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
     int lane = threadIdx.x & 31;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nl) return;
-    double dm[NC];
+    T dm[NC];
     load_row<NC>(dMleaf + leaf * NS, dm);
+    const double cxl = comx[leaf], cyl = comy[leaf];
     for (int32_t i = bs[leaf] + lane; i < be[leaf]; i += 32) {
-        double px[P + 1], py[P + 1];
-        pow_fact<P, double>(x[i] - comx[leaf], px);
-        pow_fact<P, double>(y[i] - comy[leaf], py);
-        double sm = 0.0, sx = 0.0, sy = 0.0;
+        T px[P + 1], py[P + 1];
+        pow_fact<P, T>((T)(x[i] - cxl), px);
+        pow_fact<P, T>((T)(y[i] - cyl), py);
+        T sm = T(0), sx = T(0), sy = T(0);
 #pragma unroll
         for (int a = 0; a <= PP; a++)
 #pragma unroll
             for (int b = 0; b <= PP - a; b++) {
-                double c = dm[gx_mi(a, b)];
+                T c = dm[gx_mi(a, b)];
                 sm += c * px[a] * py[b];
                 if (a >= 1) sx += c * px[a - 1] * py[b];
                 if (b >= 1) sy += c * px[a] * py[b - 1];
             }
-        gm[i] += sm;
-        gx[i] += m[i] * sx;
-        gy[i] += m[i] * sy;
+        T mi = (T)m[i];
+        gm[i] += (double)sm;
+        gx[i] += (double)(mi * sx);
+        gy[i] += (double)(mi * sy);
     }
 }
 
@@ -323,11 +351,89 @@ __global__ void __launch_bounds__(128) k_adj_p2p_items(int64_t n_items, const in
     }
 }
 
+// FP32 form of A6 on the packed bodies (u, v, m) and cotangents of k_adj_l2p<float>;
+// a source leaf is moved into the target leaf's frame by one FP32 shift per leaf
+// pair formed in FP64 (as in the mixed forward P2P).
+__global__ void __launch_bounds__(128, 6) k_adj_p2p32_items(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                         const int64_t *__restrict__ item_qb,
+                                                         const int32_t *__restrict__ item_nq,
+                                                         const float4 *__restrict__ pos, const float2 *__restrict__ lam,
+                                                         const double *__restrict__ comx, const double *__restrict__ comy,
+                                                         const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                                         const int32_t *__restrict__ src_idx, float eps2, int tchunks,
+                                                         float4 *__restrict__ part) {
+    __shared__ __align__(16) float sx[4][32], sy[4][32], sm[4][32], slx[4][32], sly[4][32];
+    int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (it >= n_items) return;
+    int32_t leaf = item_leaf[it];
+    int64_t qb = item_qb[it];
+    int nq = item_nq[it];
+    int32_t t0 = bs[leaf], t1 = be[leaf];
+    double tcx = comx[leaf], tcy = comy[leaf];
+    int sl = lane < nq ? src_idx[qb + lane] : -1;
+    int sbeg = 0, send = 0;
+    float shx = 0.f, shy = 0.f;
+    if (sl >= 0) {
+        sbeg = bs[sl];
+        send = be[sl];
+        shx = (float)(comx[sl] - tcx);
+        shy = (float)(comy[sl] - tcy);
+    }
+    for (int tc = 0; tc < tchunks; tc++) {
+        int32_t i = t0 + tc * 32 + lane;
+        bool valid = i < t1;
+        float4 me = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 li = valid ? lam[i] : make_float2(0.f, 0.f);
+        const float xi = me.x, yi = me.y, mi = me.z, lxi = li.x, lyi = li.y;
+        float gxa = 0.f, gya = 0.f, gma = 0.f;
+        if (t0 + tc * 32 < t1) {
+            for (int k = 0; k < nq; k++) {
+                int s0 = __shfl_sync(0xffffffffu, sbeg, k), s1 = __shfl_sync(0xffffffffu, send, k);
+                float gxs = __shfl_sync(0xffffffffu, shx, k), gys = __shfl_sync(0xffffffffu, shy, k);
+                for (int sc = s0; sc < s1; sc += 32) {
+                    int j = sc + lane;
+                    __syncwarp();
+                    if (j < s1) {
+                        float4 b = pos[j];
+                        float2 l = lam[j];
+                        sx[w][lane] = b.x + gxs;
+                        sy[w][lane] = b.y + gys;
+                        sm[w][lane] = b.z;
+                        slx[w][lane] = l.x;
+                        sly[w][lane] = l.y;
+                    }
+                    __syncwarp();
+                    int ns = min(32, s1 - sc);
+                    for (int kk = 0; kk < ns; kk++) {
+                        float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
+                        float mj = sm[w][kk], lxj = slx[w][kk], lyj = sly[w][kk];
+                        float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                        float ir2 = ir * ir;
+                        float ir3 = ir2 * ir;
+                        float ir5 = ir3 * ir2;
+                        float wx = fmaf(mi, lxj, -mj * lxi), wy = fmaf(mi, lyj, -mj * lyi);
+                        float c = 3.f * ir5 * fmaf(dx, wx, dy * wy);
+                        float dl = fmaf(lxj, dx, lyj * dy);
+                        bool self = sc + kk == i;
+                        ir3 = self ? 0.f : ir3;
+                        c = self ? 0.f : c;
+                        gxa = fmaf(ir3, wx, fmaf(-c, dx, gxa));
+                        gya = fmaf(ir3, wy, fmaf(-c, dy, gya));
+                        gma = fmaf(-dl, ir3, gma);
+                    }
+                }
+            }
+        }
+        part[(it * tchunks + tc) * 32 + lane] = make_float4(gxa, gya, gma, 0.f);
+    }
+}
+
+template <class V, class S>
 __global__ void __launch_bounds__(128) k_adj_p2p_reduce(int64_t nl, const int32_t *__restrict__ bs,
                                                         const int32_t *__restrict__ be, const int64_t *__restrict__ item_off,
-                                                        int tchunks, const double4 *__restrict__ part,
-                                                        double *__restrict__ gx, double *__restrict__ gy,
-                                                        double *__restrict__ gm) {
+                                                        int tchunks, const V *__restrict__ part, double *__restrict__ gx,
+                                                        double *__restrict__ gy, double *__restrict__ gm) {
     int lane = threadIdx.x & 31;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nl) return;
@@ -335,66 +441,90 @@ __global__ void __launch_bounds__(128) k_adj_p2p_reduce(int64_t nl, const int32_
     for (int tc = 0; tc < tchunks && t0 + tc * 32 < t1; tc++) {
         int32_t i = t0 + tc * 32 + lane;
         if (i >= t1) continue;
-        double sx = 0.0, sy = 0.0, smm = 0.0;
+        S sx = 0, sy = 0, smm = 0;
         for (int64_t it = item_off[leaf]; it < item_off[leaf + 1]; it++) {
-            double4 v = part[(it * tchunks + tc) * 32 + lane];
+            V v = part[(it * tchunks + tc) * 32 + lane];
             sx += v.x;
             sy += v.y;
             smm += v.z;
         }
-        gx[i] += sx;
-        gy[i] += sy;
-        gm[i] += smm;
+        gx[i] += (double)sx;
+        gy[i] += (double)sy;
+        gm[i] += (double)smm;
     }
 }
 
-// Full VJP on the resident bodies.  Needs the forward local expansions of the same
-// positions (ctx->Lf after a forward evaluation in ACCURATE FP64).
-template <int P>
-int run_force_vjp(gx_ctx *ctx, const double *lx, const double *ly, double *gx, double *gy, double *gm) {
+// Full VJP at positions (X, Y) with the forward's leaf locals lf (rows of T) of those
+// positions; masses and the frozen tree/plan come from the context.
+template <int P, class T>
+int run_force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf_rows, const double *lx,
+                  const double *ly, double *gx, double *gy, double *gm) {
     constexpr int NC = nc2(P);
-    constexpr int NS = row_stride<double>(NC);
-    const int64_t nn = ctx->n_nodes, nl = ctx->n_leaves;
+    constexpr int NS = row_stride<T>(NC);
+    const int64_t nn = ctx->n_nodes, nl = ctx->n_leaves, n = ctx->n_bodies;
     cudaStream_t st = ctx->stream;
-    if (nn == 0) return GX_OK;
-    const double *X = dptr<double>(ctx->x), *Y = dptr<double>(ctx->y), *Mb = dptr<double>(ctx->m);
+    if (nn == 0 || n == 0) return GX_OK;
+    const double *Mb = dptr<double>(ctx->m);
     const double *comx = dptr<double>(ctx->comx), *comy = dptr<double>(ctx->comy);
     const int32_t *bs = dptr<int32_t>(ctx->bs), *be = dptr<int32_t>(ctx->be);
     const int4 *child = dptr<int4>(ctx->child);
     const double eps2 = ctx->eps * ctx->eps;
     const unsigned gw = (unsigned)((nl * 32 + 127) / 128);
-    GX_TRY(gx_ensure(ctx, ctx->adj_dL, sizeof(double) * NS * (size_t)nn));
-    GX_TRY(gx_ensure(ctx, ctx->adj_dM, sizeof(double) * NS * (size_t)nn));
-    GX_TRY(gx_ensure(ctx, ctx->adj_dMleaf, sizeof(double) * NS * (size_t)nl));
-    double *dL = dptr<double>(ctx->adj_dL), *dM = dptr<double>(ctx->adj_dM), *dMl = dptr<double>(ctx->adj_dMleaf);
-    // A1: L2P^T and the Hessian term (writes gx, gy)
-    k_adj_l2p<P><<<gw, 128, 0, st>>>(nl, X, Y, comx, comy, bs, be, dptr<double>(ctx->Lf), lx, ly, gx, gy, dL);
+    const T *Lf = reinterpret_cast<const T *>(lf_rows);
+    GX_TRY(gx_ensure(ctx, ctx->adj_dL, sizeof(T) * NS * (size_t)nn));
+    GX_TRY(gx_ensure(ctx, ctx->adj_dM, sizeof(T) * NS * (size_t)nn));
+    GX_TRY(gx_ensure(ctx, ctx->adj_dMleaf, sizeof(T) * NS * (size_t)nl));
+    T *dL = dptr<T>(ctx->adj_dL), *dM = dptr<T>(ctx->adj_dM), *dMl = dptr<T>(ctx->adj_dMleaf);
+    constexpr bool F32 = sizeof(T) == 4;
+    float4 *pos32 = nullptr;
+    float2 *lam32 = nullptr;
+    if (F32) {
+        GX_TRY(gx_ensure(ctx, ctx->pos32, sizeof(float4) * (size_t)n));
+        GX_TRY(gx_ensure(ctx, ctx->adj_lam32, sizeof(float2) * (size_t)n));
+        pos32 = dptr<float4>(ctx->pos32);
+        lam32 = dptr<float2>(ctx->adj_lam32);
+    }
+    // A1: L2P^T and the Hessian term (writes gx, gy; the FP32 form also packs bodies)
+    k_adj_l2p<P, T><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, Lf, lx, ly, gx, gy, dL, pos32, lam32);
     // A2: L2L^T upward, level by level (leaves are level 0)
     for (int lv = 1; lv < ctx->n_levels; lv++) {
         int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
-        k_adj_l2l_up<P><<<gx_blocks(e - s, 128), 128, 0, st>>>(s, e, child, comx, comy, dL);
+        k_adj_l2l_up<P, T><<<gx_blocks(e - s, 128), 128, 0, st>>>(s, e, child, comx, comy, dL);
     }
     // A3: M2L^T
     const int64_t *fs = dptr<int64_t>(ctx->far_off);
-    k_adj_m2l<P><<<(unsigned)((nn * 32 + 127) / 128), 128, 0, st>>>(nn, dptr<int32_t>(ctx->far_idx), fs,
-                                                                    reinterpret_cast<const int32_t *>(fs + nn), comx,
-                                                                    comy, eps2, dL, dM);
+    k_adj_m2l<P, T><<<(unsigned)((nn * 32 + 127) / 128), 128, 0, st>>>(
+        nn, dptr<int32_t>(ctx->far_idx), fs, reinterpret_cast<const int32_t *>(fs + nn), comx, comy,
+        F32 ? dptr<float4>(ctx->comhl) : nullptr, eps2, dL, dM);
     // A4: M2M^T to the leaves
-    k_adj_m2m_direct<P><<<gw, 128, 0, st>>>(nl, ctx->n_levels, dptr<int32_t>(ctx->anc), dptr<uint8_t>(ctx->has_far_acc),
-                                            comx, comy, dM, dMl);
+    k_adj_m2m_direct<P, T><<<gw, 128, 0, st>>>(nl, ctx->n_levels, dptr<int32_t>(ctx->anc),
+                                               dptr<uint8_t>(ctx->has_far_acc), comx, comy, dM, dMl);
     // A5: P2M^T (adds to gx, gy; writes gm)
-    GX_CUDA(ctx, cudaMemsetAsync(gm, 0, sizeof(double) * (size_t)ctx->n_bodies, st));
-    k_adj_p2m<P><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, dMl, gx, gy, gm);
+    GX_CUDA(ctx, cudaMemsetAsync(gm, 0, sizeof(double) * (size_t)n, st));
+    k_adj_p2m<P, T><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, dMl, gx, gy, gm);
     // A6: Hessian-vector P2P
     const gx_ctx::Items &I = ctx->items_acc;
     const int tchunks = (int)std::max<int64_t>(1, (ctx->max_leaf + 31) / 32);
-    GX_TRY(gx_ensure(ctx, ctx->part, sizeof(double4) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
-    double4 *part = dptr<double4>(ctx->part);
-    if (I.n > 0)
-        k_adj_p2p_items<<<(unsigned)((I.n * 32 + 127) / 128), 128, 0, st>>>(
-            I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), X, Y, Mb, lx, ly, bs, be,
-            dptr<int32_t>(ctx->near_idx), eps2, tchunks, part);
-    k_adj_p2p_reduce<<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks, part, gx, gy, gm);
+    const unsigned gi = (unsigned)((I.n * 32 + 127) / 128);
+    if (F32) {
+        GX_TRY(gx_ensure(ctx, ctx->part, sizeof(float4) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
+        float4 *part = dptr<float4>(ctx->part);
+        if (I.n > 0)
+            k_adj_p2p32_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
+                                                  pos32, lam32, comx, comy, bs, be, dptr<int32_t>(ctx->near_idx),
+                                                  (float)eps2, tchunks, part);
+        k_adj_p2p_reduce<float4, float><<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks, part, gx, gy,
+                                                            gm);
+    } else {
+        GX_TRY(gx_ensure(ctx, ctx->part, sizeof(double4) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
+        double4 *part = dptr<double4>(ctx->part);
+        if (I.n > 0)
+            k_adj_p2p_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), X,
+                                                Y, Mb, lx, ly, bs, be, dptr<int32_t>(ctx->near_idx), eps2, tchunks,
+                                                part);
+        k_adj_p2p_reduce<double4, double><<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks, part, gx, gy,
+                                                              gm);
+    }
     ctx->launches += 6 + (ctx->n_levels - 1);
     GX_CUDA(ctx, cudaGetLastError());
     return GX_OK;
@@ -402,8 +532,9 @@ int run_force_vjp(gx_ctx *ctx, const double *lx, const double *ly, double *gx, d
 
 }  // namespace
 
-#define GX_ADJ_INSTANTIATE(PP)                                                                              \
-    int gx_run_force_vjp_##PP(gx_ctx *ctx, const double *lx, const double *ly, double *gx, double *gy, \
-                              double *gm) {                                                              \
-        return run_force_vjp<PP>(ctx, lx, ly, gx, gy, gm);                                              \
+#define GX_ADJ_INSTANTIATE(PP)                                                                             \
+    int gx_run_force_vjp_##PP(gx_ctx *ctx, int f32, const double *X, const double *Y, const void *lf,     \
+                              const double *lx, const double *ly, double *gx, double *gy, double *gm) {  \
+        return f32 ? run_force_vjp<PP, float>(ctx, X, Y, lf, lx, ly, gx, gy, gm)                         \
+                   : run_force_vjp<PP, double>(ctx, X, Y, lf, lx, ly, gx, gy, gm);                       \
     }

@@ -22,15 +22,22 @@
 
 namespace {
 
-// Factorials and binomials come from a constant-memory table, filled by static
-// initialization from a constexpr builder: a table read is one constant-bank
-// operand whether or not the loop around it is unrolled (FP64 arithmetic is slow
-// on this part, so these must never be evaluated at run time).  The builder is
-// iterative: a recursive device function has no static stack bound.
+// Factorials, binomials and reciprocals come from a constant-memory table, filled by
+// static initialization from a constexpr builder, in both FP64 and FP32 (each FP32
+// entry is the FP64 value rounded once).  A table read is one constant-bank operand
+// when the loop around it is unrolled and one constant load when it is not; no
+// FP64 arithmetic is left at run time in the FP32 kernels (FP64 throughput is a small
+// fraction of FP32 on this part).  The builder is iterative: a recursive device
+// function has no static stack bound.
 struct GxTables {
     double fact[34];
     double invfact[34];
     double binom[17][17];
+    float binom_f[17][17];
+    double ifp[17][17];  // 1/(i! j!) as the FP64 product of 1/i! and 1/j!
+    float ifp_f[17][17];
+    double inv[34];  // 1/n
+    float inv_f[34];
 };
 __host__ __device__ constexpr GxTables gx_make_tables() {
     GxTables t{};
@@ -40,6 +47,18 @@ __host__ __device__ constexpr GxTables gx_make_tables() {
     for (int n = 0; n < 17; n++) {
         t.binom[n][0] = 1.0;
         for (int k = 1; k <= n; k++) t.binom[n][k] = t.binom[n - 1][k - 1] + (k < n ? t.binom[n - 1][k] : 0.0);
+        for (int k = 0; k < 17; k++) t.binom_f[n][k] = (float)t.binom[n][k];
+    }
+    for (int i = 0; i < 17; i++)
+        for (int j = 0; j < 17; j++) {
+            t.ifp[i][j] = t.invfact[i] * t.invfact[j];
+            t.ifp_f[i][j] = (float)t.ifp[i][j];
+        }
+    t.inv[0] = 0.0;
+    t.inv_f[0] = 0.f;
+    for (int i = 1; i < 34; i++) {
+        t.inv[i] = 1.0 / (double)i;
+        t.inv_f[i] = (float)t.inv[i];
     }
     return t;
 }
@@ -47,6 +66,16 @@ __constant__ GxTables c_tab = gx_make_tables();
 __device__ __forceinline__ double cfact(int n) { return c_tab.fact[n]; }
 __device__ __forceinline__ double cinvfact(int n) { return c_tab.invfact[n]; }
 __device__ __forceinline__ double cbinom(int n, int k) { return (k < 0 || k > n) ? 0.0 : c_tab.binom[n][k]; }
+// typed reads: C(n, k), 1/(i! j!), 1/n
+template <class T> __device__ __forceinline__ T tab_binom(int n, int k);
+template <> __device__ __forceinline__ double tab_binom<double>(int n, int k) { return c_tab.binom[n][k]; }
+template <> __device__ __forceinline__ float tab_binom<float>(int n, int k) { return c_tab.binom_f[n][k]; }
+template <class T> __device__ __forceinline__ T tab_ifp(int i, int j);
+template <> __device__ __forceinline__ double tab_ifp<double>(int i, int j) { return c_tab.ifp[i][j]; }
+template <> __device__ __forceinline__ float tab_ifp<float>(int i, int j) { return c_tab.ifp_f[i][j]; }
+template <class T> __device__ __forceinline__ T tab_inv(int n);
+template <> __device__ __forceinline__ double tab_inv<double>(int n) { return c_tab.inv[n]; }
+template <> __device__ __forceinline__ float tab_inv<float>(int n) { return c_tab.inv_f[n]; }
 __host__ __device__ constexpr int nc2(int q) { return (q + 1) * (q + 2) / 2; }  // entries with k+l <= q
 
 // Loops over expansion indices are fully unrolled (coefficient arrays stay in
@@ -70,6 +99,33 @@ __device__ __forceinline__ float rsqrt_fast(float x) {
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// Packed FP32 pairs: the .f32x2 forms of add/sub/mul/fma (sm_100 family) issue one
+// instruction for two lanes of work, each half rounded exactly as the scalar
+// instruction would round it.  A pair lives in one 64-bit register (lo, hi).
+__device__ __forceinline__ uint64_t pk2(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
 }
 
 template <class T>
@@ -167,7 +223,7 @@ __global__ void __launch_bounds__(128) k_p2m(int64_t nl, const double *__restric
         for (int i = 0; i <= PP; i++)
 #pragma unroll
             for (int j = 0; j <= PP - i; j++)
-                acc[gx_mi(i, j)] += mm * px[i] * py[j] * (T)(cinvfact(i) * cinvfact(j));
+                acc[gx_mi(i, j)] += mm * px[i] * py[j] * tab_ifp<T>(i, j);
     }
 #pragma unroll
     for (int k = 0; k < NCr; k++) {
@@ -203,8 +259,8 @@ __global__ void __launch_bounds__(128) k_m2m(int64_t s, int64_t e, const int4 *_
         py[0] = T(1);
 #pragma unroll
         for (int k = 1; k <= PP; k++) {
-            px[k] = px[k - 1] * dx * (T)(1.0 / k);  // dx^k / k!
-            py[k] = py[k - 1] * dy * (T)(1.0 / k);
+            px[k] = px[k - 1] * dx * tab_inv<T>(k);  // dx^k / k!
+            py[k] = py[k - 1] * dy * tab_inv<T>(k);
         }
         T mc[NC];
         load_row<NC>(M + (int64_t)c * NS, mc);
@@ -252,7 +308,7 @@ __device__ __forceinline__ void derivs_scaled(T dx, T dy, T eps2, T *A) {
             if (l >= 1) s1 += dy * A[gx_mi(k, l - 1)] * (T)l;
             if (k >= 2) s2 += A[gx_mi(k - 2, l)] * (T)(k * (k - 1));
             if (l >= 2) s2 += A[gx_mi(k, l - 2)] * (T)(l * (l - 1));
-            A[gx_mi(k, l)] = (-(T)(2 * n - 1) * s1 - (T)(n - 1) * s2) * ir2 * (T)(1.0 / n);
+            A[gx_mi(k, l)] = (-(T)(2 * n - 1) * s1 - (T)(n - 1) * s2) * ir2 * tab_inv<T>(n);
         }
     }
 }
@@ -301,13 +357,14 @@ __global__ void __launch_bounds__(128) k_m2l_ref(int64_t nn, const uint32_t *__r
         for (int oj = 0; oj <= PP - oi; oj++) {
             int k = gx_mi(oi, oj);
             double v = warp_sum_t<double>(acc[k]);
-            if (lane == (k & 31)) L[node * NS + k] = v * (cinvfact(oi) * cinvfact(oj));
+            if (lane == (k & 31)) L[node * NS + k] = v * tab_ifp<double>(oi, oj);
         }
 }
 
 // EXACT / ACCURATE: per-pair derivatives.  Lists given as start/count per node.
 template <int P, class T, class IDX>
-__global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__restrict__ idx,
+// FP32 at p <= 4 fits 64 registers without spills: 8 blocks (32 warps) per SM
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l_exact(int64_t nn, const IDX *__restrict__ idx,
                                                    const int64_t *__restrict__ start, const int32_t *__restrict__ cnt,
                                                    const uint8_t *__restrict__ cnt8, int64_t fixed_stride,
                                                    const double *__restrict__ comx, const double *__restrict__ comy,
@@ -325,16 +382,24 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
     int64_t st = start ? start[node] : node * fixed_stride;
     int len = cnt ? cnt[node] : (int)cnt8[node];
     double tcx = comx[node], tcy = comy[node];
-    float4 thl = comhl ? comhl[node] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 thl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (sizeof(T) == 4) thl = comhl[node];
     T eps2 = (T)eps2d;
     T acc[NC];
 #pragma unroll
     for (int k = 0; k < NCr; k++) acc[k] = T(0);
+    // the next source index is fetched one iteration ahead, and the source row is
+    // requested before the derivatives are formed, so both latencies overlap compute
+    int64_t src = lane < len ? (int64_t)idx[st + lane] : 0;
     for (int s = lane; s < len; s += 32) {
-        int64_t src = (int64_t)idx[st + s];
+        int64_t nsrc = s + 32 < len ? (int64_t)idx[st + s + 32] : 0;
+        T ms[NC];
+        load_row<NC>(M + src * NS, ms);
         T dx, dy;
-        if (sizeof(T) == 4 && comhl) {
-            // COMs as FP32 (hi, lo) pairs: the offset is exact to FP32 rounding without FP64 work
+        if constexpr (sizeof(T) == 4) {
+            // COMs as FP32 (hi, lo) pairs: the offset is exact to FP32 rounding without
+            // FP64 work (a compile-time choice: a run-time branch would be if-converted
+            // and issue the FP64 path's instructions, predicated off, on every pair)
             float4 shl = comhl[src];
             dx = (T)((thl.x - shl.x) + (thl.y - shl.y));
             dy = (T)((thl.z - shl.z) + (thl.w - shl.w));
@@ -344,8 +409,6 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
         }
         T A[ND];
         derivs_scaled<P, T>(dx, dy, eps2, A);
-        T ms[NC];
-        load_row<NC>(M + src * NS, ms);
 #pragma unroll
         for (int i = 0; i <= PP; i++)
 #pragma unroll
@@ -356,6 +419,7 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
 #pragma unroll
                     for (int oj = 0; oj <= PP - oi; oj++) acc[gx_mi(oi, oj)] += sm * A[gx_mi(i + oi, j + oj)];
             }
+        src = nsrc;
     }
     // G = -A: L[T] = -(1/T!) sum_S M'[S] A[S+T]
 #pragma unroll
@@ -364,7 +428,7 @@ __global__ void __launch_bounds__(128) k_m2l_exact(int64_t nn, const IDX *__rest
         for (int oj = 0; oj <= PP - oi; oj++) {
             int k = gx_mi(oi, oj);
             T v = warp_sum_t<T>(acc[k]);
-            if (lane == (k & 31)) L[node * NS + k] = v * (T)(-cinvfact(oi) * cinvfact(oj));
+            if (lane == (k & 31)) L[node * NS + k] = v * -tab_ifp<T>(oi, oj);
         }
 }
 
@@ -392,7 +456,7 @@ __device__ __forceinline__ void l2l_shift(const T *__restrict__ LP, T dx, T dy, 
             for (int i = oi; i <= PP; i++)
 #pragma unroll
                 for (int j = oj; j <= PP - i; j++)
-                    sum += lp[gx_mi(i, j)] * (T)(cbinom(i, oi) * cbinom(j, oj)) * px[i - oi] * py[j - oj];
+                    sum += lp[gx_mi(i, j)] * (tab_binom<T>(i, oi) * tab_binom<T>(j, oj)) * px[i - oi] * py[j - oj];
             out[gx_mi(oi, oj)] += sum;
         }
 }
@@ -593,13 +657,16 @@ __global__ void __launch_bounds__(128) k_p2p64_items(int64_t n_items, const int3
 // FP32 partials on coordinates relative to the target leaf's COM.  Bodies come packed
 // as (x - com_leaf, y - com_leaf, m) in FP32 (written by P2M); a source leaf is moved
 // into the target's frame by one FP32 shift per leaf pair, formed in FP64 and rounded once.
-__global__ void __launch_bounds__(128) k_p2p32_items(int64_t n_items, const int32_t *__restrict__ item_leaf,
+// 7 blocks per SM: 72 registers, no spills (left alone, ptxas picks 64 and spills)
+__global__ void __launch_bounds__(128, 7) k_p2p32_items(int64_t n_items, const int32_t *__restrict__ item_leaf,
                                                      const int64_t *__restrict__ item_qb, const int32_t *__restrict__ item_nq,
                                                      const float4 *__restrict__ pos, const double *__restrict__ comx,
                                                      const double *__restrict__ comy, const int32_t *__restrict__ bs,
                                                      const int32_t *__restrict__ be, const int32_t *__restrict__ src_idx,
                                                      float eps2, int tchunks, float2 *__restrict__ part) {
-    __shared__ float4 sb[4][32];
+    // staged sources, one row of 32 per warp, as x / y / m planes so that one
+    // broadcast 16-byte load yields the x (or y, m) of four consecutive sources
+    __shared__ __align__(16) float sx[4][32], sy[4][32], sm[4][32];
     int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (it >= n_items) return;
@@ -631,7 +698,12 @@ __global__ void __launch_bounds__(128) k_p2p32_items(int64_t n_items, const int3
         bool valid = i < t1;
         float4 me = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         float xi = me.x, yi = me.y;
-        float ax0 = 0.f, ay0 = 0.f, ax1 = 0.f, ay1 = 0.f;
+        const uint64_t XI = pk2(xi, xi), YI = pk2(yi, yi), E2 = pk2(eps2, eps2);
+        // full 32-source rows: four packed accumulator chains (sources 4q, 4q+1 in
+        // AXa/AYa; 4q+2, 4q+3 in AXb/AYb) so consecutive updates are independent;
+        // the own leaf and partial rows go through the scalar loop into axs/ays
+        uint64_t AXa = 0, AYa = 0, AXb = 0, AYb = 0;  // bit pattern 0 = (0.f, 0.f)
+        float axs = 0.f, ays = 0.f;
         if (t0 + tc * 32 < t1) {
             float4 cur = fetch(0, 0);
             for (int k = 0; k < nq; k++) {
@@ -642,47 +714,55 @@ __global__ void __launch_bounds__(128) k_p2p32_items(int64_t n_items, const int3
                     if (sc + 32 < s1 - s0) nxt = fetch(k, sc + 32);
                     else nxt = (k + 1 < nq) ? fetch(k + 1, 0) : make_float4(0.f, 0.f, 0.f, 0.f);
                     __syncwarp();
-                    sb[w][lane] = cur;
+                    sx[w][lane] = cur.x;
+                    sy[w][lane] = cur.y;
+                    sm[w][lane] = cur.z;
                     __syncwarp();
                     int ns = min(32, s1 - s0 - sc);
-                    if (srcl == leaf) {
-                        for (int kk = 0; kk < ns; kk++) {
-                            float4 bb = sb[w][kk];
-                            float dx = bb.x - xi, dy = bb.y - yi;
-                            float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
-                            float f = bb.z * (ir * ir * ir);
-                            f = (s0 + sc + kk == i) ? 0.f : f;
-                            ax0 = fmaf(f, dx, ax0);
-                            ay0 = fmaf(f, dy, ay0);
-                        }
-                    } else if (ns == 32) {
+                    if (ns == 32 && srcl != leaf) {
 #pragma unroll
-                        for (int kk = 0; kk < 32; kk += 2) {
-                            float4 b0 = sb[w][kk], b1 = sb[w][kk + 1];
-                            float dx0 = b0.x - xi, dy0 = b0.y - yi, dx1 = b1.x - xi, dy1 = b1.y - yi;
-                            float ir0 = rsqrt_fast(fmaf(dx0, dx0, fmaf(dy0, dy0, eps2)));
-                            float ir1 = rsqrt_fast(fmaf(dx1, dx1, fmaf(dy1, dy1, eps2)));
-                            float f0 = b0.z * (ir0 * ir0 * ir0), f1 = b1.z * (ir1 * ir1 * ir1);
-                            ax0 = fmaf(f0, dx0, ax0);
-                            ay0 = fmaf(f0, dy0, ay0);
-                            ax1 = fmaf(f1, dx1, ax1);
-                            ay1 = fmaf(f1, dy1, ay1);
+                        for (int kk = 0; kk < 32; kk += 4) {
+                            float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
+                            float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
+                            float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
+                            uint64_t dx0 = sub2(pk2(X.x, X.y), XI), dy0 = sub2(pk2(Y.x, Y.y), YI);
+                            uint64_t dx1 = sub2(pk2(X.z, X.w), XI), dy1 = sub2(pk2(Y.z, Y.w), YI);
+                            uint64_t r0 = fma2(dx0, dx0, fma2(dy0, dy0, E2));
+                            uint64_t r1 = fma2(dx1, dx1, fma2(dy1, dy1, E2));
+                            float ra, rb;
+                            upk2(r0, ra, rb);
+                            uint64_t i0 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                            upk2(r1, ra, rb);
+                            uint64_t i1 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                            uint64_t f0 = mul2(pk2(Mq.x, Mq.y), mul2(mul2(i0, i0), i0));
+                            uint64_t f1 = mul2(pk2(Mq.z, Mq.w), mul2(mul2(i1, i1), i1));
+                            AXa = fma2(f0, dx0, AXa);
+                            AYa = fma2(f0, dy0, AYa);
+                            AXb = fma2(f1, dx1, AXb);
+                            AYb = fma2(f1, dy1, AYb);
                         }
                     } else {
+                        const bool own = srcl == leaf;
                         for (int kk = 0; kk < ns; kk++) {
-                            float4 bb = sb[w][kk];
-                            float dx = bb.x - xi, dy = bb.y - yi;
+                            float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
                             float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
-                            float f = bb.z * (ir * ir * ir);
-                            ax0 = fmaf(f, dx, ax0);
-                            ay0 = fmaf(f, dy, ay0);
+                            float fk = sm[w][kk] * (ir * ir * ir);
+                            fk = (own && s0 + sc + kk == i) ? 0.f : fk;
+                            axs = fmaf(fk, dx, axs);
+                            ays = fmaf(fk, dy, ays);
                         }
                     }
                     cur = nxt;
                 }
             }
         }
-        part[(it * tchunks + tc) * 32 + lane] = make_float2(ax0 + ax1, ay0 + ay1);
+        float a0, a1, a2, a3, b0, b1, b2, b3;
+        upk2(AXa, a0, a1);
+        upk2(AXb, a2, a3);
+        upk2(AYa, b0, b1);
+        upk2(AYb, b2, b3);
+        part[(it * tchunks + tc) * 32 + lane] =
+            make_float2(((a0 + a1) + (a2 + a3)) + axs, ((b0 + b1) + (b2 + b3)) + ays);
     }
 }
 

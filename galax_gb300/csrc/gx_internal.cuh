@@ -109,10 +109,11 @@ struct gx_ctx {
 
     // adjoint: cotangents, VJP outputs, transposed expansions, checkpoints
     DevBuf adj_lx, adj_ly, adj_lvx, adj_lvy, adj_lm, adj_gx, adj_gy, adj_gm, adj_lax, adj_lay, adj_lf;
-    DevBuf adj_dL, adj_dM, adj_dMleaf;
+    DevBuf adj_dL, adj_dM, adj_dMleaf, adj_lam32;
     DevBuf ckpt, seg;
     int64_t roll_steps = 0, roll_k = 1;
     double roll_dt = 0.0;
+    int roll_prec = GX_PREC_FP64;
     bool roll_valid = false;
 
     // scratch

@@ -415,35 +415,62 @@ __device__ __forceinline__ bool mac_far(const double *comx, const double *comy, 
     return __dmul_rn(d, theta) > __dadd_rn(R[a], R[b]);
 }
 
-// Per node x of a level: children of Near(parent(x)) split into far (M2L) and near.
+// Per node x of a level: children of Near(parent(x)) split into far (M2L) and near,
+// in the order (parent's near entry, child slot).  One warp per node: the lanes take
+// 32 consecutive near entries of the parent at a time and place their children with a
+// warp prefix sum, so a node whose parent has a long near list (a wide leaf of the
+// sparse halo can be near every other leaf) costs len/32 rounds, not len.
 __global__ void k_mac(int64_t s, int64_t e, int pass, const int32_t *parent, const int4 *child, const double *comx,
                       const double *comy, const double *R, double theta, const int64_t *near_start,
                       const int32_t *near_cnt, const int32_t *near_idx_in, int32_t *fcnt, int32_t *ncnt,
                       const int64_t *fstart, const int64_t *nstart, int32_t *far_idx, int32_t *near_idx) {
-    int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= e) return;
+    const unsigned full = 0xffffffffu;
+    int lane = threadIdx.x & 31;
+    int64_t x = s + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (x >= e) return;  // whole warps leave together
     int32_t P = parent[x];
     int32_t nf = 0, nn = 0;
     int64_t fb = pass ? fstart[x] : 0, nb = pass ? nstart[x] : 0;
     if (P >= 0) {
         int64_t q0 = near_start[P], q1 = q0 + near_cnt[P];
-        for (int64_t q = q0; q < q1; q++) {
-            int4 c4 = child[near_idx_in[q]];
-            int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-            for (int k = 0; k < 4; k++) {
-                int c = cc[k];
-                if (c < 0) continue;
-                if (mac_far(comx, comy, R, x, c, theta)) {
-                    if (pass) far_idx[fb + nf] = c;
-                    nf++;
-                } else {
-                    if (pass) near_idx[nb + nn] = c;
-                    nn++;
+        for (int64_t qb = q0; qb < q1; qb += 32) {
+            int64_t q = qb + lane;
+            int cc[4] = {-1, -1, -1, -1};
+            unsigned fm = 0, nm = 0;
+            if (q < q1) {
+                int4 c4 = child[near_idx_in[q]];
+                cc[0] = c4.x;
+                cc[1] = c4.y;
+                cc[2] = c4.z;
+                cc[3] = c4.w;
+                for (int k = 0; k < 4; k++) {
+                    if (cc[k] < 0) continue;
+                    if (mac_far(comx, comy, R, x, cc[k], theta)) fm |= 1u << k;
+                    else nm |= 1u << k;
                 }
             }
+            int myf = __popc(fm), myn = __popc(nm);
+            int pf = myf, pn = myn;  // inclusive warp scans
+            for (int o = 1; o < 32; o <<= 1) {
+                int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
+                if (lane >= o) {
+                    pf += tf;
+                    pn += tn;
+                }
+            }
+            int tf = __shfl_sync(full, pf, 31), tn = __shfl_sync(full, pn, 31);
+            if (pass) {
+                int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
+                for (int k = 0; k < 4; k++) {
+                    if ((fm >> k) & 1u) far_idx[a++] = cc[k];
+                    if ((nm >> k) & 1u) near_idx[b++] = cc[k];
+                }
+            }
+            nf += tf;
+            nn += tn;
         }
     }
-    if (!pass) {
+    if (!pass && lane == 0) {
         fcnt[x] = nf;
         ncnt[x] = nn;
     }
@@ -793,7 +820,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
     GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int64_t) * (size_t)(nn + 1) * 2));
     for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
         int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
-        k_mac<<<gx_blocks(c, 128), 128, 0, ctx->stream>>>(s, e, 0, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
+        k_mac<<<gx_blocks(c * 32, 128), 128, 0, ctx->stream>>>(s, e, 0, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
                                                           dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta,
                                                           nstart, ncnt, dptr<int32_t>(ctx->near_idx), fcnt, ncnt,
                                                           nullptr, nullptr, nullptr, nullptr);
@@ -829,7 +856,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
         // starts = level offsets + running totals
         GX_TRY(gx_add_offsets(ctx, fo, fstart + s, c, far_tot));
         GX_TRY(gx_add_offsets(ctx, no, nstart + s, c, near_tot));
-        k_mac<<<gx_blocks(c, 128), 128, 0, ctx->stream>>>(s, e, 1, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
+        k_mac<<<gx_blocks(c * 32, 128), 128, 0, ctx->stream>>>(s, e, 1, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
                                                           dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta,
                                                           nstart, ncnt, dptr<int32_t>(ctx->near_idx), fcnt, ncnt, fstart,
                                                           nstart, dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx));

@@ -34,15 +34,20 @@ def test_force_vjp_matches_finite_differences(G, preset, n, p):
     rng = np.random.default_rng(1)
     lx, ly = rng.standard_normal(n), rng.standard_normal(n)
     gx, gy, gm = ctx.force_vjp(lx, ly)
-    scale = np.std(b.x)
-    for _ in range(3):
+    # h well below the closest pair separations (the FD truncation error goes as (h/r)^2)
+    # and well above the rounding noise of the forces
+    h = 1e-6
+    for kind in ("positions", "masses", "both"):
         dx, dy, dm = rng.standard_normal(n), rng.standard_normal(n), rng.standard_normal(n) * b.mass
-        h = 1e-6 * scale
-        ap = _forces(ctx, b.x + h * dx, b.y + h * dy, b.mass + h * dm / scale)
-        am = _forces(ctx, b.x - h * dx, b.y - h * dy, b.mass - h * dm / scale)
+        if kind == "positions":
+            dm = np.zeros(n)
+        elif kind == "masses":
+            dx, dy = np.zeros(n), np.zeros(n)
+        ap = _forces(ctx, b.x + h * dx, b.y + h * dy, b.mass + h * dm)
+        am = _forces(ctx, b.x - h * dx, b.y - h * dy, b.mass - h * dm)
         fd = (np.dot(lx, ap[0] - am[0]) + np.dot(ly, ap[1] - am[1])) / (2 * h)
-        an = np.dot(gx, dx) + np.dot(gy, dy) + np.dot(gm, dm) / scale
-        assert abs(fd - an) <= 1e-6 * abs(fd), (fd, an)
+        an = np.dot(gx, dx) + np.dot(gy, dy) + np.dot(gm, dm)
+        assert abs(fd - an) <= 1e-6 * abs(fd), (kind, fd, an)
     ctx.close()
 
 
@@ -136,14 +141,15 @@ def test_checkpoint_interval_does_not_change_the_gradient(G):
 
 
 def test_rollout_gradient_close_to_exact_n2_adjoint(G, oracle):
-    """The FMM rollout gradient against the exact FP64 N^2 reverse leapfrog (2000 bodies)."""
+    """The FMM rollout gradient against the exact FP64 N^2 reverse leapfrog: a 2000-body
+    galaxy (central mass and 1999 test particles), 100 steps."""
     from galax_gb300 import presets
-    n, T, dt = 2_000, 10, 2e-3
+    n, T, dt = 2_000, 100, 2e-3
     b = presets.galaxy(n, seed=55)
     ctx = _ctx(G, b, presets.BOUNDS["galaxy"], 0.05)
     R = _rot(-0.7)
     ctx.upload_bodies(b)
-    ctx.rollout_forward(T, dt, 3)
+    ctx.rollout_forward(T, dt, 10)
     fin = G.Bodies.new(n)
     ctx.download_bodies(fin)
     L, lxT, lyT, dx0, dy0 = _loss_and_grads(b.x, b.y, fin.x, fin.y, R)
@@ -153,3 +159,77 @@ def test_rollout_gradient_close_to_exact_n2_adjoint(G, oracle):
     for k in range(5):
         err = np.linalg.norm(g[k] - r[k]) / np.linalg.norm(r[k])
         assert err < 1e-3, (k, err)
+
+
+def test_mixed_force_vjp_close_to_fp64(G):
+    """The FP32 (mixed) VJP against the FP64 VJP of the same tree and lists."""
+    from galax_gb300 import presets
+    n = 20_000
+    b = presets.plummer(n, seed=56)
+    ctx = _ctx(G, b, presets.BOUNDS["plummer"], 0.05)
+    rng = np.random.default_rng(4)
+    lx, ly = rng.standard_normal(n), rng.standard_normal(n)
+    r64 = ctx.force_vjp(lx, ly)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    r32 = ctx.force_vjp(lx, ly)
+    ctx.close()
+    ex = np.linalg.norm(np.hypot(r32[0] - r64[0], r32[1] - r64[1])) / np.linalg.norm(np.hypot(r64[0], r64[1]))
+    em = np.linalg.norm(r32[2] - r64[2]) / np.linalg.norm(r64[2])
+    assert ex < 1e-4 and em < 1e-4, (ex, em)
+
+
+def _rollout_grad(ctx, G, b, T, dt, k, R):
+    n = len(b)
+    ctx.upload_bodies(b)
+    ctx.rollout_forward(T, dt, k)
+    fin = G.Bodies.new(n)
+    ctx.download_bodies(fin)
+    L, lxT, lyT, dx0, dy0 = _loss_and_grads(b.x, b.y, fin.x, fin.y, R)
+    gx, gy, gvx, gvy, gm, peak = ctx.rollout_backward(lxT, lyT, np.zeros(n), np.zeros(n))
+    return gx + dx0, gy + dy0, gvx, gvy, gm
+
+
+def test_mixed_rollout_gradient_close_to_fp64(G):
+    from galax_gb300 import presets
+    n, T, dt = 4_001, 20, 2e-3
+    b = presets.galaxy(n, seed=57)
+    ctx = _ctx(G, b, presets.BOUNDS["galaxy"], 0.05)
+    R = _rot(0.9)
+    g64 = _rollout_grad(ctx, G, b, T, dt, 4, R)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    g32 = _rollout_grad(ctx, G, b, T, dt, 4, R)
+    ctx.close()
+    for k in range(5):
+        err = np.linalg.norm(g32[k] - g64[k]) / np.linalg.norm(g64[k])
+        assert err < 1e-3, (k, err)
+
+
+def test_mixed_checkpoint_interval_does_not_change_the_gradient(G):
+    from galax_gb300 import presets
+    n, T, dt = 3_001, 13, 2e-3
+    b = presets.galaxy(n, seed=58)
+    ctx = _ctx(G, b, presets.BOUNDS["galaxy"], 0.05)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    R = _rot(0.2)
+    res = [_rollout_grad(ctx, G, b, T, dt, k, R) for k in (1, 4, 13, 20)]
+    ctx.close()
+    for r in res[1:]:
+        for a, c in zip(r, res[0]):
+            assert np.array_equal(a, c)
+
+
+def test_rollout_backward_needs_forward_and_same_precision(G):
+    from galax_gb300 import presets
+    n = 2_001
+    b = presets.galaxy(n, seed=59)
+    ctx = _ctx(G, b, presets.BOUNDS["galaxy"], 0.05)
+    z = np.zeros(n)
+    with pytest.raises(G.GpuError):
+        ctx.rollout_backward(z, z, z, z)
+    ctx.rollout_forward(3, 1e-3, 2)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    with pytest.raises(G.GpuError):
+        ctx.rollout_backward(z, z, z, z)
+    with pytest.raises(ValueError):
+        ctx.force_vjp(z[:10], z[:10])
+    ctx.close()
