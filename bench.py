@@ -174,25 +174,30 @@ def _rot(theta):
     return np.array([[c, -s], [s, c]])
 
 
-def _rollout_loss(x0, y0, xT, yT, R):
-    """L = sum |x_T - R x_0|^2 and its partials dL/dx_T, dL/dx_0 (direct term)."""
-    tx = R[0, 0] * x0 + R[0, 1] * y0
-    ty = R[1, 0] * x0 + R[1, 1] * y0
+def _rollout_loss(x0, y0, xT, yT, R, ids=None):
+    """L = sum_i |x_T[i] - R x_0[ids[i]]|^2 (ids: the starting index of each final body,
+    identity without rebuilds), its cotangent dL/dx_T and the direct term dL/dx_0."""
+    ids = np.arange(x0.size) if ids is None else ids
+    tx = R[0, 0] * x0[ids] + R[0, 1] * y0[ids]
+    ty = R[1, 0] * x0[ids] + R[1, 1] * y0[ids]
     rx, ry = xT - tx, yT - ty
-    return (float(np.sum(rx * rx + ry * ry)), 2 * rx, 2 * ry, -2 * (R[0, 0] * rx + R[1, 0] * ry),
-            -2 * (R[0, 1] * rx + R[1, 1] * ry))
+    d0x, d0y = np.zeros(x0.size), np.zeros(x0.size)
+    d0x[ids] = -2 * (R[0, 0] * rx + R[1, 0] * ry)
+    d0y[ids] = -2 * (R[0, 1] * rx + R[1, 1] * ry)
+    return float(np.sum(rx * rx + ry * ry)), 2 * rx, 2 * ry, d0x, d0y
 
 
-def _adjoint_run(G, ctx, b, T, dt, k, R):
+def _adjoint_run(G, ctx, b, T, dt, k, R, rebuild=0):
     """One forward rollout and its reverse pass; returns times, gradients and peak bytes."""
     n = len(b)
     ctx.upload_bodies(b)
     t0 = time.perf_counter()
-    ctx.rollout_forward(T, dt, k)
+    ctx.rollout_forward(T, dt, k, rebuild)
     t_fwd = time.perf_counter() - t0
     fin = G.Bodies.new(n)
     ctx.download_bodies(fin)
-    L, lxT, lyT, dx0, dy0 = _rollout_loss(b.x, b.y, fin.x, fin.y, R)
+    ids = ctx.body_ids() if rebuild else None
+    L, lxT, lyT, dx0, dy0 = _rollout_loss(b.x, b.y, fin.x, fin.y, R, ids)
     z = np.zeros(n)
     t0 = time.perf_counter()
     gx, gy, gvx, gvy, gm, peak = ctx.rollout_backward(lxT, lyT, z, z)
@@ -200,14 +205,16 @@ def _adjoint_run(G, ctx, b, T, dt, k, R):
     return t_fwd, t_bwd, (gx + dx0, gy + dy0, gvx, gvy, gm), peak, L
 
 
-def _loss_only(G, ctx, b, T, dt, R):
+def _loss_only(G, ctx, b, T, dt, R, rebuild=0, bounds=None):
     n = len(b)
     ctx.upload_bodies(b)
+    if rebuild:  # as the rollout does: the tree of the starting positions first
+        ctx.rebuild_resident(N_MAX, bounds)
     ctx.forces_resident()
-    ctx.kdk_run(T, dt, 0)
+    ctx.kdk_run(T, dt, 0, rebuild_every=rebuild)
     fin = G.Bodies.new(n)
     ctx.download_bodies(fin)
-    return _rollout_loss(b.x, b.y, fin.x, fin.y, R)[0]
+    return _rollout_loss(b.x, b.y, fin.x, fin.y, R, ctx.body_ids() if rebuild else None)[0]
 
 
 def _grad_rel(g, r):
@@ -221,11 +228,15 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
     GPU adjoint on a 20-step prefix).  The comparison with the exact FP64 N^2 adjoint
     on a 2000-body subset is a test (tests/test_gpu_adjoint.py)."""
     out = {}
-    # ---- galaxy, N = 200,001, 100 steps
+    # ---- galaxy, N = 200,001, 100 steps at the CLI time step.  The inner orbits
+    # (R = 1, v = 31.6) cross many leaves per step, and with a static tree the
+    # expansions diverge within ~30 steps (the oracle does the same), so the tree is
+    # rebuilt on the device before every step's force evaluation.
     n, T = 200_001, 100
+    bounds = presets.BOUNDS["galaxy"]
     bg = presets.galaxy(n, seed=args.seed + 4)
     cg = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 24, p=P, eps64=0.1))
-    cg.build_tree(bg, N_MAX, presets.BOUNDS["galaxy"])
+    cg.build_tree(bg, N_MAX, bounds)
     eps = presets.cli_softening(bg.x, bg.y)
     cg.set_params(P, eps)
     cg.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
@@ -236,15 +247,16 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
     dt = presets.cli_dt(a0.ax, a0.ay)
     R = _rot(float(np.random.default_rng(args.seed + 5).uniform(0, 2 * np.pi)))
     k = 10
-    gal = {"workload": f"galaxy N={n}, p={P}, n_max={N_MAX}, {T} steps, dt={dt:.4g} (CLI rule), "
-                       f"checkpoint every {k} steps", "eps": eps}
+    gal = {"workload": f"galaxy N={n}, p={P}, n_max={N_MAX}, {T} steps, dt={dt:.4g} (CLI rule), tree rebuilt "
+                       f"every step, checkpoint every {k} steps", "eps": eps}
     grads = {}
     for name, prec in (("fp64", G.PREC_FP64), ("mixed", G.PREC_MIXED)):
         cg.set_mode(G.MODE_ACCURATE, prec, THETA)
-        _adjoint_run(G, cg, bg, 5, dt, k, R)  # warm-up
-        tf, tb, g, peak, L = _adjoint_run(G, cg, bg, T, dt, k, R)
+        _adjoint_run(G, cg, bg, 3, dt, k, R, rebuild=1)  # warm-up
+        tf, tb, g, peak, L = _adjoint_run(G, cg, bg, T, dt, k, R, rebuild=1)
         grads[name] = g
-        gal[name] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak}
+        gal[name] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak,
+                     "steps_per_s_forward": T / tf}
     gal["mixed"]["grad_rel_err_vs_fp64"] = _grad_rel(grads["mixed"], grads["fp64"])
     # central finite differences of the FP64 rollout, h = 1e-6, seeded directions
     cg.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
@@ -256,7 +268,7 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
         def L_at(sg):
             pb = G.Bodies.from_arrays(bg.x + sg * h * d[0], bg.y + sg * h * d[1], bg.mass + sg * h * d[4],
                                       bg.vx + sg * h * d[2], bg.vy + sg * h * d[3])
-            return _loss_only(G, cg, pb, T, dt, R)
+            return _loss_only(G, cg, pb, T, dt, R, rebuild=1, bounds=bounds)
         num = (L_at(1) - L_at(-1)) / (2 * h)
         g = grads["fp64"]
         an = sum(float(np.dot(g[q], d[q])) for q in range(5))
@@ -274,7 +286,8 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
     for k in args.adj_k:
         _adjoint_run(G, ctx1m, b1m, 3, dt, k, Rp)  # warm-up (allocations)
         tf, tb, g, peak, L = _adjoint_run(G, ctx1m, b1m, T, dt, k, Rp)
-        sweep[str(k)] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak}
+        sweep[str(k)] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak,
+                         "finite": bool(all(np.all(np.isfinite(a)) for a in g)) and bool(np.isfinite(L))}
     # gradient of a 20-step prefix: mixed against FP64 (the FP64 form is ~50x slower)
     Tp = 20
     _, _, gm20, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp)
@@ -361,6 +374,24 @@ def run_ours(args, rank, world, local, pg):
     e2e_ms = _max_over_ranks(pg, float(np.mean(e2e_t)) * 1e3)
     peak32 = ctx.probe_fp32_tflops()
 
+    # whole steps (kick, drift, forces, kick) with the static tree and with the tree
+    # rebuilt on the device before every force evaluation (mixed form, dt = 1e-3)
+    steps_cmp = {}
+    for rb in (0, 1):
+        ctx.upload_bodies(gb)
+        if rb:
+            ctx.rebuild_resident(N_MAX, bounds)
+        ctx.forces_resident()
+        ctx.kdk_run(2, 1e-3, 0, rebuild_every=rb)  # warm-up
+        _barrier(pg)
+        t0 = time.perf_counter()
+        ctx.kdk_run(args.steps, 1e-3, 0, rebuild_every=rb)
+        t_s = (time.perf_counter() - t0) / args.steps
+        steps_cmp["rebuild_every_step" if rb else "static_tree"] = {
+            "ms_per_step": t_s * 1e3, "bodies_per_s": n / t_s, "steps_per_s": 1.0 / t_s}
+    ctx.upload_bodies(gb)
+    ctx.rebuild_resident(N_MAX, bounds)  # back to the tree of the starting positions (gb is in its order)
+
     adjoint = None
     if not args.no_adjoint and world == 1:
         adjoint = run_adjoint(G, presets, ctx, gb, args)
@@ -404,6 +435,7 @@ def run_ours(args, rank, world, local, pg):
                           "median_rel_diff": float(np.median(d))},
         "tree": {"nodes": nn, "leaves": nl, "levels": nlev, "build_s_incl_host_copies": setup_tree_s},
         "cpu_baseline": cpu,
+        "kdk_steps": steps_cmp,
         "adjoint": adjoint if adjoint is not None else "not run (--no-adjoint, or N>1 replicas: see the N=1 line)",
     }
     if adjoint is not None:

@@ -80,6 +80,7 @@ def lib():
         "gx_upload_tree": (C.c_int, [_VP, C.c_int64, C.c_int64, _D, _D, _D, _D, _D, _D, _I64, _I64, _I32, _I32, _U8,
                                      _U32, _U8, _U32, _U8]),
         "gx_build_tree": (C.c_int, [_VP, C.c_int64, _D, _D, _D, _D, _D, _D, _D, C.c_int64, _D, C.c_int]),
+        "gx_rebuild_resident": (C.c_int, [_VP, C.c_int64, _D, C.c_int, _I64]),
         "gx_tree_info": (C.c_int, [_VP, _I64, _I64, _I32, _I64]),
         "gx_export_tree": (C.c_int, [_VP, _D, _D, _D, _D, _D, _D, _I64, _I64, _I32, _I32, _U8, _I64]),
         "gx_export_lists": (C.c_int, [_VP, C.c_int, _U32, _U8]),
@@ -97,7 +98,9 @@ def lib():
         "gx_probe_fp32_tflops": (C.c_int, [_VP, _D]),
         "gx_n2_sampled_static": (C.c_int, [_VP, _VP, _VP, C.c_int64, C.c_double, _I64, C.c_int64, _D, _D, _VP]),
         "gx_force_vjp": (C.c_int, [_VP, _D, _D, _D, _D, _D]),
-        "gx_rollout_forward": (C.c_int, [_VP, C.c_int64, C.c_double, C.c_int64]),
+        "gx_rollout_forward": (C.c_int, [_VP, C.c_int64, C.c_double, C.c_int64, C.c_int64]),
+        "gx_kdk_run_rebuild": (C.c_int, [_VP, C.c_int64, C.c_double, C.c_int64, C.c_int64, _D, _I64]),
+        "gx_body_ids": (C.c_int, [_VP, _I64]),
         "gx_rollout_backward": (C.c_int, [_VP, _D, _D, _D, _D, _D, _D, _D, _D, _D, _I64]),
         "gx_host_alloc": (_VP, [C.c_size_t]),
         "gx_host_free": (None, [_VP]),
@@ -300,6 +303,17 @@ class GpuContext:
         arrs = [_f64(a) for a in (bodies.x, bodies.y, bodies.vx, bodies.vy, bodies.mass, bodies.ax, bodies.ay)]
         self._check(lib().gx_build_tree(self._h, len(bodies), *[_p(a) for a in arrs], int(n_max), _p(b),
                                         BUILD_BALANCED if balanced else 0))
+        self._n_resident = len(bodies)
+
+    def rebuild_resident(self, n_max: int, bounds, balanced: bool = False, want_perm: bool = False):
+        """Tree::build over the resident bodies (they are permuted on the device); returns,
+        if asked, each body's index before the rebuild."""
+        b = np.ascontiguousarray(np.asarray(bounds, np.float64))
+        n = getattr(self, "_n_resident", 0)
+        perm = np.zeros(n, np.int64) if (want_perm and n > 0) else None
+        self._check(lib().gx_rebuild_resident(self._h, int(n_max), _p(b), BUILD_BALANCED if balanced else 0,
+                                              _p(perm, _I64) if perm is not None else None))
+        return perm
 
     def tree_info(self):
         nn, nl, nb = C.c_int64(), C.c_int64(), C.c_int64()
@@ -374,6 +388,7 @@ class GpuContext:
     def upload_bodies(self, b: Bodies) -> None:
         arrs = [_f64(a) for a in (b.x, b.y, b.vx, b.vy, b.mass, b.ax, b.ay)]
         self._check(lib().gx_upload_bodies(self._h, len(b), *[_p(a) for a in arrs]))
+        self._n_resident = len(b)
 
     def download_bodies(self, b: Bodies) -> None:
         arrs = [_f64(a) for a in (b.x, b.y, b.vx, b.vy, b.mass, b.ax, b.ay)]
@@ -382,11 +397,13 @@ class GpuContext:
     def forces_resident(self) -> None:
         self._check(lib().gx_forces_resident(self._h))
 
-    def kdk_run(self, n_steps: int, dt: float, energy_every: int = 0) -> np.ndarray:
+    def kdk_run(self, n_steps: int, dt: float, energy_every: int = 0, rebuild_every: int = 0) -> np.ndarray:
+        """Device-resident leapfrog; rebuild_every > 0 rebuilds the tree every that many steps."""
         rows = n_steps // energy_every if energy_every > 0 else 0
         diag = np.zeros(6 * max(rows, 1))
         nd = C.c_int64()
-        self._check(lib().gx_kdk_run(self._h, int(n_steps), float(dt), int(energy_every), _p(diag), C.byref(nd)))
+        self._check(lib().gx_kdk_run_rebuild(self._h, int(n_steps), float(dt), int(energy_every), int(rebuild_every),
+                                             _p(diag), C.byref(nd)))
         return diag[: 6 * nd.value].reshape(nd.value, 6)
 
     def diagnostics(self) -> np.ndarray:
@@ -428,8 +445,17 @@ class GpuContext:
                                        _p(_f64(np.ascontiguousarray(lam_y, np.float64))), _p(gx), _p(gy), _p(gm)))
         return gx, gy, gm
 
-    def rollout_forward(self, n_steps: int, dt: float, checkpoint_every: int) -> None:
-        self._check(lib().gx_rollout_forward(self._h, int(n_steps), float(dt), int(checkpoint_every)))
+    def rollout_forward(self, n_steps: int, dt: float, checkpoint_every: int, rebuild_every: int = 0) -> None:
+        self._check(lib().gx_rollout_forward(self._h, int(n_steps), float(dt), int(checkpoint_every),
+                                             int(rebuild_every)))
+
+    def body_ids(self) -> np.ndarray:
+        """For every resident body, its index in the order of the last upload / build_tree
+        (device rebuilds reorder the bodies)."""
+        ids = np.zeros(getattr(self, "_n_resident", 0), np.int64)
+        if ids.size:
+            self._check(lib().gx_body_ids(self._h, _p(ids, _I64)))
+        return ids
 
     def rollout_backward(self, lx, ly, lvx, lvy):
         """Gradients at step 0: (g_x, g_y, g_vx, g_vy, g_m, peak_device_bytes)."""

@@ -152,7 +152,6 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1)
               const float4 *__restrict__ comhl, double eps2d, const T *__restrict__ dL, T *__restrict__ dM) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<T>(NC);
-    constexpr int ND = nc2(2 * P);
     const int PP = gx_rt_order(P);
     const int NCr = (PP + 1) * (PP + 2) / 2;
     int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -181,18 +180,11 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1)
             dx = comx[t] - scx;
             dy = comy[t] - scy;
         }
-        T A[ND];
-        derivs_scaled<P, T>(dx, dy, eps2, A);
 #pragma unroll
         for (int ti = 0; ti <= PP; ti++)
 #pragma unroll
-            for (int tj = 0; tj <= PP - ti; tj++) {
-                T w = lt[gx_mi(ti, tj)] * tab_ifp<T>(ti, tj);
-#pragma unroll
-                for (int si = 0; si <= PP; si++)
-#pragma unroll
-                    for (int sj = 0; sj <= PP - si; sj++) acc[gx_mi(si, sj)] += w * A[gx_mi(si + ti, sj + tj)];
-            }
+            for (int tj = 0; tj <= PP - ti; tj++) lt[gx_mi(ti, tj)] *= tab_ifp<T>(ti, tj);
+        m2l_fused<P, T>(dx, dy, eps2, lt, acc);
         t = nt;
     }
 #pragma unroll
@@ -353,7 +345,10 @@ __global__ void __launch_bounds__(128) k_adj_p2p_items(int64_t n_items, const in
 
 // FP32 form of A6 on the packed bodies (u, v, m) and cotangents of k_adj_l2p<float>;
 // a source leaf is moved into the target leaf's frame by one FP32 shift per leaf
-// pair formed in FP64 (as in the mixed forward P2P).
+// pair formed in FP64 (as in the mixed forward P2P).  Full 32-source rows of other
+// leaves run on packed .f32x2 arithmetic, two sources per instruction (the lo half
+// of every accumulator takes the even sources, the hi half the odd ones); the own
+// leaf and partial rows run the scalar loop, which also skips the body itself.
 __global__ void __launch_bounds__(128, 6) k_adj_p2p32_items(int64_t n_items, const int32_t *__restrict__ item_leaf,
                                                          const int64_t *__restrict__ item_qb,
                                                          const int32_t *__restrict__ item_nq,
@@ -386,11 +381,15 @@ __global__ void __launch_bounds__(128, 6) k_adj_p2p32_items(int64_t n_items, con
         float4 me = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         float2 li = valid ? lam[i] : make_float2(0.f, 0.f);
         const float xi = me.x, yi = me.y, mi = me.z, lxi = li.x, lyi = li.y;
+        const uint64_t XI = pk2(xi, xi), YI = pk2(yi, yi), E2 = pk2(eps2, eps2), MI = pk2(mi, mi);
+        const uint64_t NLXI = pk2(-lxi, -lxi), NLYI = pk2(-lyi, -lyi), N3 = pk2(-3.f, -3.f);
+        uint64_t GX = 0, GY = 0, GMN = 0;  // packed sums; GMN accumulates +lam.d/r^3
         float gxa = 0.f, gya = 0.f, gma = 0.f;
         if (t0 + tc * 32 < t1) {
             for (int k = 0; k < nq; k++) {
                 int s0 = __shfl_sync(0xffffffffu, sbeg, k), s1 = __shfl_sync(0xffffffffu, send, k);
                 float gxs = __shfl_sync(0xffffffffu, shx, k), gys = __shfl_sync(0xffffffffu, shy, k);
+                int srcl = __shfl_sync(0xffffffffu, sl, k);
                 for (int sc = s0; sc < s1; sc += 32) {
                     int j = sc + lane;
                     __syncwarp();
@@ -405,27 +404,57 @@ __global__ void __launch_bounds__(128, 6) k_adj_p2p32_items(int64_t n_items, con
                     }
                     __syncwarp();
                     int ns = min(32, s1 - sc);
-                    for (int kk = 0; kk < ns; kk++) {
-                        float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
-                        float mj = sm[w][kk], lxj = slx[w][kk], lyj = sly[w][kk];
-                        float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
-                        float ir2 = ir * ir;
-                        float ir3 = ir2 * ir;
-                        float ir5 = ir3 * ir2;
-                        float wx = fmaf(mi, lxj, -mj * lxi), wy = fmaf(mi, lyj, -mj * lyi);
-                        float c = 3.f * ir5 * fmaf(dx, wx, dy * wy);
-                        float dl = fmaf(lxj, dx, lyj * dy);
-                        bool self = sc + kk == i;
-                        ir3 = self ? 0.f : ir3;
-                        c = self ? 0.f : c;
-                        gxa = fmaf(ir3, wx, fmaf(-c, dx, gxa));
-                        gya = fmaf(ir3, wy, fmaf(-c, dy, gya));
-                        gma = fmaf(-dl, ir3, gma);
+                    if (ns == 32 && srcl != leaf) {
+#pragma unroll 4
+                        for (int kk = 0; kk < 32; kk += 2) {
+                            const uint64_t X = *reinterpret_cast<const uint64_t *>(&sx[w][kk]);
+                            const uint64_t Y = *reinterpret_cast<const uint64_t *>(&sy[w][kk]);
+                            const uint64_t Mj = *reinterpret_cast<const uint64_t *>(&sm[w][kk]);
+                            const uint64_t LXj = *reinterpret_cast<const uint64_t *>(&slx[w][kk]);
+                            const uint64_t LYj = *reinterpret_cast<const uint64_t *>(&sly[w][kk]);
+                            const uint64_t dx = sub2(X, XI), dy = sub2(Y, YI);
+                            const uint64_t r2 = fma2(dx, dx, fma2(dy, dy, E2));
+                            float ra, rb;
+                            upk2(r2, ra, rb);
+                            const uint64_t ir = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                            const uint64_t ir2 = mul2(ir, ir);
+                            const uint64_t ir3 = mul2(ir2, ir);
+                            const uint64_t ir5 = mul2(ir3, ir2);
+                            const uint64_t wx = fma2(Mj, NLXI, mul2(MI, LXj));  // mi lx_j - m_j lx_i
+                            const uint64_t wy = fma2(Mj, NLYI, mul2(MI, LYj));
+                            const uint64_t nc = mul2(mul2(N3, ir5), fma2(dx, wx, mul2(dy, wy)));  // -3 dw / r^5
+                            GX = fma2(ir3, wx, fma2(nc, dx, GX));
+                            GY = fma2(ir3, wy, fma2(nc, dy, GY));
+                            GMN = fma2(fma2(LXj, dx, mul2(LYj, dy)), ir3, GMN);
+                        }
+                    } else {
+                        const bool own = srcl == leaf;
+                        for (int kk = 0; kk < ns; kk++) {
+                            float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
+                            float mj = sm[w][kk], lxj = slx[w][kk], lyj = sly[w][kk];
+                            float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                            float ir2 = ir * ir;
+                            float ir3 = ir2 * ir;
+                            float ir5 = ir3 * ir2;
+                            float wx = fmaf(mi, lxj, -mj * lxi), wy = fmaf(mi, lyj, -mj * lyi);
+                            float c = 3.f * ir5 * fmaf(dx, wx, dy * wy);
+                            float dl = fmaf(lxj, dx, lyj * dy);
+                            bool self = own && sc + kk == i;
+                            ir3 = self ? 0.f : ir3;
+                            c = self ? 0.f : c;
+                            gxa = fmaf(ir3, wx, fmaf(-c, dx, gxa));
+                            gya = fmaf(ir3, wy, fmaf(-c, dy, gya));
+                            gma = fmaf(-dl, ir3, gma);
+                        }
                     }
                 }
             }
         }
-        part[(it * tchunks + tc) * 32 + lane] = make_float4(gxa, gya, gma, 0.f);
+        float a0, a1, b0, b1, c0, c1;
+        upk2(GX, a0, a1);
+        upk2(GY, b0, b1);
+        upk2(GMN, c0, c1);
+        part[(it * tchunks + tc) * 32 + lane] = make_float4((a0 + a1) + gxa, (b0 + b1) + gya, gma - (c0 + c1), 0.f);
     }
 }
 

@@ -125,7 +125,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->p2p_idx, &ctx->ref_voff, &ctx->ref_did, &ctx->ref_G, &ctx->radius, &ctx->anc, &ctx->has_far_ref, &ctx->has_far_acc, &ctx->comhl, &ctx->far_off, &ctx->far_idx,
                       &ctx->near_off, &ctx->near_idx, &ctx->M, &ctx->L, &ctx->Lf, &ctx->Mf32, &ctx->Lf32,
                       &ctx->Lff32, &ctx->pos32, &ctx->part, &ctx->items_ref.leaf, &ctx->items_ref.qb, &ctx->items_ref.nq, &ctx->items_ref.off, &ctx->items_acc.leaf, &ctx->items_acc.qb, &ctx->items_acc.nq, &ctx->items_acc.off, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
-                      &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush, &ctx->adj_lx, &ctx->adj_ly, &ctx->adj_lvx, &ctx->adj_lvy, &ctx->adj_lm, &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm, &ctx->adj_lax, &ctx->adj_lay, &ctx->adj_lf, &ctx->adj_dL, &ctx->adj_dM, &ctx->adj_dMleaf, &ctx->adj_lam32, &ctx->ckpt, &ctx->seg};
+                      &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush, &ctx->adj_lx, &ctx->adj_ly, &ctx->adj_lvx, &ctx->adj_lvy, &ctx->adj_lm, &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm, &ctx->adj_lax, &ctx->adj_lay, &ctx->adj_lf, &ctx->adj_dL, &ctx->adj_dM, &ctx->adj_dMleaf, &ctx->adj_lam32, &ctx->ckpt, &ctx->seg, &ctx->ids, &ctx->perm, &ctx->roll_perms};
     for (DevBuf *b : bufs) free_buf(*b);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -160,6 +160,58 @@ int gx_set_params(gx_ctx *ctx, uint32_t p, double eps) {
 // Copies the given host arrays to the resident bodies.  A NULL array is zeroed when
 // zero_missing is set; otherwise its resident contents are kept (zeroed only if the
 // buffer had to be allocated).
+}  // extern "C"
+
+namespace {
+__global__ void k_iota_i32(int64_t n, int32_t *v) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (int32_t)i;
+}
+__global__ void k_gather_i32(int64_t n, const uint32_t *perm, const int32_t *in, int32_t *out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[perm[i]];
+}
+}  // namespace
+
+// Device Tree::build over the resident bodies with the last build's parameters.
+int gx_rebuild_internal(gx_ctx *ctx) {
+    if (ctx->build_n_max <= 0) return gx_fail(ctx, GX_ERR_STATE, "no tree parameters: build a tree first");
+    const int64_t n = ctx->n_bodies;
+    ctx->have_tree = false;
+    ctx->plan_ref_valid = ctx->plan_acc_valid = ctx->aux_valid = ctx->ref_lists_valid = false;
+    if (ctx->ids.bytes < sizeof(int32_t) * (size_t)(n > 0 ? n : 1)) GX_TRY(gx_ids_reset(ctx));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
+    if ((ctx->build_flags & GX_BUILD_BALANCED) && n > 0) {
+        GX_TRY(gx_tree_balance(ctx, ctx->build_n_max, ctx->build_bounds));
+    } else {
+        GX_TRY(gx_tree_build_device(ctx, n, ctx->build_n_max, ctx->build_bounds, 0));
+        if (n > 0) {  // ids follow the bodies
+            GX_TRY(gx_ensure(ctx, ctx->scratch_g, sizeof(int32_t) * (size_t)n));
+            k_gather_i32<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(n, dptr<uint32_t>(ctx->perm),
+                                                                    dptr<int32_t>(ctx->ids), dptr<int32_t>(ctx->scratch_g));
+            std::swap(ctx->ids.p, ctx->scratch_g.p);
+            std::swap(ctx->ids.bytes, ctx->scratch_g.bytes);
+            ctx->launches++;
+        }
+    }
+    if (ctx->cfg.max_nodes && (uint64_t)ctx->n_nodes > ctx->cfg.max_nodes)
+        return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "tree node count exceeds max_nodes");
+    ctx->max_leaf = std::min<int64_t>(ctx->build_n_max, n);
+    ctx->have_tree = true;
+    GX_CUDA(ctx, cudaGetLastError());
+    return GX_OK;
+}
+
+int gx_ids_reset(gx_ctx *ctx) {
+    int64_t n = ctx->n_bodies;
+    GX_TRY(gx_ensure(ctx, ctx->ids, sizeof(int32_t) * (size_t)(n > 0 ? n : 1)));
+    if (n > 0) k_iota_i32<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(n, dptr<int32_t>(ctx->ids));
+    GX_CUDA(ctx, cudaGetLastError());
+    return GX_OK;
+}
+
+extern "C" {
+
 static int upload_bodies_impl(gx_ctx *ctx, int64_t n, const double *x, const double *y, const double *vx,
                               const double *vy, const double *m, const double *ax, const double *ay,
                               bool zero_missing = true) {
@@ -191,6 +243,7 @@ int gx_upload_bodies(gx_ctx *ctx, int64_t n, const double *x, const double *y, c
     if (ctx->have_tree && n != ctx->n_bodies) return gx_fail(ctx, GX_ERR_INVALID_ARG, "n differs from the tree's body count");
     GX_TRY(upload_bodies_impl(ctx, n, x, y, vx, vy, m, ax, ay));
     ctx->n_bodies = n;
+    GX_TRY(gx_ids_reset(ctx));
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return GX_OK;
 }
@@ -217,6 +270,9 @@ int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, doub
     ctx->plan_ref_valid = ctx->plan_acc_valid = ctx->aux_valid = ctx->roll_valid = false;
     GX_TRY(upload_bodies_impl(ctx, n, x, y, vx, vy, m, ax, ay));
     ctx->n_bodies = n;
+    ctx->build_n_max = n_max;
+    for (int k = 0; k < 4; k++) ctx->build_bounds[k] = bounds[k];
+    ctx->build_flags = flags;
     GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
     if (flags & GX_BUILD_BALANCED) {
         if (n == 0) {
@@ -233,6 +289,7 @@ int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, doub
     ctx->max_leaf = std::min<int64_t>(n_max, n);
     // Tree::build permutes the caller's arrays (lib.rs:204); so do we.
     if (!(flags & GX_BUILD_BALANCED)) GX_TRY(gx_download_bodies(ctx, x, y, vx, vy, m, ax, ay));
+    GX_TRY(gx_ids_reset(ctx));  // the caller's arrays are now in tree order
     ctx->have_tree = true;
     return GX_OK;
 }
@@ -307,7 +364,46 @@ int gx_upload_tree(gx_ctx *ctx, int64_t n_nodes, int64_t n_bodies, const double 
     ctx->n_bodies = n_bodies;
     ctx->max_leaf = 0;
     for (int64_t i = 0; i < nl; i++) ctx->max_leaf = std::max(ctx->max_leaf, body_end[i] - body_start[i]);
+    ctx->ref_lists_valid = true;  // the caller's lists
     ctx->have_tree = true;
+    return GX_OK;
+}
+
+int gx_rebuild_resident(gx_ctx *ctx, int64_t n_max, const double bounds[4], int flags, int64_t *perm) {
+    GX_TRY(check_ctx(ctx));
+    if (n_max <= 0 || !bounds) return gx_fail(ctx, GX_ERR_INVALID_ARG, "bad n_max or bounds");
+    if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no resident bodies: call gx_upload_bodies first");
+    ctx->build_n_max = n_max;
+    for (int k = 0; k < 4; k++) ctx->build_bounds[k] = bounds[k];
+    ctx->build_flags = flags;
+    ctx->roll_valid = false;
+    GX_TRY(gx_rebuild_internal(ctx));
+    const int64_t n = ctx->n_bodies;
+    if (perm && n > 0) {
+        if (flags & GX_BUILD_BALANCED) {
+            for (int64_t i = 0; i < n; i++) perm[i] = i;  // build_constrained does not reorder
+        } else {
+            std::vector<uint32_t> p32((size_t)n);
+            GX_CUDA(ctx, cudaMemcpyAsync(p32.data(), ctx->perm.p, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+            GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            for (int64_t i = 0; i < n; i++) perm[i] = p32[(size_t)i];
+        }
+    }
+    return GX_OK;
+}
+
+int gx_body_ids(gx_ctx *ctx, int64_t *ids) {
+    GX_TRY(check_ctx(ctx));
+    if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no resident bodies");
+    if (!ids) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null array");
+    const int64_t n = ctx->n_bodies;
+    if (n == 0) return GX_OK;
+    if (ctx->ids.bytes < sizeof(int32_t) * (size_t)n) GX_TRY(gx_ids_reset(ctx));
+    std::vector<int32_t> v((size_t)n);
+    GX_CUDA(ctx, cudaMemcpyAsync(v.data(), ctx->ids.p, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t i = 0; i < n; i++) ids[i] = v[(size_t)i];
     return GX_OK;
 }
 
@@ -352,6 +448,7 @@ int gx_export_lists(gx_ctx *ctx, int which, uint32_t *data, uint8_t *lengths) {
     GX_TRY(check_ctx(ctx));
     if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree");
     if (which != GX_LIST_V && which != GX_LIST_U) return gx_fail(ctx, GX_ERR_INVALID_ARG, "unknown list");
+    if (!ctx->ref_lists_valid) GX_TRY(gx_lists_build_ref(ctx));
     DevBuf &d = which == GX_LIST_V ? ctx->vdata : ctx->udata;
     DevBuf &l = which == GX_LIST_V ? ctx->vlen : ctx->ulen;
     size_t nn = (size_t)ctx->n_nodes;
@@ -372,6 +469,10 @@ static int ensure_plan(gx_ctx *ctx) {
             GX_TRY(gx_plan_items(ctx, true));
         }
     } else {
+        if (!ctx->ref_lists_valid) {
+            GX_TRY(gx_lists_build_ref(ctx));
+            ctx->plan_ref_valid = false;
+        }
         if (!ctx->plan_ref_valid || ctx->plan_p != ctx->p || ctx->plan_eps != ctx->eps) {
             GX_TRY(gx_plan_ref(ctx));
             GX_TRY(gx_plan_items(ctx, false));
@@ -380,7 +481,9 @@ static int ensure_plan(gx_ctx *ctx) {
     return GX_OK;
 }
 
+}  // extern "C"
 int gx_ensure_plan_public(gx_ctx *ctx) { return ensure_plan(ctx); }
+extern "C" {
 
 int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64_t *n_p2p_interactions) {
     GX_TRY(check_ctx(ctx));
@@ -471,11 +574,18 @@ int gx_forces_resident(gx_ctx *ctx) {
 }
 
 int gx_kdk_run(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag) {
+    return gx_kdk_run_rebuild(ctx, n_steps, dt, energy_every, 0, diag, n_diag);
+}
+
+int gx_kdk_run_rebuild(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, int64_t rebuild_every,
+                       double *diag, int64_t *n_diag) {
     GX_TRY(check_ctx(ctx));
-    if (n_steps < 0) return gx_fail(ctx, GX_ERR_INVALID_ARG, "n_steps < 0");
+    if (n_steps < 0 || rebuild_every < 0) return gx_fail(ctx, GX_ERR_INVALID_ARG, "n_steps < 0 or rebuild_every < 0");
+    if (rebuild_every > 0 && ctx->build_n_max <= 0)
+        return gx_fail(ctx, GX_ERR_STATE, "rebuilds need the parameters of a device tree build");
     GX_TRY(ensure_plan(ctx));
     GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
-    GX_TRY(gx_kdk_device(ctx, n_steps, dt, energy_every, diag, n_diag));
+    GX_TRY(gx_kdk_device(ctx, n_steps, dt, energy_every, diag, n_diag, rebuild_every));
     return GX_OK;
 }
 

@@ -38,6 +38,8 @@ struct GxTables {
     float ifp_f[17][17];
     double inv[34];  // 1/n
     float inv_f[34];
+    double ff[33][33];  // k! l! (derivative scale, k + l <= 32)
+    float ff_f[33][33];
 };
 __host__ __device__ constexpr GxTables gx_make_tables() {
     GxTables t{};
@@ -53,6 +55,11 @@ __host__ __device__ constexpr GxTables gx_make_tables() {
         for (int j = 0; j < 17; j++) {
             t.ifp[i][j] = t.invfact[i] * t.invfact[j];
             t.ifp_f[i][j] = (float)t.ifp[i][j];
+        }
+    for (int i = 0; i < 33; i++)
+        for (int j = 0; j < 33; j++) {
+            t.ff[i][j] = i + j <= 32 ? t.fact[i] * t.fact[j] : 0.0;
+            t.ff_f[i][j] = (float)t.ff[i][j];
         }
     t.inv[0] = 0.0;
     t.inv_f[0] = 0.f;
@@ -73,6 +80,9 @@ template <> __device__ __forceinline__ float tab_binom<float>(int n, int k) { re
 template <class T> __device__ __forceinline__ T tab_ifp(int i, int j);
 template <> __device__ __forceinline__ double tab_ifp<double>(int i, int j) { return c_tab.ifp[i][j]; }
 template <> __device__ __forceinline__ float tab_ifp<float>(int i, int j) { return c_tab.ifp_f[i][j]; }
+template <class T> __device__ __forceinline__ T tab_ff(int k, int l);
+template <> __device__ __forceinline__ double tab_ff<double>(int k, int l) { return c_tab.ff[k][l]; }
+template <> __device__ __forceinline__ float tab_ff<float>(int k, int l) { return c_tab.ff_f[k][l]; }
 template <class T> __device__ __forceinline__ T tab_inv(int n);
 template <> __device__ __forceinline__ double tab_inv<double>(int n) { return c_tab.inv[n]; }
 template <> __device__ __forceinline__ float tab_inv<float>(int n) { return c_tab.inv_f[n]; }
@@ -286,29 +296,49 @@ __global__ void k_scrub(int64_t n, T *v) {
 // ---------------------------------------------------------------- M2L
 // Derivatives of 1/R (R^2 = dx^2+dy^2+eps^2) scaled by k! l!:  A[k,l] = k! l! a_kl with
 // |k| R^2 a_k = -(2|k|-1)(dx a_{k-ex} + dy a_{k-ey}) - (|k|-1)(a_{k-2ex} + a_{k-2ey}), a_0 = 1/R.
+// The recurrence runs on the unscaled a (no per-term index multipliers: two
+// coefficients per order) and each term is scaled once by k! l!.
 // The kernel of the reference is G = -1/R, so G^(k,l) = -A[k,l].
+// One far pair, derivatives and contraction fused:  out[X] += sum_Y in[Y] A[X+Y]
+// (|X|, |Y| <= p) with A the scaled derivatives at (dx, dy).  Each A[U] is used by
+// every (X, Y) with X + Y = U the moment it is formed, so no derivative array is kept:
+// only the unscaled values of the last two orders feed the recurrence.  The forward
+// M2L takes in = signed moments (-1)^|S| M[S], out = the local accumulator; the
+// adjoint M2L^T takes in = dL[T]/T!, out = the moment cotangent accumulator.
 template <int P, class T>
-__device__ __forceinline__ void derivs_scaled(T dx, T dy, T eps2, T *A) {
+__device__ __forceinline__ void m2l_fused(T dx, T dy, T eps2, const T *in, T *out) {
     const int PP = gx_rt_order(P);
     const int Q = 2 * PP;
-    const int NCr = (PP + 1) * (PP + 2) / 2;
-    (void)NCr;
+    T a[nc2(2 * P)];
     T r2 = dx * dx + dy * dy + eps2;
     T ir = rsqrt_t<T>(r2);
     T ir2 = ir * ir;
-    A[0] = ir;
+    a[0] = ir;
+    out[0] += in[0] * ir;
 #pragma unroll
     for (int n = 1; n <= Q; n++) {
+        const T in_ = tab_inv<T>(n) * ir2;
+        const T c1 = -(T)(2 * n - 1) * in_, c2 = -(T)(n - 1) * in_;
 #pragma unroll
         for (int k = 0; k <= n; k++) {
-            int l = n - k;
-            T s1 = T(0), s2 = T(0);
-            // a_{k-1,l} = A[k-1,l]/((k-1)! l!)  ->  in A units: A[k,l] = k!l! a_kl
-            if (k >= 1) s1 += dx * A[gx_mi(k - 1, l)] * (T)k;
-            if (l >= 1) s1 += dy * A[gx_mi(k, l - 1)] * (T)l;
-            if (k >= 2) s2 += A[gx_mi(k - 2, l)] * (T)(k * (k - 1));
-            if (l >= 2) s2 += A[gx_mi(k, l - 2)] * (T)(l * (l - 1));
-            A[gx_mi(k, l)] = (-(T)(2 * n - 1) * s1 - (T)(n - 1) * s2) * ir2 * tab_inv<T>(n);
+            const int l = n - k;
+            T s1, s2 = T(0);
+            if (k >= 1 && l >= 1) s1 = dx * a[gx_mi(k - 1, l)] + dy * a[gx_mi(k, l - 1)];
+            else if (k >= 1) s1 = dx * a[gx_mi(k - 1, l)];
+            else s1 = dy * a[gx_mi(k, l - 1)];
+            if (k >= 2) s2 += a[gx_mi(k - 2, l)];
+            if (l >= 2) s2 += a[gx_mi(k, l - 2)];
+            const T v = n >= 2 ? c1 * s1 + c2 * s2 : c1 * s1;
+            a[gx_mi(k, l)] = v;
+            const T Av = n >= 2 ? v * tab_ff<T>(k, l) : v;
+            // all splits (k, l) = X + Y with |X| <= p, |Y| <= p
+#pragma unroll
+            for (int yi = (k > PP ? k - PP : 0); yi <= (k < PP ? k : PP); yi++)
+#pragma unroll
+                for (int yj = (l > PP ? l - PP : 0); yj <= (l < PP ? l : PP); yj++) {
+                    const int xi = k - yi, xj = l - yj;
+                    if (yi + yj <= PP && xi + xj <= PP) out[gx_mi(xi, xj)] += in[gx_mi(yi, yj)] * Av;
+                }
         }
     }
 }
@@ -375,7 +405,6 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l
     const int PP = gx_rt_order(P);
     const int NCr = (PP + 1) * (PP + 2) / 2;
     (void)NCr;
-    constexpr int ND = nc2(2 * P);
     int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
     if (node >= nn) return;
@@ -407,18 +436,12 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l
             dx = (T)(tcx - comx[src]);
             dy = (T)(tcy - comy[src]);
         }
-        T A[ND];
-        derivs_scaled<P, T>(dx, dy, eps2, A);
 #pragma unroll
         for (int i = 0; i <= PP; i++)
 #pragma unroll
-            for (int j = 0; j <= PP - i; j++) {
-                T sm = ((i + j) & 1) ? -ms[gx_mi(i, j)] : ms[gx_mi(i, j)];
-#pragma unroll
-                for (int oi = 0; oi <= PP; oi++)
-#pragma unroll
-                    for (int oj = 0; oj <= PP - oi; oj++) acc[gx_mi(oi, oj)] += sm * A[gx_mi(i + oi, j + oj)];
-            }
+            for (int j = 0; j <= PP - i; j++)
+                if ((i + j) & 1) ms[gx_mi(i, j)] = -ms[gx_mi(i, j)];
+        m2l_fused<P, T>(dx, dy, eps2, ms, acc);
         src = nsrc;
     }
     // G = -A: L[T] = -(1/T!) sum_S M'[S] A[S+T]

@@ -73,8 +73,18 @@ struct gx_ctx {
     DevBuf x, y, vx, vy, m, ax, ay;
     bool have_bodies = false;
 
-    // REF lists, reference layout
+    // REF lists, reference layout (built with the tree by gx_build_tree, lazily after
+    // gx_rebuild_resident)
     DevBuf vdata, vlen, udata, ulen;
+    bool ref_lists_valid = false;
+    DevBuf perm;  // uint32: pre-sort index of each body after the last device sort
+    // parameters of the last tree build (reused by device rebuilds)
+    int64_t build_n_max = 0;
+    double build_bounds[4] = {0, 0, 0, 0};
+    int build_flags = 0;
+    // int32: for each resident body, its index in the order of the last upload (or
+    // build_tree); device rebuilds permute it with the bodies
+    DevBuf ids;
 
     // plans (static per tree, mode, p, eps)
     bool plan_ref_valid = false, plan_acc_valid = false;
@@ -114,6 +124,8 @@ struct gx_ctx {
     int64_t roll_steps = 0, roll_k = 1;
     double roll_dt = 0.0;
     int roll_prec = GX_PREC_FP64;
+    int64_t roll_rebuild = 0;
+    DevBuf roll_perms;  // uint32 [T+1][n]: the permutation of every rebuild of a rollout
     bool roll_valid = false;
 
     // scratch
@@ -140,6 +152,11 @@ int gx_plan_items(gx_ctx *ctx, bool accurate);
 int gx_plan_tree_aux(gx_ctx *ctx);
 // gx_fmm.cu
 int gx_forces_device(gx_ctx *ctx, bool timed);
+// gx_api.cu: device rebuild with the last build's parameters (permutes the resident
+// bodies and ids; invalidates the plans), plan check, ids reset
+int gx_rebuild_internal(gx_ctx *ctx);
+int gx_ensure_plan_public(gx_ctx *ctx);
+int gx_ids_reset(gx_ctx *ctx);
 int gx_poly_table_host(int p, double eps, std::vector<double> &out);
 // gx_scan.cu
 int gx_exclusive_scan_i64(gx_ctx *ctx, const int64_t *in, int64_t *out, int64_t n);
@@ -147,7 +164,8 @@ int gx_exclusive_scan_i32(gx_ctx *ctx, const int32_t *in, int32_t *out, int64_t 
 int gx_radix_sort_u64(gx_ctx *ctx, uint64_t *keys, uint32_t *vals, int64_t n, int begin_bit, int end_bit,
                       uint64_t *keys_alt, uint32_t *vals_alt, bool *result_in_alt);
 // gx_kdk.cu
-int gx_kdk_device(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag);
+int gx_kdk_device(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag,
+                  int64_t rebuild_every = 0);
 int gx_diag_device(gx_ctx *ctx, double out[5]);
 int gx_n2_device(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, double *ay);
 

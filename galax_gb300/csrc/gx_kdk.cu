@@ -121,7 +121,8 @@ int gx_diag_device(gx_ctx *ctx, double out[5]) {
     return GX_OK;
 }
 
-int gx_kdk_device(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag) {
+int gx_kdk_device(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag,
+                  int64_t rebuild_every) {
     int64_t n = ctx->n_bodies, nd = 0;
     double h = 0.5 * dt;
     for (int64_t step = 0; step < n_steps; step++) {
@@ -129,6 +130,11 @@ int gx_kdk_device(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every,
                                                                  dptr<double>(ctx->vx), dptr<double>(ctx->vy),
                                                                  dptr<double>(ctx->ax), dptr<double>(ctx->ay));
         ctx->launches++;
+        if (rebuild_every > 0 && (step + 1) % rebuild_every == 0) {
+            // the tree of the drifted positions (the bodies, ids and accelerations are permuted with it)
+            GX_TRY(gx_rebuild_internal(ctx));
+            GX_TRY(gx_ensure_plan_public(ctx));
+        }
         GX_TRY(gx_forces_device(ctx, false));
         k_kick<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(n, h, dptr<double>(ctx->vx), dptr<double>(ctx->vy),
                                                            dptr<double>(ctx->ax), dptr<double>(ctx->ay));

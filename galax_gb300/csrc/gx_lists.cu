@@ -662,6 +662,7 @@ int gx_lists_build_ref(gx_ctx *ctx) {
         ctx->launches++;
         GX_CUDA(ctx, cudaGetLastError());
     }
+    ctx->ref_lists_valid = true;
     return check_status(ctx);
 }
 

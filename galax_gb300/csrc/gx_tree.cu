@@ -254,7 +254,7 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
 // Morton order on the device, then builds the node hierarchy.
 int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bounds[4], int flags) {
     ctx->have_tree = false;
-    ctx->plan_ref_valid = ctx->plan_acc_valid = false;
+    ctx->plan_ref_valid = ctx->plan_acc_valid = ctx->ref_lists_valid = false;
     if (n <= 0) {
         ctx->n_nodes = ctx->n_leaves = 0;
         ctx->n_levels = 0;
@@ -289,6 +289,8 @@ int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bou
             std::swap(a->p, ctx->scratch_d.p);
             std::swap(a->bytes, ctx->scratch_d.bytes);
         }
+        GX_TRY(gx_ensure(ctx, ctx->perm, sizeof(uint32_t) * n));
+        GX_CUDA(ctx, cudaMemcpyAsync(ctx->perm.p, idx, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
         GX_CUDA(ctx, cudaGetLastError());
     }
     int64_t nl = (n + n_max - 1) / n_max;

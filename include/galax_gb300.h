@@ -104,6 +104,14 @@ int gx_upload_tree(gx_ctx *ctx, int64_t n_nodes, int64_t n_bodies, const double 
 int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, double *vy, double *m,
                   double *ax, double *ay, int64_t n_max, const double bounds[4], int flags);
 /* Tree shape of the current tree. */
+/* Tree::build (galax-core/src/lib.rs:163-361) over the RESIDENT bodies: Morton keys,
+ * device radix sort, permutation of the seven resident arrays, leaves and parents, with
+ * no host round trip -- for a run that rebuilds the tree every step instead of keeping
+ * it static as the reference's CLI does (galax-cli/src/main.rs:159).  perm (optional,
+ * host, n_bodies entries) receives for every body its index before the rebuild.  The
+ * plans (and, in REF mode, the V/U lists) are rebuilt by the next evaluation.
+ * GX_BUILD_BALANCED runs build_constrained (lib.rs:541-694), which does not reorder. */
+int gx_rebuild_resident(gx_ctx *ctx, int64_t n_max, const double bounds[4], int flags, int64_t *perm);
 int gx_tree_info(gx_ctx *ctx, int64_t *n_nodes, int64_t *n_leaves, int32_t *n_levels, int64_t *n_bodies);
 /* Copies the current tree to host arrays (any pointer may be NULL); the Tree the
  * CLI keeps on the host.  level_start has n_levels+1 entries. */
@@ -132,6 +140,16 @@ int gx_forces_resident(gx_ctx *ctx);
  * steps a row {step, KE, FMM PE, px, py, Lz} is written to diag (6 doubles per row).
  * *n_diag receives the row count. */
 int gx_kdk_run(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, double *diag, int64_t *n_diag);
+/* gx_kdk_run with a rebuild policy (the reference keeps the tree static): every
+ * rebuild_every steps (0 = never) the tree is rebuilt on the device from the drifted
+ * positions, with the parameters of the last gx_build_tree / gx_rebuild_resident,
+ * before that step's force evaluation.  Rebuilds reorder the resident bodies;
+ * gx_body_ids gives the mapping. */
+int gx_kdk_run_rebuild(gx_ctx *ctx, int64_t n_steps, double dt, int64_t energy_every, int64_t rebuild_every,
+                       double *diag, int64_t *n_diag);
+/* For every resident body, its index in the order of the last gx_upload_bodies or
+ * gx_build_tree (device rebuilds reorder the bodies; this undoes it).  ids: n_bodies. */
+int gx_body_ids(gx_ctx *ctx, int64_t *ids);
 /* Diagnostics of the resident bodies (lib.rs:1638-1683): {KE, FMM PE, px, py, Lz}. */
 int gx_diagnostics(gx_ctx *ctx, double out[5]);
 /* GpuContext::n2_debug (galax-gpu/src/lib.rs:670-714) restricted to sampled
@@ -165,9 +183,14 @@ int gx_n2_sampled_static(const double *x, const double *y, const double *m, int6
  * M2L^T, M2M^T, P2M^T, Hessian-vector P2P), computed in FP64.  p in {1..6, 8}. */
 int gx_force_vjp(gx_ctx *ctx, const double *lam_x, const double *lam_y, double *gx, double *gy, double *gm);
 /* Leapfrog rollout from the resident state (simulate, galax-integrate/src/lib.rs:204-237)
- * keeping (x, y, vx, vy) every checkpoint_every steps; the resident state ends at
- * step n_steps. */
-int gx_rollout_forward(gx_ctx *ctx, int64_t n_steps, double dt, int64_t checkpoint_every);
+ * keeping a checkpoint (positions, velocities, accelerations, masses and the leaf
+ * locals of that step) every checkpoint_every steps; the resident state ends at step
+ * n_steps.  rebuild_every = 0 keeps the tree static (the reference's CLI); 1 rebuilds
+ * it on the device from the drifted positions before every step's force evaluation
+ * (bodies are reordered: gx_body_ids, read right after this call, maps the final
+ * order to the order at the start). */
+int gx_rollout_forward(gx_ctx *ctx, int64_t n_steps, double dt, int64_t checkpoint_every,
+                       int64_t rebuild_every);
 /* Reverse leapfrog of the last gx_rollout_forward: given dL/d(x, y, vx, vy) at the
  * final step, returns dL/d(x, y, vx, vy) at step 0 and dL/dm.  Segments between
  * checkpoints are recomputed (deterministically, so bit for bit); *peak_bytes (may be

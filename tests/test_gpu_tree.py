@@ -116,3 +116,65 @@ def test_empty(G):
     ctx.build_tree(Bodies.new(0), 32, (0.0, 1.0, 0.0, 1.0))
     assert ctx.tree_info()[0] == 0
     ctx.close()
+
+
+@pytest.mark.parametrize("preset,n", [("plummer", 30_000), ("uniform", 7_001)])
+def test_resident_rebuild_matches_host_build(G, oracle, preset, n):
+    """gx_rebuild_resident: the same Morton order, tree and (lazily built) REF lists as
+    Tree::build over the same bodies, and a permutation that maps the old order to the new."""
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=21)
+    bounds = presets.BOUNDS[preset]
+    ctx = _ctx(G, n)
+    ctx.upload_bodies(b)
+    perm = ctx.rebuild_resident(32, bounds, want_perm=True)
+    out = G.Bodies.new(n)
+    ctx.download_bodies(out)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass, b.vx, b.vy)
+    t = oracle.tree_build(ob, 32, bounds)
+    for name in ("x", "y", "vx", "vy", "mass"):
+        assert np.array_equal(getattr(out, name), getattr(ob, name)), name
+        assert np.array_equal(getattr(out, name), getattr(b, name)[perm]), name
+    dt = ctx.export_tree()
+    for f in FIELDS:
+        assert np.array_equal(getattr(dt, f), getattr(t, f)), f
+    v = oracle.vlist_build(t)
+    vd, vl = ctx.export_lists(G.LIST_V)
+    assert np.array_equal(vl, v.lengths) and np.array_equal(vd, v.data)
+    ctx.close()
+
+
+def test_rebuild_after_steps_sorts_the_moved_bodies(G, oracle):
+    """Steps on a static tree, then a resident rebuild: the bodies come out in the
+    Morton order of their new positions; the ACCURATE forces of the rebuilt tree match
+    those of a fresh host build of the same bodies bit for bit."""
+    from galax_gb300 import presets
+    n = 20_001
+    b = presets.galaxy(n, seed=22)
+    bounds = presets.BOUNDS["galaxy"]
+    ctx = _ctx(G, n)
+    ctx.build_tree(b, 32, bounds)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    ctx.upload_bodies(b)
+    ctx.forces_resident()
+    ctx.kdk_run(5, 1e-2, 0)
+    moved = G.Bodies.new(n)
+    ctx.download_bodies(moved)
+    ctx.rebuild_resident(32, bounds)
+    ctx.forces_resident()
+    out = G.Bodies.new(n)
+    ctx.download_bodies(out)
+    ob = oracle.Bodies.from_arrays(moved.x, moved.y, moved.mass, moved.vx, moved.vy)
+    oracle.tree_build(ob, 32, bounds)
+    assert np.array_equal(out.x, ob.x) and np.array_equal(out.y, ob.y)
+    c2 = _ctx(G, n)
+    fresh = moved.copy()
+    c2.build_tree(fresh, 32, bounds)
+    c2.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    c2.upload_bodies(fresh)
+    c2.forces_resident()
+    ref = G.Bodies.new(n)
+    c2.download_bodies(ref)
+    c2.close()
+    ctx.close()
+    assert np.array_equal(out.ax, ref.ax) and np.array_equal(out.ay, ref.ay)
