@@ -174,19 +174,6 @@ def _rot(theta):
     return np.array([[c, -s], [s, c]])
 
 
-def _rollout_loss(x0, y0, xT, yT, R, ids=None):
-    """L = sum_i |x_T[i] - R x_0[ids[i]]|^2 (ids: the starting index of each final body,
-    identity without rebuilds), its cotangent dL/dx_T and the direct term dL/dx_0."""
-    ids = np.arange(x0.size) if ids is None else ids
-    tx = R[0, 0] * x0[ids] + R[0, 1] * y0[ids]
-    ty = R[1, 0] * x0[ids] + R[1, 1] * y0[ids]
-    rx, ry = xT - tx, yT - ty
-    d0x, d0y = np.zeros(x0.size), np.zeros(x0.size)
-    d0x[ids] = -2 * (R[0, 0] * rx + R[1, 0] * ry)
-    d0y[ids] = -2 * (R[0, 1] * rx + R[1, 1] * ry)
-    return float(np.sum(rx * rx + ry * ry)), 2 * rx, 2 * ry, d0x, d0y
-
-
 def _adjoint_run(G, ctx, b, T, dt, k, R, rebuild=0):
     """One forward rollout and its reverse pass; returns times, gradients and peak bytes."""
     n = len(b)
@@ -197,24 +184,13 @@ def _adjoint_run(G, ctx, b, T, dt, k, R, rebuild=0):
     fin = G.Bodies.new(n)
     ctx.download_bodies(fin)
     ids = ctx.body_ids() if rebuild else None
-    L, lxT, lyT, dx0, dy0 = _rollout_loss(b.x, b.y, fin.x, fin.y, R, ids)
+    from galax_gb300.fdcheck import rollout_loss
+    L, lxT, lyT, dx0, dy0 = rollout_loss(b.x, b.y, fin.x, fin.y, R, ids)
     z = np.zeros(n)
     t0 = time.perf_counter()
     gx, gy, gvx, gvy, gm, peak = ctx.rollout_backward(lxT, lyT, z, z)
     t_bwd = time.perf_counter() - t0
     return t_fwd, t_bwd, (gx + dx0, gy + dy0, gvx, gvy, gm), peak, L
-
-
-def _loss_only(G, ctx, b, T, dt, R, rebuild=0, bounds=None):
-    n = len(b)
-    ctx.upload_bodies(b)
-    if rebuild:  # as the rollout does: the tree of the starting positions first
-        ctx.rebuild_resident(N_MAX, bounds)
-    ctx.forces_resident()
-    ctx.kdk_run(T, dt, 0, rebuild_every=rebuild)
-    fin = G.Bodies.new(n)
-    ctx.download_bodies(fin)
-    return _rollout_loss(b.x, b.y, fin.x, fin.y, R, ctx.body_ids() if rebuild else None)[0]
 
 
 def _grad_rel(g, r):
@@ -258,43 +234,43 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
         gal[name] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak,
                      "steps_per_s_forward": T / tf}
     gal["mixed"]["grad_rel_err_vs_fp64"] = _grad_rel(grads["mixed"], grads["fp64"])
-    # central finite differences of the FP64 rollout, h = 1e-6, seeded directions
+    # central finite differences of the FP64 rollout, h = 1e-6, seeded directions, with
+    # every step's tree taken from the unperturbed trajectory (the function the adjoint
+    # differentiates; a perturbation of 1e-6 reorders bodies across Morton cells)
+    from galax_gb300 import fdcheck
     cg.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
     rng = np.random.default_rng(args.seed + 6)
-    fd = []
     h = 1e-6
-    for _ in range(args.fd_dirs):
-        d = [rng.standard_normal(n) for _ in range(4)] + [rng.standard_normal(n) * bg.mass]
-        def L_at(sg):
-            pb = G.Bodies.from_arrays(bg.x + sg * h * d[0], bg.y + sg * h * d[1], bg.mass + sg * h * d[4],
-                                      bg.vx + sg * h * d[2], bg.vy + sg * h * d[3])
-            return _loss_only(G, cg, pb, T, dt, R, rebuild=1, bounds=bounds)
-        num = (L_at(1) - L_at(-1)) / (2 * h)
-        g = grads["fp64"]
-        an = sum(float(np.dot(g[q], d[q])) for q in range(5))
-        fd.append(abs(num - an) / abs(num))
+    dirs = [[rng.standard_normal(n) for _ in range(4)] + [rng.standard_normal(n) * bg.mass]
+            for _ in range(args.fd_dirs)]
+    num = fdcheck.fd_frozen_trees(G, cg, bg, T, dt, R, dirs, h, N_MAX, bounds, rebuild=True) if dirs else []
+    g = grads["fp64"]
+    fd = [abs(num[i] - sum(float(np.dot(g[q], dirs[i][q])) for q in range(5))) / abs(num[i]) for i in range(len(dirs))]
     gal["fp64"]["fd_rel_err_max"] = float(max(fd)) if fd else None
     gal["fp64"]["fd_directions"] = args.fd_dirs
     cg.close()
     out["galaxy_200k"] = gal
 
-    # ---- Plummer 1M, 500 steps at dt = 1e-3, mixed, checkpoint sweep
+    # ---- Plummer 1M, 500 steps at dt = 1e-3, mixed, checkpoint sweep.  Core bodies
+    # cross ~80 leaf widths in 500 steps; with a static tree the run diverges, so the
+    # tree is rebuilt before every step's force evaluation here too.
     T, dt = args.adj_steps, 1e-3
     Rp = _rot(float(np.random.default_rng(args.seed + 8).uniform(0, 2 * np.pi)))
     ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
     sweep = {}
     for k in args.adj_k:
-        _adjoint_run(G, ctx1m, b1m, 3, dt, k, Rp)  # warm-up (allocations)
-        tf, tb, g, peak, L = _adjoint_run(G, ctx1m, b1m, T, dt, k, Rp)
+        _adjoint_run(G, ctx1m, b1m, 3, dt, k, Rp, rebuild=1)  # warm-up (allocations)
+        tf, tb, g, peak, L = _adjoint_run(G, ctx1m, b1m, T, dt, k, Rp, rebuild=1)
         sweep[str(k)] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak,
                          "finite": bool(all(np.all(np.isfinite(a)) for a in g)) and bool(np.isfinite(L))}
     # gradient of a 20-step prefix: mixed against FP64 (the FP64 form is ~50x slower)
     Tp = 20
-    _, _, gm20, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp)
+    _, _, gm20, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp, rebuild=1)
     ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
-    _, _, g64, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp)
+    _, _, g64, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp, rebuild=1)
     ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
-    out["plummer_1m"] = {"workload": f"plummer N={len(b1m)}, p={P}, n_max={N_MAX}, {T} steps, dt={dt}, mixed",
+    out["plummer_1m"] = {"workload": f"plummer N={len(b1m)}, p={P}, n_max={N_MAX}, {T} steps, dt={dt}, mixed, "
+                                     f"tree rebuilt every step",
                          "checkpoint_sweep": sweep,
                          "grad_rel_err_mixed_vs_fp64_20_steps": _grad_rel(gm20, g64)}
     return out
@@ -422,7 +398,7 @@ def run_ours(args, rank, world, local, pg):
                 "d2h_bytes_per_step": 2 * 8 * n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32 if peak32 else None, "traffic": None,
-                     "kernel": "k_l2p_p2p32 (fused L2P + P2P)",
+                     "kernel": "k_p2p32_items (P2P, packed FP32)",
                      "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)"},
         "gpu_launches": int(sum(r["launches"] * (r["steps"] + 1) for r in res.values())),
         "clocks": clocks,

@@ -909,6 +909,28 @@ int run_forces(gx_ctx *ctx, bool timed) {
         k_p2m<P, T><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, M, pos);
         ctx->launches++;
         tm.mark();  // 2
+        // near field on the second stream, beside M2M -> M2L -> L2L on this one: both
+        // are FP32-pipe bound but neither fills it alone (latency, occupancy), and
+        // their blocks share the SMs.  Deterministic: P2P writes per-item partials
+        // that L2P sums in order after the join.
+        const size_t pbytes = (mixed ? sizeof(float2) : sizeof(double2)) * 32 * (size_t)tchunks * (size_t)(I.n + 1);
+        GX_TRY(gx_ensure(ctx, ctx->part, pbytes));
+        GX_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+        GX_CUDA(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+        if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[14], ctx->stream2));
+        if (I.n > 0) {
+            if (mixed)
+                k_p2p32_items<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                            dptr<int32_t>(I.nq), pos, comx, comy, bs, be, src_idx,
+                                                            (float)eps2, tchunks, dptr<float2>(ctx->part));
+            else
+                k_p2p64_items<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                            dptr<int32_t>(I.nq), X, Y, Mb, bs, be, src_idx, eps2,
+                                                            tchunks, dptr<double2>(ctx->part));
+            ctx->launches++;
+        }
+        if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[15], ctx->stream2));
+        GX_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->stream2));
         // M2M, bottom-up by level
         for (int lv = 1; lv < ctx->n_levels; lv++) {
             int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
@@ -955,27 +977,18 @@ int run_forces(gx_ctx *ctx, bool timed) {
             Lleaf = Lf;
         }
         tm.mark();  // 5
-        // P2P work items, then L2P + ordered sum of the partials
+        // join the near field, then L2P + ordered sum of the P2P partials
+        GX_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
         if (mixed) {
-            GX_TRY(gx_ensure(ctx, ctx->part, sizeof(float2) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
-            float2 *part = dptr<float2>(ctx->part);
-            if (I.n > 0)
-                k_p2p32_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
-                                                  pos, comx, comy, bs, be, src_idx, (float)eps2, tchunks, part);
             k_l2p_reduce32<P><<<gw, 128, 0, st>>>(nl, pos, bs, be, reinterpret_cast<const float *>(Lleaf),
-                                                  dptr<int64_t>(I.off), tchunks, part, dptr<double>(ctx->ax),
-                                                  dptr<double>(ctx->ay));
+                                                  dptr<int64_t>(I.off), tchunks, dptr<float2>(ctx->part),
+                                                  dptr<double>(ctx->ax), dptr<double>(ctx->ay));
         } else {
-            GX_TRY(gx_ensure(ctx, ctx->part, sizeof(double2) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
-            double2 *part = dptr<double2>(ctx->part);
-            if (I.n > 0)
-                k_p2p64_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
-                                                  X, Y, Mb, bs, be, src_idx, eps2, tchunks, part);
             k_l2p_reduce64<P><<<gw, 128, 0, st>>>(nl, X, Y, comx, comy, bs, be, reinterpret_cast<const double *>(Lleaf),
-                                                  dptr<int64_t>(I.off), tchunks, part, dptr<double>(ctx->ax),
-                                                  dptr<double>(ctx->ay));
+                                                  dptr<int64_t>(I.off), tchunks, dptr<double2>(ctx->part),
+                                                  dptr<double>(ctx->ax), dptr<double>(ctx->ay));
         }
-        ctx->launches += 2;
+        ctx->launches++;
         tm.mark();  // 6
         return GX_OK;
     };

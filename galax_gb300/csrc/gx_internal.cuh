@@ -58,6 +58,10 @@ struct gx_ctx {
     int prec = GX_PREC_FP64;
     double theta = 0.5;
     cudaStream_t stream = nullptr;
+    // second stream: the near field (P2P) runs beside the far-field chain
+    // (M2M, M2L, L2L) of the same evaluation; forked after P2M, joined before L2P
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
     int sm_count = 0;
 
@@ -137,6 +141,7 @@ struct gx_ctx {
     // timing
     cudaEvent_t ev[16] = {};
     double last_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+    double last_p2p_ms = 0;  // the P2P kernel alone (events on the near-field stream)
     int64_t last_launches = 0;
     int64_t launches = 0;
 };

@@ -416,64 +416,99 @@ __device__ __forceinline__ bool mac_far(const double *comx, const double *comy, 
 }
 
 // Per node x of a level: children of Near(parent(x)) split into far (M2L) and near,
-// in the order (parent's near entry, child slot).  One warp per node: the lanes take
-// 32 consecutive near entries of the parent at a time and place their children with a
-// warp prefix sum, so a node whose parent has a long near list (a wide leaf of the
-// sparse halo can be near every other leaf) costs len/32 rounds, not len.
-__global__ void k_mac(int64_t s, int64_t e, int pass, const int32_t *parent, const int4 *child, const double *comx,
-                      const double *comy, const double *R, double theta, const int64_t *near_start,
-                      const int32_t *near_cnt, const int32_t *near_idx_in, int32_t *fcnt, int32_t *ncnt,
-                      const int64_t *fstart, const int64_t *nstart, int32_t *far_idx, int32_t *near_idx) {
+// in the order (parent's near entry, child slot).  The parent's near list is cut into
+// chunks of MAC_CHUNK entries and every (node, chunk) unit is one warp: the lanes take
+// 32 consecutive entries at a time and place their children with a warp prefix sum.
+// A wide leaf of the sparse halo can be near every other leaf; chunking spreads the
+// nodes below it over many warps instead of one.
+constexpr int MAC_CHUNK = 128;
+
+__global__ void k_mac_nchunks(int64_t s, int64_t e, const int32_t *parent, const int32_t *near_cnt, int64_t *nch) {
+    int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= e) return;
+    int32_t P = parent[x];
+    int64_t cand = P >= 0 ? near_cnt[P] : 0;
+    nch[x - s] = (cand + MAC_CHUNK - 1) / MAC_CHUNK;
+}
+
+__global__ void k_mac_units(int64_t s, int64_t e, const int64_t *uoff, int32_t *unode, int32_t *uchunk) {
+    int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= e) return;
+    int64_t a = uoff[x - s], b = uoff[x - s + 1];
+    for (int64_t u = a; u < b; u++) {
+        unode[u] = (int32_t)x;
+        uchunk[u] = (int32_t)(u - a);
+    }
+}
+
+// pass 0: per-unit counts (ufar, unear); pass 1: write at the per-unit offsets
+__global__ void k_mac(int64_t n_units, int pass, const int32_t *unode, const int32_t *uchunk, const int32_t *parent,
+                      const int4 *child, const double *comx, const double *comy, const double *R, double theta,
+                      const int64_t *near_start, const int32_t *near_cnt, const int32_t *near_idx_in, int64_t *ufar,
+                      int64_t *unear, int32_t *far_idx, int32_t *near_idx) {
     const unsigned full = 0xffffffffu;
     int lane = threadIdx.x & 31;
-    int64_t x = s + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (x >= e) return;  // whole warps leave together
+    int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (u >= n_units) return;  // whole warps leave together
+    int32_t x = unode[u];
     int32_t P = parent[x];
-    int32_t nf = 0, nn = 0;
-    int64_t fb = pass ? fstart[x] : 0, nb = pass ? nstart[x] : 0;
-    if (P >= 0) {
-        int64_t q0 = near_start[P], q1 = q0 + near_cnt[P];
-        for (int64_t qb = q0; qb < q1; qb += 32) {
-            int64_t q = qb + lane;
-            int cc[4] = {-1, -1, -1, -1};
-            unsigned fm = 0, nm = 0;
-            if (q < q1) {
-                int4 c4 = child[near_idx_in[q]];
-                cc[0] = c4.x;
-                cc[1] = c4.y;
-                cc[2] = c4.z;
-                cc[3] = c4.w;
-                for (int k = 0; k < 4; k++) {
-                    if (cc[k] < 0) continue;
-                    if (mac_far(comx, comy, R, x, cc[k], theta)) fm |= 1u << k;
-                    else nm |= 1u << k;
-                }
+    int64_t qa = near_start[P] + (int64_t)uchunk[u] * MAC_CHUNK;
+    int64_t qe = min(near_start[P] + (int64_t)near_cnt[P], qa + MAC_CHUNK);
+    int64_t nf = 0, nn = 0;
+    int64_t fb = pass ? ufar[u] : 0, nb = pass ? unear[u] : 0;
+    for (int64_t qb = qa; qb < qe; qb += 32) {
+        int64_t q = qb + lane;
+        int cc[4] = {-1, -1, -1, -1};
+        unsigned fm = 0, nm = 0;
+        if (q < qe) {
+            int4 c4 = child[near_idx_in[q]];
+            cc[0] = c4.x;
+            cc[1] = c4.y;
+            cc[2] = c4.z;
+            cc[3] = c4.w;
+            for (int k = 0; k < 4; k++) {
+                if (cc[k] < 0) continue;
+                if (mac_far(comx, comy, R, x, cc[k], theta)) fm |= 1u << k;
+                else nm |= 1u << k;
             }
-            int myf = __popc(fm), myn = __popc(nm);
-            int pf = myf, pn = myn;  // inclusive warp scans
-            for (int o = 1; o < 32; o <<= 1) {
-                int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
-                if (lane >= o) {
-                    pf += tf;
-                    pn += tn;
-                }
-            }
-            int tf = __shfl_sync(full, pf, 31), tn = __shfl_sync(full, pn, 31);
-            if (pass) {
-                int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
-                for (int k = 0; k < 4; k++) {
-                    if ((fm >> k) & 1u) far_idx[a++] = cc[k];
-                    if ((nm >> k) & 1u) near_idx[b++] = cc[k];
-                }
-            }
-            nf += tf;
-            nn += tn;
         }
+        int myf = __popc(fm), myn = __popc(nm);
+        int pf = myf, pn = myn;  // inclusive warp scans
+        for (int o = 1; o < 32; o <<= 1) {
+            int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
+            if (lane >= o) {
+                pf += tf;
+                pn += tn;
+            }
+        }
+        int tf = __shfl_sync(full, pf, 31), tn = __shfl_sync(full, pn, 31);
+        if (pass) {
+            int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
+            for (int k = 0; k < 4; k++) {
+                if ((fm >> k) & 1u) far_idx[a++] = cc[k];
+                if ((nm >> k) & 1u) near_idx[b++] = cc[k];
+            }
+        }
+        nf += tf;
+        nn += tn;
     }
     if (!pass && lane == 0) {
-        fcnt[x] = nf;
-        ncnt[x] = nn;
+        ufar[u] = nf;
+        unear[u] = nn;
     }
+}
+
+// per node of the level: start (running total + first unit's offset) and count
+__global__ void k_mac_node_lists(int64_t s, int64_t e, const int64_t *uoff, const int64_t *ufo, const int64_t *uno,
+                                 int64_t far_tot, int64_t near_tot, int64_t *fstart, int32_t *fcnt, int64_t *nstart,
+                                 int32_t *ncnt) {
+    int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= e) return;
+    int64_t a = uoff[x - s], b = uoff[x - s + 1];
+    fstart[x] = far_tot + ufo[a];
+    nstart[x] = near_tot + uno[a];
+    fcnt[x] = (int32_t)(ufo[b] - ufo[a]);
+    ncnt[x] = (int32_t)(uno[b] - uno[a]);
 }
 
 // ---------------------------------------------------------------- balanced build
@@ -817,26 +852,36 @@ int gx_plan_accurate(gx_ctx *ctx) {
     GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
     GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
                                  ctx->stream));
-    GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(nn + 1) * 2));
-    GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int64_t) * (size_t)(nn + 1) * 2));
     for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
-        int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
-        k_mac<<<gx_blocks(c * 32, 128), 128, 0, ctx->stream>>>(s, e, 0, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
-                                                          dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta,
-                                                          nstart, ncnt, dptr<int32_t>(ctx->near_idx), fcnt, ncnt,
-                                                          nullptr, nullptr, nullptr, nullptr);
-        // offsets of this level: exclusive scans of the counts, shifted by the running totals
-        int64_t *fc64 = dptr<int64_t>(ctx->scratch_a), *nc64 = fc64 + (c + 1);
-        int64_t *fo = dptr<int64_t>(ctx->scratch_b), *no = fo + (c + 1);
-        GX_CUDA(ctx, cudaMemsetAsync(fc64 + c, 0, sizeof(int64_t), ctx->stream));
-        GX_CUDA(ctx, cudaMemsetAsync(nc64 + c, 0, sizeof(int64_t), ctx->stream));
-        k_i32_to_i64<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(fcnt + s, fc64, c);
-        k_i32_to_i64<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(ncnt + s, nc64, c);
-        GX_TRY(gx_exclusive_scan_i64(ctx, fc64, fo, c + 1));
-        GX_TRY(gx_exclusive_scan_i64(ctx, nc64, no, c + 1));
+        const int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
+        // units: chunks of each node's candidate list
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(c + 1) * 2));
+        int64_t *nch = dptr<int64_t>(ctx->scratch_a), *uoff = nch + (c + 1);
+        GX_CUDA(ctx, cudaMemsetAsync(nch + c, 0, sizeof(int64_t), ctx->stream));
+        k_mac_nchunks<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, dptr<int32_t>(ctx->parent), ncnt, nch);
+        GX_TRY(gx_exclusive_scan_i64(ctx, nch, uoff, c + 1));
+        int64_t U = 0;
+        GX_CUDA(ctx, cudaMemcpyAsync(&U, uoff + c, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        // unit -> (node, chunk); per-unit counts, then their offsets
+        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int32_t) * (size_t)(U + 1) * 2));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_e, sizeof(int64_t) * (size_t)(U + 1) * 4));
+        int32_t *unode = dptr<int32_t>(ctx->scratch_b), *uchunk = unode + (U + 1);
+        int64_t *ufar = dptr<int64_t>(ctx->scratch_e), *unear = ufar + (U + 1), *ufo = unear + (U + 1),
+                *uno = ufo + (U + 1);
+        k_mac_units<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, unode, uchunk);
+        GX_CUDA(ctx, cudaMemsetAsync(ufar + U, 0, sizeof(int64_t), ctx->stream));
+        GX_CUDA(ctx, cudaMemsetAsync(unear + U, 0, sizeof(int64_t), ctx->stream));
+        const unsigned gu = (unsigned)((U * 32 + 127) / 128);
+        if (U > 0)
+            k_mac<<<gu, 128, 0, ctx->stream>>>(U, 0, unode, uchunk, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
+                                               dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta, nstart,
+                                               ncnt, dptr<int32_t>(ctx->near_idx), ufar, unear, nullptr, nullptr);
+        GX_TRY(gx_exclusive_scan_i64(ctx, ufar, ufo, U + 1));
+        GX_TRY(gx_exclusive_scan_i64(ctx, unear, uno, U + 1));
         int64_t ft = 0, nt = 0;
-        GX_CUDA(ctx, cudaMemcpyAsync(&ft, fo + c, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
-        GX_CUDA(ctx, cudaMemcpyAsync(&nt, no + c, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(&ft, ufo + U, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(&nt, uno + U, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         // grow (preserving) the index arrays
         auto grow = [&](DevBuf &b, size_t &cap, int64_t need) -> int {
@@ -854,14 +899,17 @@ int gx_plan_accurate(gx_ctx *ctx) {
         };
         GX_TRY(grow(ctx->far_idx, far_cap, far_tot + ft + 1));
         GX_TRY(grow(ctx->near_idx, near_cap, near_tot + nt + 1));
-        // starts = level offsets + running totals
-        GX_TRY(gx_add_offsets(ctx, fo, fstart + s, c, far_tot));
-        GX_TRY(gx_add_offsets(ctx, no, nstart + s, c, near_tot));
-        k_mac<<<gx_blocks(c * 32, 128), 128, 0, ctx->stream>>>(s, e, 1, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
-                                                          dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta,
-                                                          nstart, ncnt, dptr<int32_t>(ctx->near_idx), fcnt, ncnt, fstart,
-                                                          nstart, dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx));
-        ctx->launches += 6;
+        // fill: unit u writes at running total + its offset
+        GX_TRY(gx_add_offsets(ctx, ufo, ufar, U, far_tot));
+        GX_TRY(gx_add_offsets(ctx, uno, unear, U, near_tot));
+        if (U > 0)
+            k_mac<<<gu, 128, 0, ctx->stream>>>(U, 1, unode, uchunk, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
+                                               dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, ctx->theta, nstart,
+                                               ncnt, dptr<int32_t>(ctx->near_idx), ufar, unear,
+                                               dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx));
+        k_mac_node_lists<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, ufo, uno, far_tot, near_tot, fstart,
+                                                                     fcnt, nstart, ncnt);
+        ctx->launches += 9;
         GX_CUDA(ctx, cudaGetLastError());
         far_tot += ft;
         near_tot += nt;

@@ -199,11 +199,13 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
                         double *gx0, double *gy0, double *gvx0, double *gvy0, double *gm, int64_t *peak_bytes);
 
 /* Device time of the last force evaluation per pass, in ms:
- * {total, prepare, p2m, m2m, m2l, l2l, l2p+p2p}; returns 7 entries. */
+ * {total, prepare, p2m, m2m, m2l, l2l, l2p+p2p}; returns 7 entries.  The near field
+ * (P2P) runs on a second, lower-priority stream beside m2m..l2l, so those passes
+ * include the slots it takes, and the last entry is the wait for it plus L2P. */
 int gx_last_timings(gx_ctx *ctx, double out[7]);
 /* Runs `reps` force evaluations on the resident bodies and returns the CUDA-event
- * time of each on the context stream (ms) and the time of one pass of it
- * (`which`: 0 = L2P+P2P, 1 = M2L).  With flush_l2 != 0 a 256 MB buffer (twice
+ * time of each on the context stream (ms) and the time of one kernel of it
+ * (`which`: 0 = the P2P kernel, timed on its own stream; 1 = the M2L pass).  With flush_l2 != 0 a 256 MB buffer (twice
  * the L2) is written before each evaluation, outside its timed interval. */
 int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each, int32_t which,
                     double *kernel_ms_each);

@@ -320,3 +320,31 @@ def test_kdk_rebuild_every_step_stays_finite_and_conserves_momentum(G):
     pscale = np.sum(b.mass * np.hypot(b.vx, b.vy))
     p0 = np.array([np.sum(b.mass * b.vx), np.sum(b.mass * b.vy)])
     assert np.all(np.abs(diag[:, 3:5] - p0) / pscale < 1e-3)
+
+
+@pytest.mark.parametrize("rebuild", [0, 1])
+def test_rollout_gradient_matches_frozen_tree_finite_differences(G, rebuild):
+    """FP64 rollout gradient against central differences with every step's tree taken
+    from the unperturbed trajectory (galax_gb300.fdcheck), static and rebuilt trees."""
+    from galax_gb300 import fdcheck, presets
+    n, T, dt = 3_001, 15, 5e-3
+    bounds = presets.BOUNDS["galaxy"]
+    b = presets.galaxy(n, seed=63)
+    ctx = _ctx(G, b, bounds, 0.05)
+    R = _rot(0.8)
+    n_ = len(b)
+    ctx.upload_bodies(b)
+    ctx.rollout_forward(T, dt, 4, rebuild_every=rebuild)
+    ids = ctx.body_ids() if rebuild else None
+    fin = G.Bodies.new(n_)
+    ctx.download_bodies(fin)
+    L, lxT, lyT, d0x, d0y = fdcheck.rollout_loss(b.x, b.y, fin.x, fin.y, R, ids)
+    gx, gy, gvx, gvy, gm, _ = ctx.rollout_backward(lxT, lyT, np.zeros(n_), np.zeros(n_))
+    g = (gx + d0x, gy + d0y, gvx, gvy, gm)
+    rng = np.random.default_rng(7)
+    dirs = [[rng.standard_normal(n_) for _ in range(4)] + [rng.standard_normal(n_) * b.mass] for _ in range(3)]
+    num = fdcheck.fd_frozen_trees(G, ctx, b, T, dt, R, dirs, 1e-6, 32, bounds, rebuild=bool(rebuild))
+    ctx.close()
+    for i, d in enumerate(dirs):
+        an = sum(float(np.dot(g[q], d[q])) for q in range(5))
+        assert abs(num[i] - an) <= 1e-5 * abs(num[i]), (i, num[i], an)
