@@ -4,19 +4,26 @@ Metric (one JSON line on rank 0): bodies/s of one FMM force evaluation of the
 mixed-precision form (FP32 P2M/L2P/P2P, FP32 M2L, FP64 state) in ACCURATE mode
 (near/far lists by the opening angle theta on the reference's Morton tree,
 median relative force error <= 1e-4 against the exact FP64 N^2 sum), with the
-FP64 form and the reference-semantics (REF) FP64 form timed beside it, and the
-force error of each against the FP64 N^2 sum on 1000 seeded sample bodies.
+FP64 form and the reference-semantics (REF) FP64 form timed beside it, the force
+error of each against the FP64 N^2 sum on 1000 seeded sample bodies, whole
+leapfrog steps with a static and with a per-step rebuilt tree, and the
+adjoint/forward time of reverse-mode rollouts.
 
   value      whole-job bodies/s with bodies resident in HBM (CUDA events on the
              context stream, L2 flushed by a 256 MB write before every step,
              outside the step's timed interval)
   e2e        the same through the C ABI call gx_compute_forces with pinned host
              buffers: each step copies x, y, m host->device and ax, ay back
-  roofline   the dominant kernel (fused L2P+P2P, FP32 pipe): algorithmic FLOPs
-             (14 per body-body interaction) per launch / its event-timed duration,
-             against the FP32 FMA peak measured on this GPU in the same run
+  roofline   the dominant kernel (P2P, FP32 pipe): algorithmic FLOPs (14 per
+             body-body interaction) per launch / its event-timed duration, against
+             the FP32 FMA peak measured on this GPU in the same run
   cpu_baseline  the oracle (C restatement of galax-core's CPU FMM, REF semantics,
              OpenMP where the reference uses Rayon) on the host cores
+  kdk_steps  leapfrog steps/s, static tree and tree rebuilt every step
+  adjoint    galaxy N=200,001 x 100 steps (FP64 and mixed, finite differences with
+             the tree sequence frozen) and Plummer N=1M x 500 steps (mixed,
+             checkpoint interval sweep, peak device bytes), both rebuilding the
+             tree every step
 
 ``--impl reference`` times the reference's CPU algorithm (the oracle port) on the
 same workload instead.  Multi-GPU: the force evaluation does not shard here, so
@@ -113,6 +120,16 @@ class ClockSampler:
 def _rel_err(ax, ay, rx, ry):
     den = np.maximum(np.hypot(rx, ry), 1e-30)
     return np.hypot(ax - rx, ay - ry) / den
+
+
+def _err_stats(ax, ay, rx, ry):
+    """Vector metric |a - a*| / |a*| (median, p99) and the reference's magnitude metric
+    ||a| - |a*|| / max(|a*|, 1e-20) (validate_fmm, galax-core lib.rs:1553-1557: mean, max)."""
+    e = _rel_err(ax, ay, rx, ry)
+    am, rm = np.hypot(ax, ay), np.hypot(rx, ry)
+    mag = np.abs(am - rm) / np.maximum(rm, 1e-20)
+    return {"err_median": float(np.median(e)), "err_p99": float(np.percentile(e, 99)),
+            "err_mag_mean": float(np.mean(mag)), "err_mag_max": float(np.max(mag))}
 
 
 def _cpu_baseline(bodies_sorted, bounds, eps, n_evals: int = 2):
@@ -277,6 +294,74 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
 
 
 
+def run_build_only(args):
+    """Tree construction alone (device Morton keys, radix sort, permutation, leaves and
+    parent rounds) over resident Plummer bodies, a few times: the workload of the tree
+    build profile.  Prints one JSON line with the host-timed rebuilds."""
+    import galax_gb300 as G
+    from galax_gb300 import build as gbuild
+    from galax_gb300 import presets
+    gbuild.build()
+    n = args.n
+    b = presets.plummer(n, seed=args.seed)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=P, eps64=0.1))
+    ctx.build_tree(b.copy(), N_MAX, presets.BOUNDS["plummer"])
+    times = []
+    for _ in range(max(1, args.steps)):
+        ctx.upload_bodies(b)  # unsorted order again: the sort does full work
+        t0 = time.perf_counter()
+        ctx.rebuild_resident(N_MAX, presets.BOUNDS["plummer"])
+        times.append(time.perf_counter() - t0)
+    nn, nl, lv, _ = ctx.tree_info()
+    ctx.close()
+    print(json.dumps({"build_only": True, "n": n, "nodes": nn, "leaves": nl, "levels": lv,
+                      "ms": [t * 1e3 for t in times]}), flush=True)
+    return 0
+
+
+def run_sweep_disk(args):
+    """Accuracy/throughput sweep on the disk preset (N = 4,000,000 by default):
+    p in {2,4,6,8} x n_max in {16,32,64}, mixed and FP64 forms, errors against the FP64
+    N^2 sum on 1000 seeded samples.  Prints one JSON line."""
+    import galax_gb300 as G
+    from galax_gb300 import build as gbuild
+    from galax_gb300 import presets
+    gbuild.build()
+    n = args.sweep_n
+    bounds = presets.BOUNDS["disk"]
+    b0 = presets.disk(n, seed=args.seed + 3)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=8, eps64=0.1))
+    rows = []
+    for n_max in (16, 32, 64):
+        b = b0.copy()
+        ctx.build_tree(b, n_max, bounds)
+        eps = presets.cli_softening(b.x, b.y)
+        ctx.upload_bodies(b)
+        idx = np.sort(np.random.default_rng(4321).choice(n, min(1000, n), replace=False))
+        for p in (2, 4, 6, 8):
+            ctx.set_params(p, eps)
+            ex, ey = ctx.n2_sampled(idx)
+            for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+                ctx.set_mode(G.MODE_ACCURATE, prec, THETA)
+                ctx.forces_resident()
+                reps = 3 if name == "mixed" else 1
+                ms, _ = ctx.bench_forces(reps, True, 0)
+                r = G.Bodies.new(n)
+                ctx.download_bodies(r)
+                far, near, inter = ctx.plan_info()
+                row = {"n_max": n_max, "p": p, "form": name, "ms": float(np.mean(ms)),
+                       "bodies_per_s": n / (float(np.mean(ms)) * 1e-3), "far_pairs": far,
+                       "near_leaf_pairs": near, "p2p_interactions": inter,
+                       "tiles": {"m2l": f"warp per target node, lane per far source; C(p)={(p + 1) * (p + 2) // 2} "
+                                        f"coefficients, {(2 * p + 1) * (2 * p + 2) // 2} derivatives per pair",
+                                 "p2p": f"warp per item (target leaf of <= {n_max} bodies x <= 32 source leaves)"}}
+                row.update(_err_stats(r.ax[idx], r.ay[idx], ex, ey))
+                rows.append(row)
+    ctx.close()
+    print(json.dumps({"sweep": "disk", "n": n, "theta": THETA, "seed": args.seed + 3, "rows": rows}), flush=True)
+    return 0
+
+
 def run_ours(args, rank, world, local, pg):
     import galax_gb300 as G
     from galax_gb300 import build as gbuild
@@ -327,9 +412,7 @@ def run_ours(args, rank, world, local, pg):
     idx = np.sort(np.random.default_rng(1234).choice(n, min(1000, n), replace=False))
     ex, ey = ctx.n2_sampled(idx)
     for name in res:
-        e = _rel_err(res[name]["ax"][idx], res[name]["ay"][idx], ex, ey)
-        res[name]["err_median"] = float(np.median(e))
-        res[name]["err_p99"] = float(np.percentile(e, 99))
+        res[name].update(_err_stats(res[name]["ax"][idx], res[name]["ay"][idx], ex, ey))
     d = _rel_err(res["mixed"]["ax"], res["mixed"]["ay"], res["fp64"]["ax"], res["fp64"]["ay"])
 
     # end to end through the C ABI with pinned host buffers (mixed form)
@@ -403,7 +486,8 @@ def run_ours(args, rank, world, local, pg):
         "gpu_launches": int(sum(r["launches"] * (r["steps"] + 1) for r in res.values())),
         "clocks": clocks,
         "forms": {k: {"bodies_per_s": n / (float(np.mean(r["ms"])) * 1e-3), "ms_per_step": float(np.mean(r["ms"])),
-                      "err_median": r["err_median"], "err_p99": r["err_p99"], "plan_s": r["plan_s"],
+                      "err_median": r["err_median"], "err_p99": r["err_p99"], "err_mag_mean": r["err_mag_mean"],
+                      "err_mag_max": r["err_mag_max"], "plan_s": r["plan_s"],
                       "far_pairs": r["far"], "near_leaf_pairs": r["near"], "p2p_interactions": r["inter"],
                       "pass_ms": dict(zip(["total", "prepare", "p2m", "m2m", "m2l", "l2l", "l2p_p2p"], r["passes"]))}
                   for k, r in res.items()},
@@ -437,6 +521,9 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=500)
     ap.add_argument("--adj-k", type=lambda s: [int(v) for v in s.split(",")], default=[10, 22, 50, 1])
     ap.add_argument("--fd-dirs", type=int, default=2)
+    ap.add_argument("--sweep", choices=["disk"], default=None)
+    ap.add_argument("--build-only", action="store_true")
+    ap.add_argument("--sweep-n", type=int, default=4_000_000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -444,6 +531,10 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args, rank, world, pg)
+        if args.sweep == "disk":
+            return run_sweep_disk(args) if rank == 0 else 0
+        if args.build_only:
+            return run_build_only(args) if rank == 0 else 0
         return run_ours(args, rank, world, local, pg)
     finally:
         if pg is not None:

@@ -306,7 +306,7 @@ __global__ void k_scrub(int64_t n, T *v) {
 // M2L takes in = signed moments (-1)^|S| M[S], out = the local accumulator; the
 // adjoint M2L^T takes in = dL[T]/T!, out = the moment cotangent accumulator.
 template <int P, class T>
-__device__ __forceinline__ void m2l_fused(T dx, T dy, T eps2, const T *in, T *out) {
+__device__ __forceinline__ void m2l_fused_core(T dx, T dy, T eps2, const T *in, T *out) {
     const int PP = gx_rt_order(P);
     const int Q = 2 * PP;
     T a[nc2(2 * P)];
@@ -340,6 +340,38 @@ __device__ __forceinline__ void m2l_fused(T dx, T dy, T eps2, const T *in, T *ou
                     if (yi + yj <= PP && xi + xj <= PP) out[gx_mi(xi, xj)] += in[gx_mi(yi, yj)] * Av;
                 }
         }
+    }
+}
+
+// FP32 at p >= 6: the order-2p derivatives reach R^-(4p+1) (2p)!, beyond the FP32
+// range for R ~ 0.1.  The 1/R kernel is homogeneous of degree -1 in (d, eps), so the
+// derivatives are formed at unit distance, d' = d/R, and the powers of 1/R go to the
+// operands:  out[X] += R^-(1+|X|) sum_Y (in[Y] R^-|Y|) A'[X+Y].
+template <int P, class T>
+__device__ __forceinline__ void m2l_fused(T dx, T dy, T eps2, const T *in, T *out) {
+    if constexpr (sizeof(T) == 4 && P >= 6) {
+        constexpr int NC = nc2(P);
+        const int PP = gx_rt_order(P);
+        const T ir = rsqrt_t<T>(dx * dx + dy * dy + eps2);
+        T pw[P + 2];
+        pw[0] = T(1);
+#pragma unroll
+        for (int q = 1; q <= PP + 1; q++) pw[q] = pw[q - 1] * ir;
+        T sin_[NC], sout[NC];
+#pragma unroll
+        for (int yi = 0; yi <= PP; yi++)
+#pragma unroll
+            for (int yj = 0; yj <= PP - yi; yj++) {
+                sin_[gx_mi(yi, yj)] = in[gx_mi(yi, yj)] * pw[yi + yj];
+                sout[gx_mi(yi, yj)] = T(0);
+            }
+        m2l_fused_core<P, T>(dx * ir, dy * ir, eps2 * (ir * ir), sin_, sout);
+#pragma unroll
+        for (int xi = 0; xi <= PP; xi++)
+#pragma unroll
+            for (int xj = 0; xj <= PP - xi; xj++) out[gx_mi(xi, xj)] += sout[gx_mi(xi, xj)] * pw[1 + xi + xj];
+    } else {
+        m2l_fused_core<P, T>(dx, dy, eps2, in, out);
     }
 }
 

@@ -134,3 +134,28 @@ def test_p2p_only_at_p0_equals_p2p(G, oracle):
     oracle.p2p(pp, t, u, 0.1)
     ax, ay = _run_gpu(G, ob, t, v, u, 0, 0.1, G.MODE_REF)
     assert np.max(np.abs(ax - pp.ax)) < 1e-12 and np.max(np.abs(ay - pp.ay)) < 1e-12
+
+
+@pytest.mark.parametrize("p", [6, 8])
+def test_mixed_high_order_dense_cluster_stays_finite(G, p):
+    """100k bodies in the unit square: far pairs at R ~ 0.04, where the order-2p
+    derivatives (R^-(4p+1) (2p)!) exceed the FP32 range at p = 8.  The FP32 M2L forms
+    them at unit distance and rescales the operands; the mixed forces stay finite and
+    agree with the FP64 form."""
+    n = 100_000
+    rng = np.random.default_rng(31)
+    b = G.Bodies.from_arrays(rng.uniform(0, 1, n), rng.uniform(0, 1, n), np.full(n, 1.0 / n))
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=p, eps64=1e-3))
+    ctx.build_tree(b, 32, (0.0, 1.0, 0.0, 1.0))
+    ctx.upload_bodies(b)
+    out = {}
+    for name, prec in (("fp64", G.PREC_FP64), ("mixed", G.PREC_MIXED)):
+        ctx.set_mode(G.MODE_ACCURATE, prec, 0.5)
+        ctx.forces_resident()
+        r = G.Bodies.new(n)
+        ctx.download_bodies(r)
+        out[name] = (r.ax.copy(), r.ay.copy())
+    ctx.close()
+    assert np.all(np.isfinite(out["mixed"][0])) and np.all(np.isfinite(out["mixed"][1]))
+    d = rel_vec_err(out["mixed"][0], out["mixed"][1], out["fp64"][0], out["fp64"][1])
+    assert np.median(d) < 1e-5, np.median(d)
