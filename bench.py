@@ -47,6 +47,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FMM bodies/s (1M, p=4) mixed vs FP64 at equal force error; adjoint/fwd time"
 N_DEFAULT = 1_000_000
+# DRAM bytes (read + write) of one k_p2p32_items launch at the default workload, from
+# the ncu capture summarised in profiles/k_p2p32_items_plummer1m_dram.md (None until
+# captured)
+P2P_TRAFFIC_1M = None
 P, N_MAX, THETA = 4, 32, 0.5
 
 
@@ -459,6 +463,10 @@ def run_ours(args, rank, world, local, pg):
     kms = float(np.mean(mix["kms"]))
     flops = 14.0 * mix["inter"]
     achieved = flops / (kms * 1e-3) / 1e12
+    # the whole evaluation's FP32 work (P2P and the M2L contraction, 2 C(p)^2 = 450 FLOP
+    # per far pair) over its event time: P2P shares the SMs with M2L while it runs
+    eval_flops = flops + 2.0 * ((P + 1) * (P + 2) // 2) ** 2 * mix["far"]
+    eval_tflops = eval_flops / (float(np.mean(mix["ms"])) * 1e-3) / 1e12
     if rank != 0:
         ctx.close()
         return 0
@@ -480,9 +488,11 @@ def run_ours(args, rank, world, local, pg):
         "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "bodies/s", "h2d_bytes_per_step": 3 * 8 * n,
                 "d2h_bytes_per_step": 2 * 8 * n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
-                     "frac": achieved / peak32 if peak32 else None, "traffic": None,
-                     "kernel": "k_p2p32_items (P2P, packed FP32)",
-                     "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)"},
+                     "frac": achieved / peak32 if peak32 else None, "traffic": P2P_TRAFFIC_1M if n == N_DEFAULT else None,
+                     "kernel": "k_p2p32_items (P2P, packed FP32; timed on its own stream while it shares the SMs "
+                               "with M2L)",
+                     "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)",
+                     "evaluation_tflops": eval_tflops, "evaluation_frac": eval_tflops / peak32 if peak32 else None},
         "gpu_launches": int(sum(r["launches"] * (r["steps"] + 1) for r in res.values())),
         "clocks": clocks,
         "forms": {k: {"bodies_per_s": n / (float(np.mean(r["ms"])) * 1e-3), "ms_per_step": float(np.mean(r["ms"])),
