@@ -47,10 +47,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FMM bodies/s (1M, p=4) mixed vs FP64 at equal force error; adjoint/fwd time"
 N_DEFAULT = 1_000_000
-# DRAM bytes (read + write) of one k_p2p32_items launch at the default workload, from
-# the ncu capture summarised in profiles/k_p2p32_items_plummer1m_dram.md (None until
-# captured)
-P2P_TRAFFIC_1M = None
+# DRAM bytes (read 46.86 MB + written 19.06 MB) of one k_p2p32_items launch at the
+# default workload, from the one-pass ncu capture summarised in
+# profiles/k_p2p32_items_plummer200k.md (the kernel works out of L2)
+P2P_TRAFFIC_1M = 65.92e6
 P, N_MAX, THETA = 4, 32, 0.5
 
 

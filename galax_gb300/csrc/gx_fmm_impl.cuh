@@ -93,7 +93,7 @@ __host__ __device__ constexpr int nc2(int q) { return (q + 1) * (q + 2) / 2; }  
 // (a zero the compiler cannot see through) so the loops stay rolled and the
 // translation units compile in seconds.
 __constant__ int g_rt_zero = 0;
-__device__ __forceinline__ int gx_rt_order(int P) { return P <= 5 ? P : P + g_rt_zero; }
+__device__ __forceinline__ int gx_rt_order(int P) { return P <= 8 ? P : P + g_rt_zero; }
 
 template <class T>
 __device__ __forceinline__ T warp_sum_t(T v) {
@@ -305,40 +305,75 @@ __global__ void k_scrub(int64_t n, T *v) {
 // only the unscaled values of the last two orders feed the recurrence.  The forward
 // M2L takes in = signed moments (-1)^|S| M[S], out = the local accumulator; the
 // adjoint M2L^T takes in = dL[T]/T!, out = the moment cotangent accumulator.
-template <int P, class T>
-__device__ __forceinline__ void m2l_fused_core(T dx, T dy, T eps2, const T *in, T *out) {
-    const int PP = gx_rt_order(P);
-    const int Q = 2 * PP;
-    T a[nc2(2 * P)];
-    T r2 = dx * dx + dy * dy + eps2;
-    T ir = rsqrt_t<T>(r2);
-    T ir2 = ir * ir;
-    a[0] = ir;
-    out[0] += in[0] * ir;
+// One derivative order N of the fused M2L: the recurrence for the N+1 terms of order N
+// (from the unscaled orders N-1 and N-2) and every contraction term they complete.
+// A compile-time order keeps every index constant, so the arrays stay in registers.
+template <int P, int N, class T>
+__device__ __forceinline__ void m2l_order(T dx, T dy, T ir2, T *a, const T *in, T *out) {
+    if constexpr (N <= 2 * P) {
+        const T in_ = tab_inv<T>(N) * ir2;
+        const T c1 = -(T)(2 * N - 1) * in_, c2 = -(T)(N - 1) * in_;
 #pragma unroll
-    for (int n = 1; n <= Q; n++) {
-        const T in_ = tab_inv<T>(n) * ir2;
-        const T c1 = -(T)(2 * n - 1) * in_, c2 = -(T)(n - 1) * in_;
-#pragma unroll
-        for (int k = 0; k <= n; k++) {
-            const int l = n - k;
+        for (int k = 0; k <= N; k++) {
+            const int l = N - k;
             T s1, s2 = T(0);
             if (k >= 1 && l >= 1) s1 = dx * a[gx_mi(k - 1, l)] + dy * a[gx_mi(k, l - 1)];
             else if (k >= 1) s1 = dx * a[gx_mi(k - 1, l)];
             else s1 = dy * a[gx_mi(k, l - 1)];
             if (k >= 2) s2 += a[gx_mi(k - 2, l)];
             if (l >= 2) s2 += a[gx_mi(k, l - 2)];
-            const T v = n >= 2 ? c1 * s1 + c2 * s2 : c1 * s1;
+            const T v = N >= 2 ? c1 * s1 + c2 * s2 : c1 * s1;
             a[gx_mi(k, l)] = v;
-            const T Av = n >= 2 ? v * tab_ff<T>(k, l) : v;
+            const T Av = N >= 2 ? v * tab_ff<T>(k, l) : v;
             // all splits (k, l) = X + Y with |X| <= p, |Y| <= p
 #pragma unroll
-            for (int yi = (k > PP ? k - PP : 0); yi <= (k < PP ? k : PP); yi++)
+            for (int yi = (k > P ? k - P : 0); yi <= (k < P ? k : P); yi++)
 #pragma unroll
-                for (int yj = (l > PP ? l - PP : 0); yj <= (l < PP ? l : PP); yj++) {
+                for (int yj = (l > P ? l - P : 0); yj <= (l < P ? l : P); yj++) {
                     const int xi = k - yi, xj = l - yj;
-                    if (yi + yj <= PP && xi + xj <= PP) out[gx_mi(xi, xj)] += in[gx_mi(yi, yj)] * Av;
+                    if (yi + yj <= P && xi + xj <= P) out[gx_mi(xi, xj)] += in[gx_mi(yi, yj)] * Av;
                 }
+        }
+        m2l_order<P, N + 1, T>(dx, dy, ir2, a, in, out);
+    }
+}
+
+template <int P, class T>
+__device__ __forceinline__ void m2l_fused_core(T dx, T dy, T eps2, const T *in, T *out) {
+    T r2 = dx * dx + dy * dy + eps2;
+    T ir = rsqrt_t<T>(r2);
+    T ir2 = ir * ir;
+    out[0] += in[0] * ir;
+    if constexpr (P <= 8) {
+        T a[nc2(2 * P)];
+        a[0] = ir;
+        m2l_order<P, 1, T>(dx, dy, ir2, a, in, out);
+    } else {
+        // high orders: run-time loop bounds keep the code size bounded
+        const int PP = gx_rt_order(P);
+        const int Q = 2 * PP;
+        T a[nc2(2 * P)];
+        a[0] = ir;
+        for (int n = 1; n <= Q; n++) {
+            const T in_ = tab_inv<T>(n) * ir2;
+            const T c1 = -(T)(2 * n - 1) * in_, c2 = -(T)(n - 1) * in_;
+            for (int k = 0; k <= n; k++) {
+                const int l = n - k;
+                T s1, s2 = T(0);
+                if (k >= 1 && l >= 1) s1 = dx * a[gx_mi(k - 1, l)] + dy * a[gx_mi(k, l - 1)];
+                else if (k >= 1) s1 = dx * a[gx_mi(k - 1, l)];
+                else s1 = dy * a[gx_mi(k, l - 1)];
+                if (k >= 2) s2 += a[gx_mi(k - 2, l)];
+                if (l >= 2) s2 += a[gx_mi(k, l - 2)];
+                const T v = n >= 2 ? c1 * s1 + c2 * s2 : c1 * s1;
+                a[gx_mi(k, l)] = v;
+                const T Av = n >= 2 ? v * tab_ff<T>(k, l) : v;
+                for (int yi = (k > PP ? k - PP : 0); yi <= (k < PP ? k : PP); yi++)
+                    for (int yj = (l > PP ? l - PP : 0); yj <= (l < PP ? l : PP); yj++) {
+                        const int xi = k - yi, xj = l - yj;
+                        if (yi + yj <= PP && xi + xj <= PP) out[gx_mi(xi, xj)] += in[gx_mi(yi, yj)] * Av;
+                    }
+            }
         }
     }
 }
@@ -774,38 +809,46 @@ __global__ void __launch_bounds__(128, 7) k_p2p32_items(int64_t n_items, const i
                     sm[w][lane] = cur.z;
                     __syncwarp();
                     int ns = min(32, s1 - s0 - sc);
-                    if (ns == 32 && srcl != leaf) {
+                    // four sources kk .. kk+3 on packed FP32
+                    auto quad = [&](int kk) {
+                        float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
+                        float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
+                        float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
+                        uint64_t dx0 = sub2(pk2(X.x, X.y), XI), dy0 = sub2(pk2(Y.x, Y.y), YI);
+                        uint64_t dx1 = sub2(pk2(X.z, X.w), XI), dy1 = sub2(pk2(Y.z, Y.w), YI);
+                        uint64_t r0 = fma2(dx0, dx0, fma2(dy0, dy0, E2));
+                        uint64_t r1 = fma2(dx1, dx1, fma2(dy1, dy1, E2));
+                        float ra, rb;
+                        upk2(r0, ra, rb);
+                        uint64_t i0 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                        upk2(r1, ra, rb);
+                        uint64_t i1 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                        uint64_t f0 = mul2(pk2(Mq.x, Mq.y), mul2(mul2(i0, i0), i0));
+                        uint64_t f1 = mul2(pk2(Mq.z, Mq.w), mul2(mul2(i1, i1), i1));
+                        AXa = fma2(f0, dx0, AXa);
+                        AYa = fma2(f0, dy0, AYa);
+                        AXb = fma2(f1, dx1, AXb);
+                        AYb = fma2(f1, dy1, AYb);
+                    };
+                    const bool own = srcl == leaf;
+                    int k0 = 0;  // sources below k0 are done
+                    if (!own) {
+                        if (ns == 32) {
 #pragma unroll
-                        for (int kk = 0; kk < 32; kk += 4) {
-                            float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
-                            float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
-                            float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
-                            uint64_t dx0 = sub2(pk2(X.x, X.y), XI), dy0 = sub2(pk2(Y.x, Y.y), YI);
-                            uint64_t dx1 = sub2(pk2(X.z, X.w), XI), dy1 = sub2(pk2(Y.z, Y.w), YI);
-                            uint64_t r0 = fma2(dx0, dx0, fma2(dy0, dy0, E2));
-                            uint64_t r1 = fma2(dx1, dx1, fma2(dy1, dy1, E2));
-                            float ra, rb;
-                            upk2(r0, ra, rb);
-                            uint64_t i0 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
-                            upk2(r1, ra, rb);
-                            uint64_t i1 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
-                            uint64_t f0 = mul2(pk2(Mq.x, Mq.y), mul2(mul2(i0, i0), i0));
-                            uint64_t f1 = mul2(pk2(Mq.z, Mq.w), mul2(mul2(i1, i1), i1));
-                            AXa = fma2(f0, dx0, AXa);
-                            AYa = fma2(f0, dy0, AYa);
-                            AXb = fma2(f1, dx1, AXb);
-                            AYb = fma2(f1, dy1, AYb);
+                            for (int kk = 0; kk < 32; kk += 4) quad(kk);
+                            k0 = 32;
+                        } else {
+                            // partial rows (leaves below n_max, or n_max = 16): packed quads, scalar tail
+                            for (k0 = 0; k0 + 4 <= ns; k0 += 4) quad(k0);
                         }
-                    } else {
-                        const bool own = srcl == leaf;
-                        for (int kk = 0; kk < ns; kk++) {
-                            float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
-                            float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
-                            float fk = sm[w][kk] * (ir * ir * ir);
-                            fk = (own && s0 + sc + kk == i) ? 0.f : fk;
-                            axs = fmaf(fk, dx, axs);
-                            ays = fmaf(fk, dy, ays);
-                        }
+                    }
+                    for (int kk = k0; kk < ns; kk++) {
+                        float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
+                        float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                        float fk = sm[w][kk] * (ir * ir * ir);
+                        fk = (own && s0 + sc + kk == i) ? 0.f : fk;
+                        axs = fmaf(fk, dx, axs);
+                        ays = fmaf(fk, dy, ays);
                     }
                     cur = nxt;
                 }

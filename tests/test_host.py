@@ -58,3 +58,31 @@ def test_cli_rules_match_oracle(oracle):
     ax, ay = np.array([3.0, -4.0]), np.array([4.0, 0.0])
     assert presets.cli_dt(ax, ay) == 0.5 / 5.0 ** 0.5
     assert presets.cli_dt(np.zeros(3), np.zeros(3)) == 0.01
+
+
+def test_rollout_loss_partials_match_finite_differences():
+    """galax_gb300.fdcheck.rollout_loss: L = sum_i |x_T[i] - R x_0[ids[i]]|^2 with the
+    final bodies in a rebuilt (permuted) order."""
+    import numpy as np
+    from galax_gb300 import fdcheck
+    rng = np.random.default_rng(0)
+    n = 50
+    x0, y0, xT, yT = (rng.standard_normal(n) for _ in range(4))
+    ids = rng.permutation(n)
+    c, s = np.cos(0.7), np.sin(0.7)
+    R = np.array([[c, -s], [s, c]])
+    L, lx, ly, d0x, d0y = fdcheck.rollout_loss(x0, y0, xT, yT, R, ids)
+    h = 1e-6
+    for arr, grad in ((xT, lx), (yT, ly), (x0, d0x), (y0, d0y)):
+        for i in (0, 17, 49):
+            old = arr[i]
+            arr[i] = old + h
+            lp = fdcheck.rollout_loss(x0, y0, xT, yT, R, ids)[0]
+            arr[i] = old - h
+            lm = fdcheck.rollout_loss(x0, y0, xT, yT, R, ids)[0]
+            arr[i] = old
+            assert abs((lp - lm) / (2 * h) - grad[i]) < 1e-6 * max(1.0, abs(grad[i]))
+    # identity order by default
+    L2 = fdcheck.rollout_loss(x0, y0, xT, yT, R)[0]
+    L3 = fdcheck.rollout_loss(x0, y0, xT, yT, R, np.arange(n))[0]
+    assert L2 == L3
