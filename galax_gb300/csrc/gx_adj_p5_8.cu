@@ -3,4 +3,5 @@
 
 GX_ADJ_INSTANTIATE(5)
 GX_ADJ_INSTANTIATE(6)
+GX_ADJ_INSTANTIATE(7)
 GX_ADJ_INSTANTIATE(8)

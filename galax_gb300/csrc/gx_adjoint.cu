@@ -17,12 +17,14 @@
 #define GX_VJP_DECL(PP)                                                                                 \
     int gx_run_force_vjp_##PP(gx_ctx *, int, const double *, const double *, const void *, const double *, \
                               const double *, double *, double *, double *);
+GX_VJP_DECL(0)
 GX_VJP_DECL(1)
 GX_VJP_DECL(2)
 GX_VJP_DECL(3)
 GX_VJP_DECL(4)
 GX_VJP_DECL(5)
 GX_VJP_DECL(6)
+GX_VJP_DECL(7)
 GX_VJP_DECL(8)
 
 namespace {
@@ -33,14 +35,16 @@ int force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf, con
               double *gx, double *gy, double *gm) {
     int f32 = ctx->prec == GX_PREC_MIXED;
     switch (ctx->p) {
+        case 0: return gx_run_force_vjp_0(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         case 1: return gx_run_force_vjp_1(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         case 2: return gx_run_force_vjp_2(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         case 3: return gx_run_force_vjp_3(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         case 4: return gx_run_force_vjp_4(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         case 5: return gx_run_force_vjp_5(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         case 6: return gx_run_force_vjp_6(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
+        case 7: return gx_run_force_vjp_7(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
         case 8: return gx_run_force_vjp_8(ctx, f32, X, Y, lf, lx, ly, gx, gy, gm);
-        default: return gx_fail(ctx, GX_ERR_INVALID_ARG, "the adjoint supports p in {1,2,3,4,5,6,8}");
+        default: return gx_fail(ctx, GX_ERR_INVALID_ARG, "the adjoint supports p in 0..8");
     }
 }
 

@@ -175,12 +175,13 @@ int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, do
 int gx_n2_sampled_static(const double *x, const double *y, const double *m, int64_t n, double eps,
                          const int64_t *idx, int64_t n_idx, double *ax, double *ay, void *stream);
 
-/* Reverse mode (GX_MODE_ACCURATE).  Not in the reference: its north star asks for a
- * backward() of the force operator.  gx_force_vjp returns, for cotangents lam of
- * the accelerations of the resident bodies, g_x = sum lam . da/dx and
- * g_m = sum lam . da/dm (host arrays, tree order), the exact transpose of the
+/* Reverse mode (GX_MODE_ACCURATE); no counterpart in the reference, which has no
+ * gradients: the backward() of the force operator.  gx_force_vjp returns, for
+ * cotangents lam of the accelerations of the resident bodies, g_x = sum lam . da/dx
+ * and g_m = sum lam . da/dm (host arrays, tree order), the exact transpose of the
  * frozen-tree evaluation (L2P^T with the Hessian of the local expansion, L2L^T,
- * M2L^T, M2M^T, P2M^T, Hessian-vector P2P), computed in FP64.  p in {1..6, 8}. */
+ * M2L^T, M2M^T, P2M^T, Hessian-vector P2P), in the context's precision (FP64, or
+ * FP32 passes with FP64 outputs in the mixed form).  p in 0..8. */
 int gx_force_vjp(gx_ctx *ctx, const double *lam_x, const double *lam_y, double *gx, double *gy, double *gm);
 /* Leapfrog rollout from the resident state (simulate, galax-integrate/src/lib.rs:204-237)
  * keeping a checkpoint (positions, velocities, accelerations, masses and the leaf

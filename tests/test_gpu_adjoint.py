@@ -26,7 +26,8 @@ def _forces(ctx, x, y, m):
     return ax, ay
 
 
-@pytest.mark.parametrize("preset,n,p", [("plummer", 20_000, 4), ("uniform", 8_000, 2), ("galaxy", 6_001, 6)])
+@pytest.mark.parametrize("preset,n,p", [("plummer", 20_000, 4), ("uniform", 8_000, 2), ("galaxy", 6_001, 6),
+                                          ("uniform", 4_000, 0), ("plummer", 6_000, 8)])
 def test_force_vjp_matches_finite_differences(G, preset, n, p):
     from galax_gb300 import presets
     b = presets.make(preset, n, seed=51)
