@@ -81,7 +81,7 @@ def _max_over_ranks(pg, v: float) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms."""
 
     def __init__(self, device: int):
         self.device = device
@@ -94,7 +94,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
-                                        "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                        "--format=csv,noheader,nounits", "-lms", "20"], stdout=subprocess.PIPE,
                                        stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
