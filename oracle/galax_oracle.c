@@ -1384,10 +1384,13 @@ static void iv_push(ivec *a, int32_t x) {
     a->v[a->n++] = x;
 }
 
-static int mac_far(const gxo_tree *t, const double *R, int64_t a, int64_t b, double theta) {
+/* far when |com_a - com_b| theta > R_a + R_b, compared squared (the device plan does
+ * the same operations, each rounded once: -ffp-contract=off) */
+static int mac_far(const gxo_tree *t, const double *R, int64_t a, int64_t b, double theta2) {
     double ex = t->comx[a] - t->comx[b], ey = t->comy[a] - t->comy[b];
-    double d = sqrt(ex * ex + ey * ey);
-    return d * theta > R[a] + R[b];
+    double d2 = ex * ex + ey * ey;
+    double s = R[a] + R[b];
+    return d2 * theta2 > s * s;
 }
 
 void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_csr **far_out, gxo_csr **near_out) {
@@ -1400,6 +1403,7 @@ void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_c
     ivec *fv = (ivec *)calloc((size_t)(nn > 0 ? nn : 1), sizeof(ivec));
     ivec *nv = (ivec *)calloc((size_t)(nn > 0 ? nn : 1), sizeof(ivec));
     if (nn > 0) iv_push(&nv[nn - 1], (int32_t)(nn - 1)); /* the root is near itself */
+    const double theta2 = theta * theta;
     for (int64_t id = nn - 1; id >= 0; id--) {
         int32_t P = t->parent[id];
         if (P < 0) continue;
@@ -1408,7 +1412,7 @@ void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_c
             for (int k = 0; k < 4; k++) {
                 int32_t c = t->child[4 * y + k];
                 if (c < 0) continue;
-                if (mac_far(t, R, id, c, theta)) iv_push(&fv[id], c);
+                if (mac_far(t, R, id, c, theta2)) iv_push(&fv[id], c);
                 else iv_push(&nv[id], c);
             }
         }
