@@ -406,6 +406,41 @@ class GpuContext:
                                              _p(diag), C.byref(nd)))
         return diag[: 6 * nd.value].reshape(nd.value, 6)
 
+    def simulate(self, n_steps: int, dt: float, energy_every: int = 0, snap_every: int = 0, snapshot=None,
+                 rebuild_every: int = 0) -> np.ndarray:
+        """simulate (galax-integrate/src/lib.rs:204-237) on the resident bodies, with the
+        snapshots the reference CLI's --snap-every asks for (galax-cli/src/main.rs:49):
+        every snap_every steps the bodies are read back, in the order of the last upload
+        even when the tree is rebuilt, and passed to snapshot(step, bodies) -- e.g. a
+        function that writes galx_io.write_snapshot to a file per step.  Returns the
+        diagnostics rows of gx_kdk_run (step, KE, FMM PE, px, py, Lz), taken every
+        energy_every steps counted from the start of each snapshot interval (from the
+        start of the run when snap_every is a multiple of energy_every)."""
+        rows = []
+        done = 0
+        chunk = snap_every if (snap_every > 0 and snapshot is not None) else n_steps
+        while done < n_steps:
+            k = min(chunk, n_steps - done)
+            d = self.kdk_run(k, dt, energy_every, rebuild_every=rebuild_every)
+            if d.size:
+                d = d.copy()
+                d[:, 0] += done
+                rows.append(d)
+            done += k
+            if snapshot is not None and snap_every > 0 and done % snap_every == 0:
+                n = getattr(self, "_n_resident", 0)
+                out = Bodies.new(n)
+                self.download_bodies(out)
+                if rebuild_every > 0:  # back to the order of the last upload
+                    ids = self.body_ids()
+                    for name in ("x", "y", "vx", "vy", "mass", "ax", "ay"):
+                        arr = getattr(out, name)
+                        res = np.empty_like(arr)
+                        res[ids] = arr
+                        setattr(out, name, res)
+                snapshot(done, out)
+        return np.concatenate(rows) if rows else np.zeros((0, 6))
+
     def diagnostics(self) -> np.ndarray:
         out = np.zeros(5)
         self._check(lib().gx_diagnostics(self._h, _p(out)))

@@ -117,3 +117,36 @@ def test_accurate_mixed_kdk_conserves_momentum(G):
     p0 = np.array([np.sum(b.mass * b.vx), np.sum(b.mass * b.vy)])
     assert diag.shape == (2, 6)
     assert np.all(np.abs(diag[:, 3:5] - p0) / pscale < 1e-5)
+
+
+def test_simulate_writes_snapshots_in_upload_order(G, tmp_path):
+    """simulate() with --snap-every semantics: GALX snapshots every k steps, bodies in
+    the order of the upload although the tree (and the resident order) is rebuilt every
+    step; the last snapshot equals the final state."""
+    import io
+    from galax_gb300 import galx_io, presets
+    n = 5_001
+    b = presets.galaxy(n, seed=14)
+    bounds = presets.BOUNDS["galaxy"]
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=4, eps64=0.05))
+    ctx.build_tree(b, 32, bounds)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    ctx.upload_bodies(b)
+    ctx.forces_resident()
+    snaps = {}
+
+    def snapshot(step, bodies):
+        f = io.BytesIO()
+        galx_io.write_snapshot(f, bodies, timestamp=float(step))
+        snaps[step] = f.getvalue()
+
+    diag = ctx.simulate(12, 2e-3, energy_every=4, snap_every=4, snapshot=snapshot, rebuild_every=1)
+    final = G.Bodies.new(n)
+    ctx.download_bodies(final)
+    ids = ctx.body_ids()
+    ctx.close()
+    assert sorted(snaps) == [4, 8, 12]
+    assert diag.shape == (3, 6) and list(diag[:, 0]) == [4.0, 8.0, 12.0]
+    last = galx_io.read_snapshot(io.BytesIO(snaps[12]))
+    assert np.array_equal(last.x[ids], final.x) and np.array_equal(last.vy[ids], final.vy)
+    assert np.array_equal(last.mass, b.mass)  # upload order
