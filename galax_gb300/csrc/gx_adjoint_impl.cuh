@@ -470,13 +470,27 @@ __global__ void __launch_bounds__(128) k_adj_p2p_reduce(int64_t nl, const int32_
     for (int tc = 0; tc < tchunks && t0 + tc * 32 < t1; tc++) {
         int32_t i = t0 + tc * 32 + lane;
         if (i >= t1) continue;
-        S sx = 0, sy = 0, smm = 0;
-        for (int64_t it = item_off[leaf]; it < item_off[leaf + 1]; it++) {
-            V v = part[(it * tchunks + tc) * 32 + lane];
-            sx += v.x;
-            sy += v.y;
-            smm += v.z;
+        // four independent accumulators keep the loads of long item ranges in flight
+        S ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, am[4] = {0, 0, 0, 0};
+        int64_t it = item_off[leaf];
+        const int64_t ie = item_off[leaf + 1];
+        for (; it + 4 <= ie; it += 4) {
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                V v = part[((it + u) * tchunks + tc) * 32 + lane];
+                ax[u] += v.x;
+                ay[u] += v.y;
+                am[u] += v.z;
+            }
         }
+        for (; it < ie; it++) {
+            V v = part[(it * tchunks + tc) * 32 + lane];
+            ax[0] += v.x;
+            ay[0] += v.y;
+            am[0] += v.z;
+        }
+        const S sx = (ax[0] + ax[1]) + (ax[2] + ax[3]), sy = (ay[0] + ay[1]) + (ay[2] + ay[3]),
+                smm = (am[0] + am[1]) + (am[2] + am[3]);
         gx[i] += (double)sx;
         gy[i] += (double)sy;
         gm[i] += (double)smm;
@@ -515,6 +529,27 @@ int run_force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf_
     }
     // A1: L2P^T and the Hessian term (writes gx, gy; the FP32 form also packs bodies)
     k_adj_l2p<P, T><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, Lf, lx, ly, gx, gy, dL, pos32, lam32);
+    // A6 (items) on the second, lower-priority stream beside A2..A5: it needs only the
+    // bodies packed by A1 and writes per-item partials, summed in order after the join
+    const gx_ctx::Items &I = ctx->items_acc;
+    const int tchunks = (int)std::max<int64_t>(1, (ctx->max_leaf + 31) / 32);
+    const unsigned gi = (unsigned)((I.n * 32 + 127) / 128);
+    GX_TRY(gx_ensure(ctx, ctx->part, (F32 ? sizeof(float4) : sizeof(double4)) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
+    GX_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+    GX_CUDA(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+    if (I.n > 0) {
+        if (F32)
+            k_adj_p2p32_items<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                            dptr<int32_t>(I.nq), pos32, lam32, comx, comy, bs, be,
+                                                            dptr<int32_t>(ctx->near_idx), (float)eps2, tchunks,
+                                                            dptr<float4>(ctx->part));
+        else
+            k_adj_p2p_items<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                          dptr<int32_t>(I.nq), X, Y, Mb, lx, ly, bs, be,
+                                                          dptr<int32_t>(ctx->near_idx), eps2, tchunks,
+                                                          dptr<double4>(ctx->part));
+    }
+    GX_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->stream2));
     // A2: L2L^T upward, level by level (leaves are level 0)
     for (int lv = 1; lv < ctx->n_levels; lv++) {
         int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
@@ -531,29 +566,14 @@ int run_force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf_
     // A5: P2M^T (adds to gx, gy; writes gm)
     GX_CUDA(ctx, cudaMemsetAsync(gm, 0, sizeof(double) * (size_t)n, st));
     k_adj_p2m<P, T><<<gw, 128, 0, st>>>(nl, X, Y, Mb, comx, comy, bs, be, dMl, gx, gy, gm);
-    // A6: Hessian-vector P2P
-    const gx_ctx::Items &I = ctx->items_acc;
-    const int tchunks = (int)std::max<int64_t>(1, (ctx->max_leaf + 31) / 32);
-    const unsigned gi = (unsigned)((I.n * 32 + 127) / 128);
-    if (F32) {
-        GX_TRY(gx_ensure(ctx, ctx->part, sizeof(float4) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
-        float4 *part = dptr<float4>(ctx->part);
-        if (I.n > 0)
-            k_adj_p2p32_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
-                                                  pos32, lam32, comx, comy, bs, be, dptr<int32_t>(ctx->near_idx),
-                                                  (float)eps2, tchunks, part);
-        k_adj_p2p_reduce<float4, float><<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks, part, gx, gy,
-                                                            gm);
-    } else {
-        GX_TRY(gx_ensure(ctx, ctx->part, sizeof(double4) * 32 * (size_t)tchunks * (size_t)(I.n + 1)));
-        double4 *part = dptr<double4>(ctx->part);
-        if (I.n > 0)
-            k_adj_p2p_items<<<gi, 128, 0, st>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), X,
-                                                Y, Mb, lx, ly, bs, be, dptr<int32_t>(ctx->near_idx), eps2, tchunks,
-                                                part);
-        k_adj_p2p_reduce<double4, double><<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks, part, gx, gy,
-                                                              gm);
-    }
+    // A6: join, then the ordered sums of the partials (add to gx, gy, gm)
+    GX_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
+    if (F32)
+        k_adj_p2p_reduce<float4, float><<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks,
+                                                            dptr<float4>(ctx->part), gx, gy, gm);
+    else
+        k_adj_p2p_reduce<double4, double><<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks,
+                                                              dptr<double4>(ctx->part), gx, gy, gm);
     ctx->launches += 6 + (ctx->n_levels - 1);
     GX_CUDA(ctx, cudaGetLastError());
     return GX_OK;

@@ -127,6 +127,11 @@ __device__ __forceinline__ uint64_t sub2(uint64_t a, uint64_t b) {
     asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
     return d;
 }
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 __device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
     uint64_t d;
     asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
@@ -758,113 +763,139 @@ __global__ void __launch_bounds__(128, 7) k_p2p32_items(int64_t n_items, const i
     // broadcast 16-byte load yields the x (or y, m) of four consecutive sources
     __shared__ __align__(16) float sx[4][32], sy[4][32], sm[4][32];
     int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (it >= n_items) return;
-    int32_t leaf = item_leaf[it];
-    int64_t qb = item_qb[it];
-    int nq = item_nq[it];
-    int32_t t0 = bs[leaf], t1 = be[leaf];
-    double tcx = comx[leaf], tcy = comy[leaf];
-    int sl = lane < nq ? src_idx[qb + lane] : -1;
-    int sbeg = 0, send = 0;
-    float shx = 0.f, shy = 0.f;
-    if (sl >= 0) {
-        sbeg = bs[sl];
-        send = be[sl];
-        shx = (float)(comx[sl] - tcx);
-        shy = (float)(comy[sl] - tcy);
-    }
-    auto fetch = [&](int k, int sc) -> float4 {
-        int s0 = __shfl_sync(0xffffffffu, sbeg, k) + sc, s1 = __shfl_sync(0xffffffffu, send, k);
-        float gx = __shfl_sync(0xffffffffu, shx, k), gy = __shfl_sync(0xffffffffu, shy, k);
-        int j = s0 + lane;
-        float4 v = (j < s1) ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        v.x += gx;
-        v.y += gy;
-        return v;
-    };
-    for (int tc = 0; tc < tchunks; tc++) {
-        int32_t i = t0 + tc * 32 + lane;
-        bool valid = i < t1;
-        float4 me = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        float xi = me.x, yi = me.y;
-        const uint64_t XI = pk2(xi, xi), YI = pk2(yi, yi), E2 = pk2(eps2, eps2);
-        // full 32-source rows: four packed accumulator chains (sources 4q, 4q+1 in
-        // AXa/AYa; 4q+2, 4q+3 in AXb/AYb) so consecutive updates are independent;
-        // the own leaf and partial rows go through the scalar loop into axs/ays
-        uint64_t AXa = 0, AYa = 0, AXb = 0, AYb = 0;  // bit pattern 0 = (0.f, 0.f)
-        float axs = 0.f, ays = 0.f;
-        if (t0 + tc * 32 < t1) {
-            float4 cur = fetch(0, 0);
-            for (int k = 0; k < nq; k++) {
-                int s0 = __shfl_sync(0xffffffffu, sbeg, k), s1 = __shfl_sync(0xffffffffu, send, k);
-                int srcl = __shfl_sync(0xffffffffu, sl, k);
-                for (int sc = 0; sc < s1 - s0; sc += 32) {
-                    float4 nxt;
-                    if (sc + 32 < s1 - s0) nxt = fetch(k, sc + 32);
-                    else nxt = (k + 1 < nq) ? fetch(k + 1, 0) : make_float4(0.f, 0.f, 0.f, 0.f);
-                    __syncwarp();
-                    sx[w][lane] = cur.x;
-                    sy[w][lane] = cur.y;
-                    sm[w][lane] = cur.z;
-                    __syncwarp();
-                    int ns = min(32, s1 - s0 - sc);
-                    // four sources kk .. kk+3 on packed FP32
-                    auto quad = [&](int kk) {
-                        float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
-                        float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
-                        float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
-                        uint64_t dx0 = sub2(pk2(X.x, X.y), XI), dy0 = sub2(pk2(Y.x, Y.y), YI);
-                        uint64_t dx1 = sub2(pk2(X.z, X.w), XI), dy1 = sub2(pk2(Y.z, Y.w), YI);
-                        uint64_t r0 = fma2(dx0, dx0, fma2(dy0, dy0, E2));
-                        uint64_t r1 = fma2(dx1, dx1, fma2(dy1, dy1, E2));
-                        float ra, rb;
-                        upk2(r0, ra, rb);
-                        uint64_t i0 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
-                        upk2(r1, ra, rb);
-                        uint64_t i1 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
-                        uint64_t f0 = mul2(pk2(Mq.x, Mq.y), mul2(mul2(i0, i0), i0));
-                        uint64_t f1 = mul2(pk2(Mq.z, Mq.w), mul2(mul2(i1, i1), i1));
-                        AXa = fma2(f0, dx0, AXa);
-                        AYa = fma2(f0, dy0, AYa);
-                        AXb = fma2(f1, dx1, AXb);
-                        AYb = fma2(f1, dy1, AYb);
-                    };
-                    const bool own = srcl == leaf;
-                    int k0 = 0;  // sources below k0 are done
-                    if (!own) {
-                        if (ns == 32) {
+    // one warp per item (a grid-stride loop, launched with one warp for every item)
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
+        int32_t leaf = item_leaf[it];
+        int64_t qb = item_qb[it];
+        int nq = item_nq[it];
+        int32_t t0 = bs[leaf], t1 = be[leaf];
+        double tcx = comx[leaf], tcy = comy[leaf];
+        int sl = lane < nq ? src_idx[qb + lane] : -1;
+        int sbeg = 0, send = 0;
+        float shx = 0.f, shy = 0.f;
+        if (sl >= 0) {
+            sbeg = bs[sl];
+            send = be[sl];
+            shx = (float)(comx[sl] - tcx);
+            shy = (float)(comy[sl] - tcy);
+        }
+        auto fetch = [&](int k, int sc) -> float4 {
+            int s0 = __shfl_sync(0xffffffffu, sbeg, k) + sc, s1 = __shfl_sync(0xffffffffu, send, k);
+            float gx = __shfl_sync(0xffffffffu, shx, k), gy = __shfl_sync(0xffffffffu, shy, k);
+            int j = s0 + lane;
+            float4 v = (j < s1) ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            v.x += gx;
+            v.y += gy;
+            return v;
+        };
+        for (int tc = 0; tc < tchunks; tc++) {
+            int32_t i = t0 + tc * 32 + lane;
+            bool valid = i < t1;
+            float4 me = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            float xi = me.x, yi = me.y;
+            const uint64_t XI = pk2(xi, xi), YI = pk2(yi, yi), E2 = pk2(eps2, eps2);
+            // full 32-source rows: four packed accumulator chains (sources 4q, 4q+1 in
+            // AXa/AYa; 4q+2, 4q+3 in AXb/AYb) so consecutive updates are independent;
+            // the own leaf and partial rows go through the scalar loop into axs/ays
+            uint64_t AXa = 0, AYa = 0, AXb = 0, AYb = 0;  // bit pattern 0 = (0.f, 0.f)
+            float axs = 0.f, ays = 0.f;
+            if (t0 + tc * 32 < t1) {
+                float4 cur = fetch(0, 0);
+                for (int k = 0; k < nq; k++) {
+                    int s0 = __shfl_sync(0xffffffffu, sbeg, k), s1 = __shfl_sync(0xffffffffu, send, k);
+                    int srcl = __shfl_sync(0xffffffffu, sl, k);
+                    for (int sc = 0; sc < s1 - s0; sc += 32) {
+                        float4 nxt;
+                        if (sc + 32 < s1 - s0) nxt = fetch(k, sc + 32);
+                        else nxt = (k + 1 < nq) ? fetch(k + 1, 0) : make_float4(0.f, 0.f, 0.f, 0.f);
+                        __syncwarp();
+                        sx[w][lane] = cur.x;
+                        sy[w][lane] = cur.y;
+                        sm[w][lane] = cur.z;
+                        __syncwarp();
+                        int ns = min(32, s1 - s0 - sc);
+                        // four sources kk .. kk+3 on packed FP32
+                        auto quad = [&](int kk) {
+                            float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
+                            float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
+                            float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
+                            uint64_t dx0 = sub2(pk2(X.x, X.y), XI), dy0 = sub2(pk2(Y.x, Y.y), YI);
+                            uint64_t dx1 = sub2(pk2(X.z, X.w), XI), dy1 = sub2(pk2(Y.z, Y.w), YI);
+                            uint64_t r0 = fma2(dx0, dx0, fma2(dy0, dy0, E2));
+                            uint64_t r1 = fma2(dx1, dx1, fma2(dy1, dy1, E2));
+                            float ra, rb;
+                            upk2(r0, ra, rb);
+                            uint64_t i0 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                            upk2(r1, ra, rb);
+                            uint64_t i1 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                            uint64_t f0 = mul2(pk2(Mq.x, Mq.y), mul2(mul2(i0, i0), i0));
+                            uint64_t f1 = mul2(pk2(Mq.z, Mq.w), mul2(mul2(i1, i1), i1));
+                            AXa = fma2(f0, dx0, AXa);
+                            AYa = fma2(f0, dy0, AYa);
+                            AXb = fma2(f1, dx1, AXb);
+                            AYb = fma2(f1, dy1, AYb);
+                        };
+                        const bool own = srcl == leaf;
+                        int k0 = 0;  // sources below k0 are done
+                        if (!own) {
+                            if (ns == 32) {
 #pragma unroll
-                            for (int kk = 0; kk < 32; kk += 4) quad(kk);
-                            k0 = 32;
-                        } else {
-                            // partial rows (leaves below n_max, or n_max = 16): packed quads, scalar tail
-                            for (k0 = 0; k0 + 4 <= ns; k0 += 4) quad(k0);
+                                for (int kk = 0; kk < 32; kk += 4) quad(kk);
+                                k0 = 32;
+                            } else {
+                                // partial rows (leaves below n_max, or n_max = 16): packed quads, scalar tail
+                                for (k0 = 0; k0 + 4 <= ns; k0 += 4) quad(k0);
+                            }
                         }
+                        for (int kk = k0; kk < ns; kk++) {
+                            float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
+                            float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                            float fk = sm[w][kk] * (ir * ir * ir);
+                            fk = (own && s0 + sc + kk == i) ? 0.f : fk;
+                            axs = fmaf(fk, dx, axs);
+                            ays = fmaf(fk, dy, ays);
+                        }
+                        cur = nxt;
                     }
-                    for (int kk = k0; kk < ns; kk++) {
-                        float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
-                        float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
-                        float fk = sm[w][kk] * (ir * ir * ir);
-                        fk = (own && s0 + sc + kk == i) ? 0.f : fk;
-                        axs = fmaf(fk, dx, axs);
-                        ays = fmaf(fk, dy, ays);
-                    }
-                    cur = nxt;
                 }
             }
+            float a0, a1, a2, a3, b0, b1, b2, b3;
+            upk2(AXa, a0, a1);
+            upk2(AXb, a2, a3);
+            upk2(AYa, b0, b1);
+            upk2(AYb, b2, b3);
+            part[(it * tchunks + tc) * 32 + lane] =
+                make_float2(((a0 + a1) + (a2 + a3)) + axs, ((b0 + b1) + (b2 + b3)) + ays);
         }
-        float a0, a1, a2, a3, b0, b1, b2, b3;
-        upk2(AXa, a0, a1);
-        upk2(AXb, a2, a3);
-        upk2(AYa, b0, b1);
-        upk2(AYb, b2, b3);
-        part[(it * tchunks + tc) * 32 + lane] =
-            make_float2(((a0 + a1) + (a2 + a3)) + axs, ((b0 + b1) + (b2 + b3)) + ays);
     }
 }
 
-// L2P (lib.rs:1321-1345) + the ordered sum of the leaf's P2P partials:  a = -grad(local) + near
+// Sum of a leaf's P2P partials over its items [i0, i1) for one lane: eight independent
+// accumulators so the loads are in flight together (a wide halo leaf can have ~1000
+// items, and a single dependent chain made that one warp the whole kernel's length).
+template <class V, class S>
+__device__ __forceinline__ void sum_items(const V *__restrict__ part, int64_t i0, int64_t i1, int tchunks, int tc,
+                                          int lane, S &sx, S &sy) {
+    S ax[8] = {0, 0, 0, 0, 0, 0, 0, 0}, ay[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int64_t it = i0;
+    for (; it + 8 <= i1; it += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            V v = part[((it + u) * tchunks + tc) * 32 + lane];
+            ax[u] += v.x;
+            ay[u] += v.y;
+        }
+    }
+    for (; it < i1; it++) {
+        V v = part[(it * tchunks + tc) * 32 + lane];
+        ax[0] += v.x;
+        ay[0] += v.y;
+    }
+    sx = ((ax[0] + ax[1]) + (ax[2] + ax[3])) + ((ax[4] + ax[5]) + (ax[6] + ax[7]));
+    sy = ((ay[0] + ay[1]) + (ay[2] + ay[3])) + ((ay[4] + ay[5]) + (ay[6] + ay[7]));
+}
+
 template <int P>
 __global__ void __launch_bounds__(128) k_l2p_reduce64(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
                                                       const double *__restrict__ comx, const double *__restrict__ comy,
@@ -884,14 +915,10 @@ __global__ void __launch_bounds__(128) k_l2p_reduce64(int64_t nl, const double *
         if (i >= t1) continue;
         double fx, fy;
         l2p_eval<P, double>(Lf + leaf * NS, x[i] - comx[leaf], y[i] - comy[leaf], fx, fy);
-        double sx = -fx, sy = -fy;
-        for (int64_t it = i0; it < i1; it++) {
-            double2 v = part[(it * tchunks + tc) * 32 + lane];
-            sx += v.x;
-            sy += v.y;
-        }
-        ax[i] = sx;
-        ay[i] = sy;
+        double sx, sy;
+        sum_items<double2, double>(part, i0, i1, tchunks, tc, lane, sx, sy);
+        ax[i] = sx - fx;
+        ay[i] = sy - fy;
     }
 }
 
@@ -914,12 +941,8 @@ __global__ void __launch_bounds__(128) k_l2p_reduce32(int64_t nl, const float4 *
         float4 me = pos[i];
         float fx, fy;
         l2p_eval<P, float>(Lf + leaf * NS, me.x, me.y, fx, fy);
-        float sx = 0.f, sy = 0.f;
-        for (int64_t it = i0; it < i1; it++) {
-            float2 v = part[(it * tchunks + tc) * 32 + lane];
-            sx += v.x;
-            sy += v.y;
-        }
+        float sx, sy;
+        sum_items<float2, float>(part, i0, i1, tchunks, tc, lane, sx, sy);
         ax[i] = (double)sx - (double)fx;
         ay[i] = (double)sy - (double)fy;
     }
