@@ -49,6 +49,14 @@ def test_invalid_arguments_are_rejected_without_a_device(G):
     assert L.gx_create(C.byref(cfg), C.byref(h)) == 4
     assert L.gx_last_error(None) == b"null context"
     assert L.gx_set_mode(None, 0, 0, 0.5) == 4
+    # entry points beyond the reference's API: null contexts are rejected, no device touched
+    bounds = (C.c_double * 4)(0.0, 1.0, 0.0, 1.0)
+    assert L.gx_rebuild_resident(None, 32, bounds, 0, None) == 4
+    assert L.gx_kdk_run_rebuild(None, 1, 0.1, 0, 1, None, None) == 4
+    assert L.gx_body_ids(None, None) == 4
+    assert L.gx_force_vjp(None, None, None, None, None, None) == 4
+    assert L.gx_rollout_forward(None, 1, 0.1, 1, 0) == 4
+    assert L.gx_rollout_backward(None, *([None] * 10)) == 4
 
 
 def test_no_device_reports_init_failure(G):
