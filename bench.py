@@ -299,9 +299,10 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
 
 
 def run_build_only(args):
-    """Tree construction alone (device Morton keys, radix sort, permutation, leaves and
-    parent rounds) over resident Plummer bodies, a few times: the workload of the tree
-    build profile.  Prints one JSON line with the host-timed rebuilds."""
+    """Tree construction (device Morton keys, radix sort, permutation, leaves and parent
+    rounds) over resident Plummer bodies, then the ACCURATE plan of the new tree, a few
+    times: the workload of the tree-build profile.  Prints one JSON line with the
+    host-timed rebuilds and plans."""
     import galax_gb300 as G
     from galax_gb300 import build as gbuild
     from galax_gb300 import presets
@@ -310,16 +311,24 @@ def run_build_only(args):
     b = presets.plummer(n, seed=args.seed)
     ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=P, eps64=0.1))
     ctx.build_tree(b.copy(), N_MAX, presets.BOUNDS["plummer"])
-    times = []
+    ctx.set_params(P, presets.cli_softening(b.x, b.y))
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
+    times, plan = [], []
     for _ in range(max(1, args.steps)):
         ctx.upload_bodies(b)  # unsorted order again: the sort does full work
         t0 = time.perf_counter()
         ctx.rebuild_resident(N_MAX, presets.BOUNDS["plummer"])
-        times.append(time.perf_counter() - t0)
+        t1 = time.perf_counter()
+        ctx.forces_resident()  # the ACCURATE plan of the new tree, then one evaluation
+        t2 = time.perf_counter()
+        ctx.forces_resident()
+        t3 = time.perf_counter()
+        times.append(t1 - t0)
+        plan.append((t2 - t1) - (t3 - t2))
     nn, nl, lv, _ = ctx.tree_info()
     ctx.close()
     print(json.dumps({"build_only": True, "n": n, "nodes": nn, "leaves": nl, "levels": lv,
-                      "ms": [t * 1e3 for t in times]}), flush=True)
+                      "build_ms": [t * 1e3 for t in times], "plan_ms": [t * 1e3 for t in plan]}), flush=True)
     return 0
 
 
