@@ -193,9 +193,13 @@ int gx_force_vjp(gx_ctx *ctx, const double *lam_x, const double *lam_y, double *
 int gx_rollout_forward(gx_ctx *ctx, int64_t n_steps, double dt, int64_t checkpoint_every,
                        int64_t rebuild_every);
 /* Reverse leapfrog of the last gx_rollout_forward: given dL/d(x, y, vx, vy) at the
- * final step, returns dL/d(x, y, vx, vy) at step 0 and dL/dm.  Segments between
- * checkpoints are recomputed (deterministically, so bit for bit); *peak_bytes (may be
- * NULL) receives the device bytes of the checkpoint, segment and adjoint buffers. */
+ * final step (host arrays in the final body order), returns dL/d(x, y, vx, vy) at
+ * step 0 and dL/dm, in the body order at the start of the rollout.  Segments between
+ * checkpoints are recomputed (deterministically, so bit for bit); under the rebuild
+ * policy every step's tree is rebuilt, bit-identically, and the cotangents are carried
+ * back through each rebuild's permutation.  The resident bodies are left at an
+ * intermediate state.  *peak_bytes (may be NULL) receives the device bytes of the
+ * checkpoint, segment, permutation and adjoint buffers. */
 int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const double *lvx, const double *lvy,
                         double *gx0, double *gy0, double *gvx0, double *gvy0, double *gm, int64_t *peak_bytes);
 
