@@ -101,6 +101,7 @@ struct gx_ctx {
     DevBuf ref_G;                    // n_keys x (2p+1)^2 doubles
     int64_t n_ref_keys = 0, n_v_pairs = 0;
     DevBuf radius;                   // accurate mode node radii
+    DevBuf radius32;                 // the radii rounded to FP32 (MAC operands)
     DevBuf anc;                      // per leaf, its ancestor at every level (level-major), -1 above the root
     DevBuf has_far_ref, has_far_acc; // per node: 1 if its M2L list is non-empty
     DevBuf comhl;                    // per node COM as FP32 (x_hi, x_lo, y_hi, y_lo)

@@ -409,15 +409,24 @@ __global__ void k_radius_parents(int64_t s, int64_t e, const int4 *child, const 
     R[q] = r;
 }
 
-// Far when |com_a - com_b| theta > R_a + R_b, compared squared (no square root: FP64
-// is slow on this part and the plan tests ~10^8 pairs), each operation separately
-// rounded so the oracle's decision is the same bit for bit.
-__device__ __forceinline__ bool mac_far(const double *comx, const double *comy, const double *R, int64_t a, int64_t b,
-                                        double theta2) {
-    double ex = __dsub_rn(comx[a], comx[b]), ey = __dsub_rn(comy[a], comy[b]);
-    double d2 = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
-    double s = __dadd_rn(R[a], R[b]);
-    return __dmul_rn(d2, theta2) > __dmul_rn(s, s);
+// Far when |com_a - com_b| theta > R_a + R_b, decided in FP32 and compared squared:
+// the COM offset from the FP32 (hi, lo) split of each COM, the radii rounded to FP32
+// once.  FP64 throughput on this part is a small fraction of FP32 and the plan tests
+// ~10^8 pairs at 1M bodies; every operation is separately rounded so the oracle's
+// decision is the same bit for bit.
+__device__ __forceinline__ bool mac_far(const float4 *__restrict__ hl, const float *__restrict__ R32, int64_t a,
+                                        int64_t b, float theta2) {
+    const float4 A = hl[a], B = hl[b];
+    const float ex = __fadd_rn(__fsub_rn(A.x, B.x), __fsub_rn(A.y, B.y));
+    const float ey = __fadd_rn(__fsub_rn(A.z, B.z), __fsub_rn(A.w, B.w));
+    const float d2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+    const float s = __fadd_rn(R32[a], R32[b]);
+    return __fmul_rn(d2, theta2) > __fmul_rn(s, s);
+}
+
+__global__ void k_to_f32(int64_t n, const double *in, float *out) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (float)in[i];
 }
 
 // Per node x of a level: children of Near(parent(x)) split into far (M2L) and near,
@@ -448,7 +457,7 @@ __global__ void k_mac_units(int64_t s, int64_t e, const int64_t *uoff, int32_t *
 
 // pass 0: per-unit counts (ufar, unear); pass 1: write at the per-unit offsets
 __global__ void k_mac(int64_t n_units, int pass, const int32_t *unode, const int32_t *uchunk, const int32_t *parent,
-                      const int4 *child, const double *comx, const double *comy, const double *R, double theta2,
+                      const int4 *child, const float4 *hl, const float *R32, float theta2,
                       const int64_t *near_start, const int32_t *near_cnt, const int32_t *near_idx_in, int64_t *ufar,
                       int64_t *unear, int32_t *far_idx, int32_t *near_idx) {
     const unsigned full = 0xffffffffu;
@@ -473,7 +482,7 @@ __global__ void k_mac(int64_t n_units, int pass, const int32_t *unode, const int
             cc[3] = c4.w;
             for (int k = 0; k < 4; k++) {
                 if (cc[k] < 0) continue;
-                if (mac_far(comx, comy, R, x, cc[k], theta2)) fm |= 1u << k;
+                if (mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
                 else nm |= 1u << k;
             }
         }
@@ -857,7 +866,13 @@ int gx_plan_accurate(gx_ctx *ctx) {
     GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
     GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
                                  ctx->stream));
-    const double theta2 = ctx->theta * ctx->theta;
+    // FP32 MAC operands: (hi, lo) COMs (built with the tree aux) and radii rounded once
+    const float thf = (float)ctx->theta;
+    const float theta2 = thf * thf;
+    GX_TRY(gx_ensure(ctx, ctx->radius32, sizeof(float) * (size_t)nn));
+    float *R32 = dptr<float>(ctx->radius32);
+    k_to_f32<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, R, R32);
+    const float4 *hl = dptr<float4>(ctx->comhl);
     for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
         const int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
         // units: chunks of each node's candidate list
@@ -881,8 +896,8 @@ int gx_plan_accurate(gx_ctx *ctx) {
         const unsigned gu = (unsigned)((U * 32 + 127) / 128);
         if (U > 0)
             k_mac<<<gu, 128, 0, ctx->stream>>>(U, 0, unode, uchunk, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
-                                               dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, theta2, nstart,
-                                               ncnt, dptr<int32_t>(ctx->near_idx), ufar, unear, nullptr, nullptr);
+                                               hl, R32, theta2, nstart, ncnt, dptr<int32_t>(ctx->near_idx), ufar,
+                                               unear, nullptr, nullptr);
         GX_TRY(gx_exclusive_scan_i64(ctx, ufar, ufo, U + 1));
         GX_TRY(gx_exclusive_scan_i64(ctx, unear, uno, U + 1));
         int64_t ft = 0, nt = 0;
@@ -910,9 +925,8 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_TRY(gx_add_offsets(ctx, uno, unear, U, near_tot));
         if (U > 0)
             k_mac<<<gu, 128, 0, ctx->stream>>>(U, 1, unode, uchunk, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
-                                               dptr<double>(ctx->comx), dptr<double>(ctx->comy), R, theta2, nstart,
-                                               ncnt, dptr<int32_t>(ctx->near_idx), ufar, unear,
-                                               dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx));
+                                               hl, R32, theta2, nstart, ncnt, dptr<int32_t>(ctx->near_idx), ufar,
+                                               unear, dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx));
         k_mac_node_lists<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, ufo, uno, far_tot, near_tot, fstart,
                                                                      fcnt, nstart, ncnt);
         ctx->launches += 9;

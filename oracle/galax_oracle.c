@@ -1384,12 +1384,16 @@ static void iv_push(ivec *a, int32_t x) {
     a->v[a->n++] = x;
 }
 
-/* far when |com_a - com_b| theta > R_a + R_b, compared squared (the device plan does
- * the same operations, each rounded once: -ffp-contract=off) */
-static int mac_far(const gxo_tree *t, const double *R, int64_t a, int64_t b, double theta2) {
-    double ex = t->comx[a] - t->comx[b], ey = t->comy[a] - t->comy[b];
-    double d2 = ex * ex + ey * ey;
-    double s = R[a] + R[b];
+/* far when |com_a - com_b| theta > R_a + R_b, decided in float and compared squared:
+ * the COM offset from the float (hi, lo) split of each COM (hi = (float)c,
+ * lo = (float)(c - hi)), the radii rounded to float once -- the device plan does the
+ * same separately rounded float operations (-ffp-contract=off here) */
+typedef struct { float xh, xl, yh, yl; } hl4;
+static int mac_far(const hl4 *hl, const float *R32, int64_t a, int64_t b, float theta2) {
+    float ex = (hl[a].xh - hl[b].xh) + (hl[a].xl - hl[b].xl);
+    float ey = (hl[a].yh - hl[b].yh) + (hl[a].yl - hl[b].yl);
+    float d2 = ex * ex + ey * ey;
+    float s = R32[a] + R32[b];
     return d2 * theta2 > s * s;
 }
 
@@ -1403,7 +1407,18 @@ void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_c
     ivec *fv = (ivec *)calloc((size_t)(nn > 0 ? nn : 1), sizeof(ivec));
     ivec *nv = (ivec *)calloc((size_t)(nn > 0 ? nn : 1), sizeof(ivec));
     if (nn > 0) iv_push(&nv[nn - 1], (int32_t)(nn - 1)); /* the root is near itself */
-    const double theta2 = theta * theta;
+    const float thf = (float)theta;
+    const float theta2 = thf * thf;
+    hl4 *hl = (hl4 *)malloc(sizeof(hl4) * (size_t)(nn > 0 ? nn : 1));
+    float *R32 = (float *)malloc(sizeof(float) * (size_t)(nn > 0 ? nn : 1));
+    for (int64_t i = 0; i < nn; i++) {
+        float xh = (float)t->comx[i], yh = (float)t->comy[i];
+        hl[i].xh = xh;
+        hl[i].xl = (float)(t->comx[i] - (double)xh);
+        hl[i].yh = yh;
+        hl[i].yl = (float)(t->comy[i] - (double)yh);
+        R32[i] = (float)R[i];
+    }
     for (int64_t id = nn - 1; id >= 0; id--) {
         int32_t P = t->parent[id];
         if (P < 0) continue;
@@ -1412,7 +1427,7 @@ void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_c
             for (int k = 0; k < 4; k++) {
                 int32_t c = t->child[4 * y + k];
                 if (c < 0) continue;
-                if (mac_far(t, R, id, c, theta2)) iv_push(&fv[id], c);
+                if (mac_far(hl, R32, id, c, theta2)) iv_push(&fv[id], c);
                 else iv_push(&nv[id], c);
             }
         }
@@ -1433,6 +1448,8 @@ void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_c
     free(fv); free(nv);
     *far_out = far;
     *near_out = near;
+    free(hl);
+    free(R32);
 }
 
 void gxo_compute_fmm_force_mac(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
