@@ -302,7 +302,7 @@ def run_build_only(args):
     """Tree construction (device Morton keys, radix sort, permutation, leaves and parent
     rounds) over resident Plummer bodies, then the ACCURATE plan of the new tree, a few
     times: the workload of the tree-build profile.  Prints one JSON line with the
-    host-timed rebuilds and plans."""
+    host-timed rebuilds and plans, and the REF form's lists and plan on the last tree."""
     import galax_gb300 as G
     from galax_gb300 import build as gbuild
     from galax_gb300 import presets
@@ -325,10 +325,19 @@ def run_build_only(args):
         t3 = time.perf_counter()
         times.append(t1 - t0)
         plan.append((t2 - t1) - (t3 - t2))
+    # REF form on the last tree: its V/U lists, P2P gather lists and derivative plan
+    ctx.set_mode(G.MODE_REF, G.PREC_FP64, THETA)
+    t0 = time.perf_counter()
+    ctx.forces_resident()
+    t1 = time.perf_counter()
+    ctx.forces_resident()
+    t2 = time.perf_counter()
+    ref_plan = (t1 - t0) - (t2 - t1)
     nn, nl, lv, _ = ctx.tree_info()
     ctx.close()
     print(json.dumps({"build_only": True, "n": n, "nodes": nn, "leaves": nl, "levels": lv,
-                      "build_ms": [t * 1e3 for t in times], "plan_ms": [t * 1e3 for t in plan]}), flush=True)
+                      "build_ms": [t * 1e3 for t in times], "plan_ms": [t * 1e3 for t in plan],
+                      "ref_plan_ms": ref_plan * 1e3, "ref_eval_ms": (t2 - t1) * 1e3}), flush=True)
     return 0
 
 

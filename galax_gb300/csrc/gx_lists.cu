@@ -248,39 +248,59 @@ __global__ void k_ulist(Level lv0, const double *cx, const double *cy, const dou
     ulen[a] = (uint8_t)len;
 }
 
-// REF P2P gather lists: per receiving leaf a, {a} then ascending b with
-// (b > a and b in U(a)) or (b < a and a in U(b)).
-__global__ void k_p2p_gather(Level lv0, const double *cx, const double *cy, const double *hw, const uint32_t *udata,
-                             const uint8_t *ulen, int pass, int32_t *cnt, const int64_t *off, int32_t *out,
-                             unsigned *status) {
-    int64_t a = lv0.s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= lv0.e) return;
-    int64_t base = pass ? off[a] : 0;
-    int32_t c = 0;
-    if (pass) out[base] = (int32_t)a;
-    c = 1;
-    int ua = ulen[a];
-    double x0, x1, y0, y1;
-    bool fin;
-    qbox(cx, cy, hw, a, lv0, x0, x1, y0, y1, fin);
-    bool ok = level_query(lv0, cx, cy, hw, x0, x1, y0, y1, fin, [&](int64_t b) {
-        if (b == a) return;
-        bool take = false;
-        if (b > a) {
-            for (int k = 1; k < ua; k++)
-                if (udata[a * GX_LIST_CAP + k] == (uint32_t)b) { take = true; break; }
-        } else {
-            int ub = ulen[b];
-            for (int k = 1; k < ub; k++)
-                if (udata[b * GX_LIST_CAP + k] == (uint32_t)a) { take = true; break; }
+// REF P2P gather lists (the ownership rule of p2p, lib.rs:1395-1462): per receiving
+// leaf a, {a} then ascending b with (b > a and b in U(a)) or (b < a and a in U(b)).
+// Built by inverting the U-lists instead of searching geometry: every entry y of U(x)
+// with y > x gives the pairs (receiver x, source y) and (receiver y, source x); a sort
+// of the (receiver, source) keys orders each receiver's sources ascending.
+__global__ void k_gather_count(int64_t nl, const uint32_t *udata, const uint8_t *ulen, int64_t *cnt) {
+    int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nl) return;
+    int64_t c = 0;
+    for (int k = 1; k < ulen[x]; k++)
+        if ((int64_t)udata[x * GX_LIST_CAP + k] > x) c += 2;
+    cnt[x] = c;
+}
+
+__global__ void k_gather_emit(int64_t nl, const uint32_t *udata, const uint8_t *ulen, const int64_t *off,
+                              uint64_t *keys) {
+    int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nl) return;
+    int64_t o = off[x];
+    for (int k = 1; k < ulen[x]; k++) {
+        uint64_t y = udata[x * GX_LIST_CAP + k];
+        if ((int64_t)y > x) {
+            keys[o++] = ((uint64_t)x << 32) | y;
+            keys[o++] = (y << 32) | (uint64_t)x;
         }
-        if (take) {
-            if (pass) out[base + c] = (int32_t)b;
-            c++;
+    }
+}
+
+// per receiver: its range in the sorted keys (binary search) and list length 1 + range
+__global__ void k_gather_ranges(int64_t nl, const uint64_t *keys, int64_t nk, int64_t *kstart, int64_t *len) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nl) return;
+    auto lower = [&](uint64_t v) {
+        int64_t lo = 0, hi = nk;
+        while (lo < hi) {
+            int64_t mid = (lo + hi) >> 1;
+            if (keys[mid] < v) lo = mid + 1;
+            else hi = mid;
         }
-    });
-    if (!ok) atomicOr(status, GX_DEV_STACK_OVERFLOW);
-    if (!pass) cnt[a] = c;
+        return lo;
+    };
+    int64_t s = lower((uint64_t)a << 32), e = lower((uint64_t)(a + 1) << 32);
+    kstart[a] = s;
+    len[a] = 1 + (e - s);
+}
+
+__global__ void k_gather_fill(int64_t nl, const uint64_t *keys, const int64_t *kstart, const int64_t *off,
+                              int32_t *out) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nl) return;
+    int64_t o = off[a], n = off[a + 1] - o;
+    out[o] = (int32_t)a;
+    for (int64_t k = 1; k < n; k++) out[o + k] = (int32_t)(uint32_t)keys[kstart[a] + k - 1];
 }
 
 // Rust `f64 as i64`
@@ -720,36 +740,48 @@ int gx_plan_ref(gx_ctx *ctx) {
     int64_t nn = ctx->n_nodes;
     ctx->plan_ref_valid = false;
     if (nn == 0) { ctx->plan_ref_valid = true; return GX_OK; }
-    const double *cx = dptr<double>(ctx->cx), *cy = dptr<double>(ctx->cy), *hw = dptr<double>(ctx->hw);
     GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
     // ---- P2P gather lists
     int64_t nl = ctx->level_start[1];
-    GX_TRY(gx_ensure(ctx, ctx->scratch_a, bvh_bytes(nl)));
-    Level L0;
-    size_t used = 0;
-    GX_TRY(build_level(ctx, 0, nl, ctx->scratch_a, 0, L0, &used));
-    GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int32_t) * (size_t)(nl + 1)));
-    GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nl + 1)));
-    GX_TRY(gx_ensure(ctx, ctx->p2p_off, sizeof(int64_t) * (size_t)(nl + 1)));
-    int32_t *cnt = dptr<int32_t>(ctx->scratch_b);
-    int64_t *cnt64 = dptr<int64_t>(ctx->scratch_c);
-    int64_t *off = dptr<int64_t>(ctx->p2p_off);
-    k_p2p_gather<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(L0, cx, cy, hw, dptr<uint32_t>(ctx->udata),
-                                                             dptr<uint8_t>(ctx->ulen), 0, cnt, nullptr, nullptr,
-                                                             dptr<unsigned>(ctx->status));
-    GX_CUDA(ctx, cudaMemsetAsync(cnt64 + nl, 0, sizeof(int64_t), ctx->stream));
-    k_i32_to_i64<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(cnt, cnt64, nl);
-    GX_TRY(gx_exclusive_scan_i64(ctx, cnt64, off, nl + 1));
-    int64_t tot = 0;
-    GX_CUDA(ctx, cudaMemcpyAsync(&tot, off + nl, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
-    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    GX_TRY(gx_ensure(ctx, ctx->p2p_idx, sizeof(int32_t) * (size_t)(tot + 1)));
-    k_p2p_gather<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(L0, cx, cy, hw, dptr<uint32_t>(ctx->udata),
-                                                             dptr<uint8_t>(ctx->ulen), 1, cnt, off,
-                                                             dptr<int32_t>(ctx->p2p_idx), dptr<unsigned>(ctx->status));
-    ctx->launches += 3;
-    ctx->n_p2p_pairs = tot;
-    GX_CUDA(ctx, cudaGetLastError());
+    {
+        GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nl + 1) * 2));
+        int64_t *cnt = dptr<int64_t>(ctx->scratch_c), *eoff = cnt + (nl + 1);
+        GX_CUDA(ctx, cudaMemsetAsync(cnt + nl, 0, sizeof(int64_t), ctx->stream));
+        k_gather_count<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, dptr<uint32_t>(ctx->udata),
+                                                                    dptr<uint8_t>(ctx->ulen), cnt);
+        GX_TRY(gx_exclusive_scan_i64(ctx, cnt, eoff, nl + 1));
+        int64_t nk = 0;
+        GX_CUDA(ctx, cudaMemcpyAsync(&nk, eoff + nl, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        // keys and their sort buffers: scratch_a (keys, alt), scratch_b (values, alt)
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(uint64_t) * (size_t)(nk + 1) * 2));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(uint32_t) * (size_t)(nk + 1) * 2));
+        uint64_t *keys = dptr<uint64_t>(ctx->scratch_a), *keys_alt = keys + (nk + 1);
+        uint32_t *vals = dptr<uint32_t>(ctx->scratch_b), *vals_alt = vals + (nk + 1);
+        k_gather_emit<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, dptr<uint32_t>(ctx->udata),
+                                                                   dptr<uint8_t>(ctx->ulen), eoff, keys);
+        int top = 1;
+        while (top < 63 && ((int64_t)1 << top) <= nl) top++;
+        bool alt = false;
+        GX_TRY(gx_radix_sort_u64(ctx, keys, vals, nk, 0, 32 + top, keys_alt, vals_alt, &alt));
+        const uint64_t *sk = alt ? keys_alt : keys;
+        // per receiver: key range, list length, offsets, fill
+        GX_TRY(gx_ensure(ctx, ctx->scratch_d, sizeof(int64_t) * (size_t)(nl + 1) * 2));
+        int64_t *kstart = dptr<int64_t>(ctx->scratch_d), *len = kstart + (nl + 1);
+        GX_CUDA(ctx, cudaMemsetAsync(len + nl, 0, sizeof(int64_t), ctx->stream));
+        k_gather_ranges<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, sk, nk, kstart, len);
+        GX_TRY(gx_ensure(ctx, ctx->p2p_off, sizeof(int64_t) * (size_t)(nl + 1)));
+        int64_t *off = dptr<int64_t>(ctx->p2p_off);
+        GX_TRY(gx_exclusive_scan_i64(ctx, len, off, nl + 1));
+        int64_t tot = 0;
+        GX_CUDA(ctx, cudaMemcpyAsync(&tot, off + nl, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        GX_TRY(gx_ensure(ctx, ctx->p2p_idx, sizeof(int32_t) * (size_t)(tot + 1)));
+        k_gather_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, sk, kstart, off, dptr<int32_t>(ctx->p2p_idx));
+        ctx->launches += 6;
+        ctx->n_p2p_pairs = tot;
+        GX_CUDA(ctx, cudaGetLastError());
+    }
 
     // ---- REF derivative plan
     GX_TRY(gx_ensure(ctx, ctx->ref_voff, sizeof(int64_t) * (size_t)(nn + 1)));  // V pair offsets per node
