@@ -47,10 +47,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FMM bodies/s (1M, p=4) mixed vs FP64 at equal force error; adjoint/fwd time"
 N_DEFAULT = 1_000_000
-# DRAM bytes (read 46.86 MB + written 19.06 MB) of one k_p2p32_items launch at the
+# DRAM bytes (read 46.92 MB + written 20.25 MB) of one k_p2p32_rows launch at the
 # default workload, from the one-pass ncu capture summarised in
-# profiles/k_p2p32_items_plummer200k.md (the kernel works out of L2)
-P2P_TRAFFIC_1M = 65.92e6
+# profiles/k_p2p32_rows_plummer200k.md (the kernel works out of L2)
+P2P_TRAFFIC_1M = 67.17e6
 P, N_MAX, THETA = 4, 32, 0.5
 
 
@@ -507,7 +507,7 @@ def run_ours(args, rank, world, local, pg):
                 "d2h_bytes_per_step": 2 * 8 * n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32 if peak32 else None, "traffic": P2P_TRAFFIC_1M if n == N_DEFAULT else None,
-                     "kernel": "k_p2p32_items (P2P, packed FP32; timed on its own stream while it shares the SMs "
+                     "kernel": "k_p2p32_rows (P2P, packed FP32; timed on its own stream while it shares the SMs "
                                "with M2L)",
                      "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)",
                      "evaluation_tflops": eval_tflops, "evaluation_frac": eval_tflops / peak32 if peak32 else None},

@@ -144,21 +144,28 @@ __global__ void __launch_bounds__(128) k_adj_l2l_up(int64_t s, int64_t e, const 
 // ---- A3: M2L^T as a gather over far(s) (far lists are symmetric):
 //   dM[s][S] = -(-1)^|S| sum_{t in far(s)} sum_T A(com_t - com_s)[S+T] dL[t][T] / T!
 // The FP32 form forms com_t - com_s from the FP32 (hi, lo) COMs exactly as the
-// forward M2L forms it for the pair (t, s).
+// forward M2L forms it for the pair (t, s).  Work units as in the forward M2L (far
+// lists cut into pieces of at most GX_M2L_UNIT entries, one warp each); a node with
+// one unit writes dM directly, otherwise k_adj_m2l_combine sums the units' partials
+// in unit order.  Nodes without far entries are not written: has_far = 0 keeps A4
+// from reading them.
 template <int P, class T>
 __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1)
-    k_adj_m2l(int64_t nn, const int32_t *__restrict__ idx, const int64_t *__restrict__ start,
-              const int32_t *__restrict__ cnt, const double *__restrict__ comx, const double *__restrict__ comy,
-              const float4 *__restrict__ comhl, double eps2d, const T *__restrict__ dL, T *__restrict__ dM) {
+    k_adj_m2l(int64_t n_units, const int32_t *__restrict__ unode, const int64_t *__restrict__ ustart,
+              const int32_t *__restrict__ ulen, const int64_t *__restrict__ node_u, const int32_t *__restrict__ idx,
+              const double *__restrict__ comx, const double *__restrict__ comy, const float4 *__restrict__ comhl,
+              double eps2d, const T *__restrict__ dL, T *__restrict__ dM, T *__restrict__ part) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
     const int NCr = (PP + 1) * (PP + 2) / 2;
-    int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int lane = threadIdx.x & 31;
-    if (node >= nn) return;
-    int64_t st = start[node];
-    int len = cnt[node];
+    if (u >= n_units) return;
+    const int64_t node = unode[u];
+    const bool single = node_u[node + 1] - node_u[node] == 1;
+    const int64_t st = ustart[u];
+    const int len = ulen[u];
     double scx = comx[node], scy = comy[node];
     float4 shl = make_float4(0.f, 0.f, 0.f, 0.f);
     if constexpr (sizeof(T) == 4) shl = comhl[node];
@@ -193,8 +200,31 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1)
         for (int sj = 0; sj <= PP - si; sj++) {
             int k = gx_mi(si, sj);
             T v = warp_sum_t<T>(acc[k]);
-            if (lane == (k & 31)) dM[node * NS + k] = ((si + sj) & 1) ? v : -v;
+            if (lane == (k & 31)) {
+                if (single) dM[node * NS + k] = ((si + sj) & 1) ? v : -v;
+                else part[u * NS + k] = v;
+            }
         }
+}
+
+template <int P, class T>
+__global__ void k_adj_m2l_combine(int64_t nn, const int64_t *__restrict__ node_u, const T *__restrict__ part,
+                                  T *__restrict__ dM) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t node = t / NC;
+    int k = (int)(t - node * NC);
+    if (node >= nn || k >= NCr) return;
+    int64_t u0 = node_u[node], u1 = node_u[node + 1];
+    if (u1 - u0 < 2) return;
+    T s = T(0);
+    for (int64_t u = u0; u < u1; u++) s += part[u * NS + k];
+    int n = 0;  // coefficient k = gx_mi(si, sj) with si + sj = n
+    while ((n + 1) * (n + 2) / 2 <= k) n++;
+    dM[node * NS + k] = (n & 1) ? s : -s;
 }
 
 // ---- A4: M2M^T straight to the leaves: the moments of an ancestor a are the leaf's
@@ -556,10 +586,16 @@ int run_force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf_
         k_adj_l2l_up<P, T><<<gx_blocks(e - s, 128), 128, 0, st>>>(s, e, child, comx, comy, dL);
     }
     // A3: M2L^T
-    const int64_t *fs = dptr<int64_t>(ctx->far_off);
-    k_adj_m2l<P, T><<<(unsigned)((nn * 32 + 127) / 128), 128, 0, st>>>(
-        nn, dptr<int32_t>(ctx->far_idx), fs, reinterpret_cast<const int32_t *>(fs + nn), comx, comy,
-        F32 ? dptr<float4>(ctx->comhl) : nullptr, eps2, dL, dM);
+    const gx_ctx::M2LUnits &U = ctx->m2l_units;
+    if (U.n > 0) {
+        const int64_t *node_u = dptr<int64_t>(U.node_u);
+        GX_TRY(gx_ensure(ctx, ctx->m2l_part, sizeof(T) * NS * (size_t)(U.n + 1)));
+        k_adj_m2l<P, T><<<(unsigned)((U.n * 32 + 127) / 128), 128, 0, st>>>(
+            U.n, dptr<int32_t>(U.node), dptr<int64_t>(U.start), dptr<int32_t>(U.len), node_u,
+            dptr<int32_t>(ctx->far_idx), comx, comy, F32 ? dptr<float4>(ctx->comhl) : nullptr, eps2, dL, dM,
+            dptr<T>(ctx->m2l_part));
+        k_adj_m2l_combine<P, T><<<gx_blocks(nn * NC, 256), 256, 0, st>>>(nn, node_u, dptr<T>(ctx->m2l_part), dM);
+    }
     // A4: M2M^T to the leaves
     k_adj_m2m_direct<P, T><<<gw, 128, 0, st>>>(nl, ctx->n_levels, dptr<int32_t>(ctx->anc),
                                                dptr<uint8_t>(ctx->has_far_acc), comx, comy, dM, dMl);

@@ -463,32 +463,16 @@ __global__ void __launch_bounds__(128) k_m2l_ref(int64_t nn, const uint32_t *__r
         }
 }
 
-// EXACT / ACCURATE: per-pair derivatives.  Lists given as start/count per node.
+// EXACT / ACCURATE M2L of one target over its sources idx[st .. st + len): lane l takes
+// sources l, l + 32, ...; acc holds the lane's unscaled sum over M'[S] A[S+T].
 template <int P, class T, class IDX>
-// FP32 at p <= 4 fits 64 registers without spills: 8 blocks (32 warps) per SM
-__global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l_exact(int64_t nn, const IDX *__restrict__ idx,
-                                                   const int64_t *__restrict__ start, const int32_t *__restrict__ cnt,
-                                                   const uint8_t *__restrict__ cnt8, int64_t fixed_stride,
-                                                   const double *__restrict__ comx, const double *__restrict__ comy,
-                                                   const float4 *__restrict__ comhl, double eps2d,
-                                                   const T *__restrict__ M, T *__restrict__ L) {
+__device__ __forceinline__ void m2l_sources(const IDX *__restrict__ idx, int64_t st, int len, int lane, double tcx,
+                                            double tcy, float4 thl, const double *__restrict__ comx,
+                                            const double *__restrict__ comy, const float4 *__restrict__ comhl, T eps2,
+                                            const T *__restrict__ M, T *acc) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
-    const int NCr = (PP + 1) * (PP + 2) / 2;
-    (void)NCr;
-    int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (node >= nn) return;
-    int64_t st = start ? start[node] : node * fixed_stride;
-    int len = cnt ? cnt[node] : (int)cnt8[node];
-    double tcx = comx[node], tcy = comy[node];
-    float4 thl = make_float4(0.f, 0.f, 0.f, 0.f);
-    if constexpr (sizeof(T) == 4) thl = comhl[node];
-    T eps2 = (T)eps2d;
-    T acc[NC];
-#pragma unroll
-    for (int k = 0; k < NCr; k++) acc[k] = T(0);
     // the next source index is fetched one iteration ahead, and the source row is
     // requested before the derivatives are formed, so both latencies overlap compute
     int64_t src = lane < len ? (int64_t)idx[st + lane] : 0;
@@ -516,6 +500,33 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l
         m2l_fused<P, T>(dx, dy, eps2, ms, acc);
         src = nsrc;
     }
+}
+
+// EXACT / ACCURATE: per-pair derivatives.  Lists given as start/count per node.
+template <int P, class T, class IDX>
+// FP32 at p <= 4 fits 64 registers without spills: 8 blocks (32 warps) per SM
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l_exact(int64_t nn, const IDX *__restrict__ idx,
+                                                   const int64_t *__restrict__ start, const int32_t *__restrict__ cnt,
+                                                   const uint8_t *__restrict__ cnt8, int64_t fixed_stride,
+                                                   const double *__restrict__ comx, const double *__restrict__ comy,
+                                                   const float4 *__restrict__ comhl, double eps2d,
+                                                   const T *__restrict__ M, T *__restrict__ L) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
+    int64_t node = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (node >= nn) return;
+    int64_t st = start ? start[node] : node * fixed_stride;
+    int len = cnt ? cnt[node] : (int)cnt8[node];
+    float4 thl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (sizeof(T) == 4) thl = comhl[node];
+    T acc[NC];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) acc[k] = T(0);
+    m2l_sources<P, T, IDX>(idx, st, len, lane, comx[node], comy[node], thl, comx, comy, comhl, (T)eps2d, M, acc);
     // G = -A: L[T] = -(1/T!) sum_S M'[S] A[S+T]
 #pragma unroll
     for (int oi = 0; oi <= PP; oi++)
@@ -525,6 +536,70 @@ __global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l
             T v = warp_sum_t<T>(acc[k]);
             if (lane == (k & 31)) L[node * NS + k] = v * -tab_ifp<T>(oi, oj);
         }
+}
+
+// ACCURATE M2L over work units: every far list is cut into units of at most
+// GX_M2L_UNIT sources (one warp each), so a node near the centre of a wide halo, with
+// tens of thousands of far sources, is spread over many warps instead of running as
+// one straggler.  A node with one unit writes its local directly; otherwise each unit
+// writes its warp-reduced partial and k_m2l_combine sums them in unit order.
+template <int P, class T>
+__global__ void __launch_bounds__(128, (sizeof(T) == 4 && P <= 4) ? 8 : 1) k_m2l_units(
+    int64_t n_units, const int32_t *__restrict__ unode, const int64_t *__restrict__ ustart,
+    const int32_t *__restrict__ ulen, const int64_t *__restrict__ node_u, const int32_t *__restrict__ idx,
+    const double *__restrict__ comx, const double *__restrict__ comy, const float4 *__restrict__ comhl, double eps2d,
+    const T *__restrict__ M, T *__restrict__ L, T *__restrict__ part) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
+    int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (u >= n_units) return;
+    const int64_t node = unode[u];
+    const bool single = node_u[node + 1] - node_u[node] == 1;
+    float4 thl = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (sizeof(T) == 4) thl = comhl[node];
+    T acc[NC];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) acc[k] = T(0);
+    m2l_sources<P, T, int32_t>(idx, ustart[u], ulen[u], lane, comx[node], comy[node], thl, comx, comy, comhl,
+                               (T)eps2d, M, acc);
+#pragma unroll
+    for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+        for (int oj = 0; oj <= PP - oi; oj++) {
+            int k = gx_mi(oi, oj);
+            T v = warp_sum_t<T>(acc[k]);
+            if (lane == (k & 31)) {
+                if (single) L[node * NS + k] = v * -tab_ifp<T>(oi, oj);
+                else part[u * NS + k] = v;
+            }
+        }
+}
+
+// Nodes cut into several M2L units: the local is the sum of the units' partials in
+// unit order.  One thread per (node, coefficient).
+template <int P, class T>
+__global__ void k_m2l_combine(int64_t nn, const int64_t *__restrict__ node_u, const T *__restrict__ part,
+                              T *__restrict__ L) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t node = t / NC;
+    int k = (int)(t - node * NC);
+    if (node >= nn || k >= NCr) return;
+    int64_t u0 = node_u[node], u1 = node_u[node + 1];
+    if (u1 - u0 < 2) return;
+    T s = T(0);
+    for (int64_t u = u0; u < u1; u++) s += part[u * NS + k];
+    int n = 0;  // coefficient k = gx_mi(oi, oj): n(n+1)/2 + oj with n = oi + oj
+    while ((n + 1) * (n + 2) / 2 <= k) n++;
+    const int oj = k - n * (n + 1) / 2, oi = n - oj;
+    L[node * NS + k] = s * -tab_ifp<T>(oi, oj);
 }
 
 // ---------------------------------------------------------------- L2L
@@ -1157,11 +1232,18 @@ int run_forces(gx_ctx *ctx, bool timed) {
                                              dptr<double>(ctx->ref_G), reinterpret_cast<const double *>(M),
                                              reinterpret_cast<double *>(L));
         } else if (mode == GX_MODE_ACCURATE) {
-            const int64_t *fs = dptr<int64_t>(ctx->far_off);
-            k_m2l_exact<P, T, int32_t><<<gn, 128, 0, st>>>(nn, dptr<int32_t>(ctx->far_idx), fs,
-                                                           reinterpret_cast<const int32_t *>(fs + nn), nullptr, 0, comx,
-                                                           comy, mixed ? dptr<float4>(ctx->comhl) : nullptr, eps2, M,
-                                                           L);
+            // nodes without far sources keep whatever L holds: has_far = 0 keeps L2L from reading it
+            const gx_ctx::M2LUnits &U = ctx->m2l_units;
+            GX_TRY(gx_ensure(ctx, ctx->m2l_part, sizeof(T) * NS * (size_t)(U.n + 1)));
+            if (U.n > 0) {
+                const int64_t *node_u = dptr<int64_t>(U.node_u);
+                k_m2l_units<P, T><<<(unsigned)((U.n * 32 + 127) / 128), 128, 0, st>>>(
+                    U.n, dptr<int32_t>(U.node), dptr<int64_t>(U.start), dptr<int32_t>(U.len), node_u,
+                    dptr<int32_t>(ctx->far_idx), comx, comy, mixed ? dptr<float4>(ctx->comhl) : nullptr, eps2, M, L,
+                    dptr<T>(ctx->m2l_part));
+                k_m2l_combine<P, T><<<gx_blocks(nn * NC, 256), 256, 0, st>>>(nn, node_u, dptr<T>(ctx->m2l_part), L);
+                ctx->launches++;
+            }
         } else {
             k_m2l_exact<P, T, uint32_t><<<gn, 128, 0, st>>>(nn, dptr<uint32_t>(ctx->vdata), nullptr, nullptr,
                                                             dptr<uint8_t>(ctx->vlen), GX_LIST_CAP, comx, comy,

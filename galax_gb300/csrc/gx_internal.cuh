@@ -113,6 +113,14 @@ struct gx_ctx {
         int64_t n = 0;
         bool valid = false;
     } items_ref, items_acc;
+    // ACCURATE M2L work units (far lists cut into pieces of at most GX_M2L_UNIT
+    // sources), per plan: unit -> node, first index, length; node_u[nn+1] = the
+    // node's first unit
+    struct M2LUnits {
+        DevBuf node, start, len, node_u;  // int32, int64, int32, int64[n_nodes+1]
+        int64_t n = 0;
+    } m2l_units;
+    DevBuf m2l_part;  // per-unit partial locals of nodes cut into several units
     DevBuf part;                   // per-item partial accelerations
     int64_t max_leaf = 0;          // largest leaf body count
     bool aux_valid = false;        // anc / comhl built for the current tree
@@ -191,6 +199,7 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 __host__ __device__ constexpr int gx_nc(int p) { return (p + 1) * (p + 2) / 2; }
+constexpr int GX_M2L_UNIT = 256;  // far sources per M2L work unit (8 rounds of a warp)
 __host__ __device__ constexpr int gx_mi(int i, int j) { return (i + j) * (i + j + 1) / 2 + j; }
 __host__ __device__ constexpr int gx_kdi(int k, int l, int p) { return (k + l) * (2 * p + 1) + l; }
 #endif

@@ -1027,6 +1027,25 @@ __global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cn
     }
 }
 
+// M2L units: per node the number of units; then unit -> (node, first, length)
+__global__ void k_m2l_units_count(int64_t nn, const int32_t *fcnt, int64_t *nunits) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a > nn) return;
+    nunits[a] = a == nn ? 0 : (fcnt[a] + GX_M2L_UNIT - 1) / GX_M2L_UNIT;
+}
+
+__global__ void k_m2l_units_fill(int64_t nn, const int64_t *fstart, const int32_t *fcnt, const int64_t *node_u,
+                                 int32_t *unode, int64_t *ustart, int32_t *ulen) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nn) return;
+    int64_t u = node_u[a];
+    for (int32_t k = 0; k < fcnt[a]; k += GX_M2L_UNIT, u++) {
+        unode[u] = (int32_t)a;
+        ustart[u] = fstart[a] + k;
+        ulen[u] = min(GX_M2L_UNIT, fcnt[a] - k);
+    }
+}
+
 __global__ void k_add_offsets(const int64_t *o, int64_t *dst, int64_t c, int64_t add) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < c) dst[i] = o[i] + add;
@@ -1117,6 +1136,31 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     GX_CUDA(ctx, cudaGetLastError());
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     I.n = tot;
+    if (accurate) {
+        // M2L units of the far lists
+        gx_ctx::M2LUnits &U = ctx->m2l_units;
+        const int64_t *fstart = dptr<int64_t>(ctx->far_off);
+        const int32_t *fcnt = reinterpret_cast<const int32_t *>(fstart + nn);
+        GX_TRY(gx_ensure(ctx, U.node_u, sizeof(int64_t) * (size_t)(nn + 1)));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nn + 1)));
+        int64_t *nu = dptr<int64_t>(ctx->scratch_c);
+        k_m2l_units_count<<<gx_blocks(nn + 1, 256), 256, 0, ctx->stream>>>(nn, fcnt, nu);
+        GX_TRY(gx_exclusive_scan_i64(ctx, nu, dptr<int64_t>(U.node_u), nn + 1));
+        int64_t nun = 0;
+        GX_CUDA(ctx, cudaMemcpyAsync(&nun, dptr<int64_t>(U.node_u) + nn, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        GX_TRY(gx_ensure(ctx, U.node, sizeof(int32_t) * (size_t)(nun + 1)));
+        GX_TRY(gx_ensure(ctx, U.start, sizeof(int64_t) * (size_t)(nun + 1)));
+        GX_TRY(gx_ensure(ctx, U.len, sizeof(int32_t) * (size_t)(nun + 1)));
+        k_m2l_units_fill<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, fstart, fcnt, dptr<int64_t>(U.node_u),
+                                                                      dptr<int32_t>(U.node), dptr<int64_t>(U.start),
+                                                                      dptr<int32_t>(U.len));
+        ctx->launches += 2;
+        GX_CUDA(ctx, cudaGetLastError());
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        U.n = nun;
+    }
     I.valid = true;
     return GX_OK;
 }
