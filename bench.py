@@ -26,7 +26,9 @@ adjoint/forward time of reverse-mode rollouts.
              tree every step
 
 ``--impl reference`` times the reference's CPU algorithm (the oracle port) on the
-same workload instead.  Multi-GPU: the force evaluation does not shard here, so
+same workload instead.  ``--sweep disk`` (p x n_max on the 4M disk preset),
+``--sweep theta`` (opening angle on the Plummer workload) and ``--build-only``
+(device tree builds and plans) print their own JSON lines.  Multi-GPU: the force evaluation does not shard here, so
 ``--gpus N`` runs N independent replicas (weak scaling); timing is the max over
 ranks.
 """
@@ -374,13 +376,50 @@ def run_sweep_disk(args):
                 row = {"n_max": n_max, "p": p, "form": name, "ms": float(np.mean(ms)),
                        "bodies_per_s": n / (float(np.mean(ms)) * 1e-3), "far_pairs": far,
                        "near_leaf_pairs": near, "p2p_interactions": inter,
-                       "tiles": {"m2l": f"warp per target node, lane per far source; C(p)={(p + 1) * (p + 2) // 2} "
-                                        f"coefficients, {(2 * p + 1) * (2 * p + 2) // 2} derivatives per pair",
+                       "tiles": {"m2l": f"warp per unit of <= 256 far sources of one target node, lane per source; "
+                                        f"C(p)={(p + 1) * (p + 2) // 2} coefficients, "
+                                        f"{(2 * p + 1) * (2 * p + 2) // 2} derivatives per pair",
                                  "p2p": f"warp per item (target leaf of <= {n_max} bodies x <= 32 source leaves)"}}
                 row.update(_err_stats(r.ax[idx], r.ay[idx], ex, ey))
                 rows.append(row)
     ctx.close()
     print(json.dumps({"sweep": "disk", "n": n, "theta": THETA, "seed": args.seed + 3, "rows": rows}), flush=True)
+    return 0
+
+
+def run_sweep_theta(args):
+    """Opening-angle sweep on the Plummer workload (N = 1,000,000 by default, p = 4,
+    n_max = 32): for each theta the near/far split, the evaluation time of the mixed and
+    FP64 forms and their errors against the FP64 N^2 sum on 1000 seeded samples.  The
+    headline uses theta = 0.5.  Prints one JSON line."""
+    import galax_gb300 as G
+    from galax_gb300 import build as gbuild
+    from galax_gb300 import presets
+    gbuild.build()
+    n = args.n
+    b = presets.plummer(n, seed=args.seed)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=P, eps64=0.1))
+    ctx.build_tree(b, N_MAX, presets.BOUNDS["plummer"])
+    ctx.set_params(P, presets.cli_softening(b.x, b.y))
+    ctx.upload_bodies(b)
+    idx = np.sort(np.random.default_rng(1234).choice(n, min(1000, n), replace=False))
+    ex, ey = ctx.n2_sampled(idx)
+    rows = []
+    for theta in (0.3, 0.4, 0.5, 0.6, 0.7):
+        for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+            ctx.set_mode(G.MODE_ACCURATE, prec, theta)
+            ctx.forces_resident()
+            ms, _ = ctx.bench_forces(10 if name == "mixed" else 1, True, 0)
+            r = G.Bodies.new(n)
+            ctx.download_bodies(r)
+            far, near, inter = ctx.plan_info()
+            row = {"theta": theta, "form": name, "ms": float(np.mean(ms)),
+                   "bodies_per_s": n / (float(np.mean(ms)) * 1e-3), "far_pairs": far, "near_leaf_pairs": near,
+                   "p2p_interactions": inter}
+            row.update(_err_stats(r.ax[idx], r.ay[idx], ex, ey))
+            rows.append(row)
+    ctx.close()
+    print(json.dumps({"sweep": "theta", "n": n, "p": P, "n_max": N_MAX, "seed": args.seed, "rows": rows}), flush=True)
     return 0
 
 
@@ -549,7 +588,7 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=500)
     ap.add_argument("--adj-k", type=lambda s: [int(v) for v in s.split(",")], default=[10, 22, 50, 1])
     ap.add_argument("--fd-dirs", type=int, default=2)
-    ap.add_argument("--sweep", choices=["disk"], default=None)
+    ap.add_argument("--sweep", choices=["disk", "theta"], default=None)
     ap.add_argument("--build-only", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=4_000_000)
     args = ap.parse_args()
@@ -561,6 +600,8 @@ def main():
             return run_reference(args, rank, world, pg)
         if args.sweep == "disk":
             return run_sweep_disk(args) if rank == 0 else 0
+        if args.sweep == "theta":
+            return run_sweep_theta(args) if rank == 0 else 0
         if args.build_only:
             return run_build_only(args) if rank == 0 else 0
         return run_ours(args, rank, world, local, pg)
