@@ -488,6 +488,122 @@ __global__ void __launch_bounds__(128, 6) k_adj_p2p32_items(int64_t n_items, con
     }
 }
 
+// The same A6 when every leaf holds at most 32 bodies (n_max <= 32): each source leaf
+// is one row, the item's source-leaf table is written to shared memory once per item,
+// and the next row's bodies and cotangents are fetched while the current row computes.
+// Same arithmetic and accumulation order as k_adj_p2p32_items with one target chunk.
+__global__ void __launch_bounds__(128, 6) k_adj_p2p32_rows(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                        const int64_t *__restrict__ item_qb,
+                                                        const int32_t *__restrict__ item_nq,
+                                                        const float4 *__restrict__ pos, const float2 *__restrict__ lam,
+                                                        const double *__restrict__ comx, const double *__restrict__ comy,
+                                                        const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                                        const int32_t *__restrict__ src_idx, float eps2,
+                                                        float4 *__restrict__ part) {
+    __shared__ __align__(16) float sx[4][32], sy[4][32], sm[4][32], slx[4][32], sly[4][32];
+    __shared__ __align__(16) int4 meta[4][32];  // per source leaf: begin, end, shift x, shift y (FP32 bits)
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (it >= n_items) return;
+    const int32_t leaf = item_leaf[it];
+    const int nq = item_nq[it];
+    const int32_t t0 = bs[leaf], t1 = be[leaf];
+    bool own_lane = false;
+    if (lane < nq) {
+        int32_t sl = src_idx[item_qb[it] + lane];
+        double tcx = comx[leaf], tcy = comy[leaf];
+        meta[w][lane] = make_int4(bs[sl], be[sl], __float_as_int((float)(comx[sl] - tcx)),
+                                  __float_as_int((float)(comy[sl] - tcy)));
+        own_lane = sl == leaf;
+    }
+    const unsigned ownm = __ballot_sync(0xffffffffu, own_lane);
+    const int kown = ownm ? __ffs(ownm) - 1 : -1;
+    __syncwarp();
+    const int32_t i = t0 + lane;
+    const bool valid = i < t1;
+    const float4 me = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 li = valid ? lam[i] : make_float2(0.f, 0.f);
+    const float xi = me.x, yi = me.y, mi = me.z, lxi = li.x, lyi = li.y;
+    const uint64_t XI = pk2(xi, xi), YI = pk2(yi, yi), E2 = pk2(eps2, eps2), MI = pk2(mi, mi);
+    const uint64_t NLXI = pk2(-lxi, -lxi), NLYI = pk2(-lyi, -lyi), N3 = pk2(-3.f, -3.f);
+    uint64_t GX = 0, GY = 0, GMN = 0;  // packed sums; GMN accumulates +lam.d/r^3
+    float gxa = 0.f, gya = 0.f, gma = 0.f;
+    auto fetch = [&](int4 m, float4 &b, float2 &l) {
+        int j = m.x + lane;
+        b = j < m.y ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        l = j < m.y ? lam[j] : make_float2(0.f, 0.f);
+        b.x += __int_as_float(m.z);
+        b.y += __int_as_float(m.w);
+    };
+    float4 cb = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 cl = make_float2(0.f, 0.f);
+    if (nq > 0) fetch(meta[w][0], cb, cl);
+    for (int k = 0; k < nq; k++) {
+        float4 nb = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 nl2 = make_float2(0.f, 0.f);
+        if (k + 1 < nq) fetch(meta[w][k + 1], nb, nl2);
+        __syncwarp();
+        sx[w][lane] = cb.x;
+        sy[w][lane] = cb.y;
+        sm[w][lane] = cb.z;
+        slx[w][lane] = cl.x;
+        sly[w][lane] = cl.y;
+        __syncwarp();
+        const int2 se = *reinterpret_cast<const int2 *>(&meta[w][k]);  // this row's begin, end
+        const int ns = se.y - se.x;
+        if (ns == 32 && k != kown) {
+#pragma unroll 4
+            for (int kk = 0; kk < 32; kk += 2) {
+                const uint64_t X = *reinterpret_cast<const uint64_t *>(&sx[w][kk]);
+                const uint64_t Y = *reinterpret_cast<const uint64_t *>(&sy[w][kk]);
+                const uint64_t Mj = *reinterpret_cast<const uint64_t *>(&sm[w][kk]);
+                const uint64_t LXj = *reinterpret_cast<const uint64_t *>(&slx[w][kk]);
+                const uint64_t LYj = *reinterpret_cast<const uint64_t *>(&sly[w][kk]);
+                const uint64_t dx = sub2(X, XI), dy = sub2(Y, YI);
+                const uint64_t r2 = fma2(dx, dx, fma2(dy, dy, E2));
+                float ra, rb;
+                upk2(r2, ra, rb);
+                const uint64_t ir = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                const uint64_t ir2 = mul2(ir, ir);
+                const uint64_t ir3 = mul2(ir2, ir);
+                const uint64_t ir5 = mul2(ir3, ir2);
+                const uint64_t wx = fma2(Mj, NLXI, mul2(MI, LXj));  // mi lx_j - m_j lx_i
+                const uint64_t wy = fma2(Mj, NLYI, mul2(MI, LYj));
+                const uint64_t nc = mul2(mul2(N3, ir5), fma2(dx, wx, mul2(dy, wy)));  // -3 dw / r^5
+                GX = fma2(ir3, wx, fma2(nc, dx, GX));
+                GY = fma2(ir3, wy, fma2(nc, dy, GY));
+                GMN = fma2(fma2(LXj, dx, mul2(LYj, dy)), ir3, GMN);
+            }
+        } else {
+            const bool own = k == kown;
+            for (int kk = 0; kk < ns; kk++) {
+                float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
+                float mj = sm[w][kk], lxj = slx[w][kk], lyj = sly[w][kk];
+                float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                float ir2 = ir * ir;
+                float ir3 = ir2 * ir;
+                float ir5 = ir3 * ir2;
+                float wx = fmaf(mi, lxj, -mj * lxi), wy = fmaf(mi, lyj, -mj * lyi);
+                float c = 3.f * ir5 * fmaf(dx, wx, dy * wy);
+                float dl = fmaf(lxj, dx, lyj * dy);
+                bool self = own && se.x + kk == i;
+                ir3 = self ? 0.f : ir3;
+                c = self ? 0.f : c;
+                gxa = fmaf(ir3, wx, fmaf(-c, dx, gxa));
+                gya = fmaf(ir3, wy, fmaf(-c, dy, gya));
+                gma = fmaf(-dl, ir3, gma);
+            }
+        }
+        cb = nb;
+        cl = nl2;
+    }
+    float a0, a1, b0, b1, c0, c1;
+    upk2(GX, a0, a1);
+    upk2(GY, b0, b1);
+    upk2(GMN, c0, c1);
+    part[it * 32 + lane] = make_float4((a0 + a1) + gxa, (b0 + b1) + gya, gma - (c0 + c1), 0.f);
+}
+
 template <class V, class S>
 __global__ void __launch_bounds__(128) k_adj_p2p_reduce(int64_t nl, const int32_t *__restrict__ bs,
                                                         const int32_t *__restrict__ be, const int64_t *__restrict__ item_off,
@@ -568,7 +684,12 @@ int run_force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf_
     GX_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
     GX_CUDA(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
     if (I.n > 0) {
-        if (F32)
+        if (F32 && tchunks == 1)
+            k_adj_p2p32_rows<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                           dptr<int32_t>(I.nq), pos32, lam32, comx, comy, bs, be,
+                                                           dptr<int32_t>(ctx->near_idx), (float)eps2,
+                                                           dptr<float4>(ctx->part));
+        else if (F32)
             k_adj_p2p32_items<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
                                                             dptr<int32_t>(I.nq), pos32, lam32, comx, comy, bs, be,
                                                             dptr<int32_t>(ctx->near_idx), (float)eps2, tchunks,
