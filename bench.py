@@ -20,6 +20,9 @@ adjoint/forward time of reverse-mode rollouts.
   cpu_baseline  the oracle (C restatement of galax-core's CPU FMM, REF semantics,
              OpenMP where the reference uses Rayon) on the host cores
   kdk_steps  leapfrog steps/s, static tree and tree rebuilt every step
+  uniform_10k  the uniform N=10,000 case: 10 leapfrog steps/s of the REF FP64,
+             ACCURATE FP64 and mixed forms, force errors against the exact N^2 sum,
+             and the oracle's steps/s and end-state difference (CPU leg)
   adjoint    galaxy N=200,001 x 100 steps (FP64 and mixed, finite differences with
              the tree sequence frozen) and Plummer N=1M x 500 steps (mixed,
              checkpoint interval sweep, peak device bytes), both rebuilding the
@@ -216,6 +219,68 @@ def _adjoint_run(G, ctx, b, T, dt, k, R, rebuild=0):
     return t_fwd, t_bwd, (gx + dx0, gy + dy0, gvx, gvy, gm), peak, L
 
 
+def run_uniform10k(G, presets, args, with_cpu: bool):
+    """Config 1: uniform N=10,000 in [0,100]^2, p=4, n_max=32, CLI softening, 10 leapfrog
+    steps with the static tree at dt = 0.5/sqrt(max|a|).  Steps/s of the REF FP64 form
+    (reference semantics) and of the ACCURATE FP64 and mixed forms, each form's initial
+    force error against the exact FP64 N^2 sum over all bodies; with the CPU leg, the
+    oracle's REF simulate of the same steps on the host cores and the largest difference
+    of the GPU REF end state from it."""
+    n, T = 10_000, 10
+    bounds = presets.BOUNDS["uniform"]
+    gb = presets.uniform(n, seed=0)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=P, eps64=0.1))
+    ctx.build_tree(gb, N_MAX, bounds)  # permutes gb into Morton order, as Tree::build does
+    eps = presets.cli_softening(gb.x, gb.y)
+    ctx.set_params(P, eps)
+    idx = np.arange(n)
+    ex, ey = ctx.n2_sampled(idx)
+    out = {"workload": f"uniform N={n} in [0,100]^2, p={P}, n_max={N_MAX}, {T} KDK steps, static tree", "eps": eps}
+    end = {}
+    for name, mode, prec in (("ref_fp64", G.MODE_REF, G.PREC_FP64), ("accurate_fp64", G.MODE_ACCURATE, G.PREC_FP64),
+                             ("accurate_mixed", G.MODE_ACCURATE, G.PREC_MIXED)):
+        ctx.set_mode(mode, prec, THETA)
+        ctx.upload_bodies(gb)
+        ctx.forces_resident()
+        a0 = G.Bodies.new(n)
+        ctx.download_bodies(a0)
+        if name == "ref_fp64":
+            dt = presets.cli_dt(a0.ax, a0.ay)
+            out["dt"] = dt
+        row = _err_stats(a0.ax, a0.ay, ex, ey)
+        ts = []
+        for r in range(3):  # the first run is a warm-up
+            ctx.upload_bodies(gb)
+            ctx.forces_resident()
+            t0 = time.perf_counter()
+            ctx.kdk_run(T, dt, 0)
+            ts.append(time.perf_counter() - t0)
+        row.update({"steps_per_s": T / float(np.mean(ts[1:])), "ms_per_step": float(np.mean(ts[1:])) / T * 1e3})
+        fin = G.Bodies.new(n)
+        ctx.download_bodies(fin)
+        end[name] = fin
+        out[name] = row
+    ctx.close()
+    if with_cpu:
+        from oracle import oracle as O
+        O.build()
+        ob = O.Bodies.from_arrays(gb.x, gb.y, gb.mass)
+        t = O.tree_build(ob, N_MAX, bounds)
+        v, u = O.vlist_build(t), O.ulist_build(t)
+        O.compute_fmm_force(ob, t, v, u, P, eps, O.MODE_REF)  # initial forces (galax-cli/src/main.rs:230)
+        t0 = time.perf_counter()
+        O.simulate(ob, t, v, u, P, eps, out["dt"], T, 0, O.MODE_REF)
+        tc = time.perf_counter() - t0
+        g = end["ref_fp64"]
+        sc, vs = float(np.max(np.abs(ob.x))), float(np.max(np.hypot(ob.vx, ob.vy)))
+        out["cpu_baseline"] = {"steps_per_s": T / tc, "cores": O.get_threads(), "kind": "port",
+                               "sample": f"{T} REF KDK steps of the same bodies (oracle simulate)"}
+        out["ref_fp64"]["end_state_max_rel_diff_vs_oracle"] = max(
+            float(np.max(np.abs(g.x - ob.x))) / sc, float(np.max(np.abs(g.y - ob.y))) / sc,
+            float(np.max(np.abs(g.vx - ob.vx))) / vs, float(np.max(np.abs(g.vy - ob.vy))) / vs)
+    return out
+
+
 def _grad_rel(g, r):
     return float(max(np.linalg.norm(a - c) / max(np.linalg.norm(c), 1e-300) for a, c in zip(g, r)))
 
@@ -291,11 +356,25 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
     _, _, gm20, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp, rebuild=1)
     ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
     _, _, g64, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp, rebuild=1)
+    pl = {"workload": f"plummer N={len(b1m)}, p={P}, n_max={N_MAX}, {T} steps, dt={dt}, mixed, tree rebuilt every step",
+          "checkpoint_sweep": sweep, "grad_rel_err_mixed_vs_fp64_20_steps": _grad_rel(gm20, g64)}
+    if args.fd_dirs_1m > 0:
+        # central differences of the FP64 20-step prefix along seeded directions, trees
+        # frozen along the unperturbed trajectory; compared with both adjoints
+        from galax_gb300 import fdcheck
+        n1 = len(b1m)
+        rng = np.random.default_rng(args.seed + 9)
+        dirs = [[rng.standard_normal(n1) for _ in range(4)] + [rng.standard_normal(n1) * b1m.mass]
+                for _ in range(args.fd_dirs_1m)]
+        num = fdcheck.fd_frozen_trees(G, ctx1m, b1m, Tp, dt, Rp, dirs, 1e-6, N_MAX, presets.BOUNDS["plummer"],
+                                      rebuild=True)
+        for key, g in (("fp64", g64), ("mixed", gm20)):
+            err = [abs(num[i] - sum(float(np.dot(g[q], dirs[i][q])) for q in range(5))) / abs(num[i])
+                   for i in range(len(dirs))]
+            pl[f"fd_rel_err_max_20_steps_{key}"] = float(max(err))
+        pl["fd_directions_20_steps"] = args.fd_dirs_1m
     ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
-    out["plummer_1m"] = {"workload": f"plummer N={len(b1m)}, p={P}, n_max={N_MAX}, {T} steps, dt={dt}, mixed, "
-                                     f"tree rebuilt every step",
-                         "checkpoint_sweep": sweep,
-                         "grad_rel_err_mixed_vs_fp64_20_steps": _grad_rel(gm20, g64)}
+    out["plummer_1m"] = pl
     return out
 
 
@@ -527,6 +606,7 @@ def run_ours(args, rank, world, local, pg):
     if rank != 0:
         ctx.close()
         return 0
+    uniform10k = run_uniform10k(G, presets, args, not args.no_cpu_baseline)
     cpu = None
     if not args.no_cpu_baseline:
         _, _, _, _, times, cores = _cpu_baseline(gb, bounds, eps, n_evals=2)
@@ -563,6 +643,7 @@ def run_ours(args, rank, world, local, pg):
         "tree": {"nodes": nn, "leaves": nl, "levels": nlev, "build_s_incl_host_copies": setup_tree_s},
         "cpu_baseline": cpu,
         "kdk_steps": steps_cmp,
+        "uniform_10k": uniform10k,
         "adjoint": adjoint if adjoint is not None else "not run (--no-adjoint, or N>1 replicas: see the N=1 line)",
     }
     if adjoint is not None:
@@ -588,6 +669,7 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=500)
     ap.add_argument("--adj-k", type=lambda s: [int(v) for v in s.split(",")], default=[10, 22, 50, 1])
     ap.add_argument("--fd-dirs", type=int, default=2)
+    ap.add_argument("--fd-dirs-1m", type=int, default=0)
     ap.add_argument("--sweep", choices=["disk", "theta"], default=None)
     ap.add_argument("--build-only", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=4_000_000)

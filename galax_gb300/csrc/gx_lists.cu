@@ -457,17 +457,41 @@ __global__ void k_to_f32(int64_t n, const double *in, float *out) {
 // nodes below it over many warps instead of one.
 constexpr int MAC_CHUNK = 128;
 
-__global__ void k_mac_nchunks(int64_t s, int64_t e, const int32_t *parent, const int32_t *near_cnt, int64_t *nch) {
+// Plan counters on the device (the level loop runs without host round trips):
+// running far / near list totals, the last level's near count, and overflow flags.
+// Capacities are fixed for one attempt; a level that would exceed one sets its flag,
+// every later kernel of the attempt returns at once, and the host grows the arrays
+// and plans again.
+enum { PC_FAR = 0, PC_NEAR = 1, PC_NEAR_LAST = 2, PC_OVF = 3, PC_N = 4 };
+enum { OVF_UNITS = 1, OVF_FAR = 2, OVF_NEAR = 4 };
+
+__global__ void k_mac_nchunks(int64_t s, int64_t e, const int32_t *parent, const int32_t *near_cnt, int64_t *nch,
+                              const int64_t *ctr) {
+    if (ctr[PC_OVF]) return;
     int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= e) return;
+    if (x > e) return;
+    if (x == e) { nch[e - s] = 0; return; }
     int32_t P = parent[x];
     int64_t cand = P >= 0 ? near_cnt[P] : 0;
     nch[x - s] = (cand + MAC_CHUNK - 1) / MAC_CHUNK;
 }
 
-__global__ void k_mac_units(int64_t s, int64_t e, const int64_t *uoff, int32_t *unode, int32_t *uchunk) {
+// unit -> (node, chunk) for the level's U = uoff[e - s] units; zero count slots at U
+// so the count scans below end on the level totals
+__global__ void k_mac_units(int64_t s, int64_t e, const int64_t *uoff, int64_t ucap, int32_t *unode, int32_t *uchunk,
+                            int64_t *ufar, int64_t *unear, int64_t *ctr) {
+    if (ctr[PC_OVF]) return;
     int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= e) return;
+    const int64_t U = uoff[e - s];
+    if (U > ucap) {
+        if (x == s) atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF), (unsigned long long)OVF_UNITS);
+        return;
+    }
+    if (x == s) {
+        ufar[U] = 0;
+        unear[U] = 0;
+    }
     int64_t a = uoff[x - s], b = uoff[x - s + 1];
     for (int64_t u = a; u < b; u++) {
         unode[u] = (int32_t)x;
@@ -475,74 +499,98 @@ __global__ void k_mac_units(int64_t s, int64_t e, const int64_t *uoff, int32_t *
     }
 }
 
-// pass 0: per-unit counts (ufar, unear); pass 1: write at the per-unit offsets
-__global__ void k_mac(int64_t n_units, int pass, const int32_t *unode, const int32_t *uchunk, const int32_t *parent,
+// pass 0: per-unit counts (ufar, unear); pass 1: write at the running totals plus the
+// per-unit offsets.  A grid-stride loop over the level's units, one warp per unit.
+__global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const int32_t *uchunk, const int32_t *parent,
                       const int4 *child, const float4 *hl, const float *R32, float theta2,
                       const int64_t *near_start, const int32_t *near_cnt, const int32_t *near_idx_in, int64_t *ufar,
-                      int64_t *unear, int32_t *far_idx, int32_t *near_idx) {
+                      int64_t *unear, int32_t *far_idx, int32_t *near_idx, int64_t far_cap, int64_t near_cap,
+                      int64_t *ctr) {
     const unsigned full = 0xffffffffu;
-    int lane = threadIdx.x & 31;
-    int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (u >= n_units) return;  // whole warps leave together
-    int32_t x = unode[u];
-    int32_t P = parent[x];
-    int64_t qa = near_start[P] + (int64_t)uchunk[u] * MAC_CHUNK;
-    int64_t qe = min(near_start[P] + (int64_t)near_cnt[P], qa + MAC_CHUNK);
-    int64_t nf = 0, nn = 0;
-    int64_t fb = pass ? ufar[u] : 0, nb = pass ? unear[u] : 0;
-    for (int64_t qb = qa; qb < qe; qb += 32) {
-        int64_t q = qb + lane;
-        int cc[4] = {-1, -1, -1, -1};
-        unsigned fm = 0, nm = 0;
-        if (q < qe) {
-            int4 c4 = child[near_idx_in[q]];
-            cc[0] = c4.x;
-            cc[1] = c4.y;
-            cc[2] = c4.z;
-            cc[3] = c4.w;
-            for (int k = 0; k < 4; k++) {
-                if (cc[k] < 0) continue;
-                if (mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
-                else nm |= 1u << k;
-            }
-        }
-        int myf = __popc(fm), myn = __popc(nm);
-        int pf = myf, pn = myn;  // inclusive warp scans
-        for (int o = 1; o < 32; o <<= 1) {
-            int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
-            if (lane >= o) {
-                pf += tf;
-                pn += tn;
-            }
-        }
-        int tf = __shfl_sync(full, pf, 31), tn = __shfl_sync(full, pn, 31);
+    if (ctr[PC_OVF]) return;
+    const int64_t n_units = *Uptr;
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t far0 = pass ? ctr[PC_FAR] : 0, near0 = pass ? ctr[PC_NEAR] : 0;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n_units; u += nwarps) {
+        int32_t x = unode[u];
+        int32_t P = parent[x];
+        int64_t qa = near_start[P] + (int64_t)uchunk[u] * MAC_CHUNK;
+        int64_t qe = min(near_start[P] + (int64_t)near_cnt[P], qa + MAC_CHUNK);
+        int64_t nf = 0, nn = 0;
+        int64_t fb = pass ? far0 + ufar[u] : 0, nb = pass ? near0 + unear[u] : 0;
         if (pass) {
-            int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
-            for (int k = 0; k < 4; k++) {
-                if ((fm >> k) & 1u) far_idx[a++] = cc[k];
-                if ((nm >> k) & 1u) near_idx[b++] = cc[k];
+            // this unit's whole range must fit; otherwise flag and write nothing
+            int64_t fe = far0 + ufar[u + 1], ne = near0 + unear[u + 1];
+            unsigned long long bad = (fe > far_cap ? OVF_FAR : 0) | (ne > near_cap ? OVF_NEAR : 0);
+            if (bad) {
+                if (lane == 0) atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF), bad);
+                continue;
             }
         }
-        nf += tf;
-        nn += tn;
-    }
-    if (!pass && lane == 0) {
-        ufar[u] = nf;
-        unear[u] = nn;
+        for (int64_t qb = qa; qb < qe; qb += 32) {
+            int64_t q = qb + lane;
+            int cc[4] = {-1, -1, -1, -1};
+            unsigned fm = 0, nm = 0;
+            if (q < qe) {
+                int4 c4 = child[near_idx_in[q]];
+                cc[0] = c4.x;
+                cc[1] = c4.y;
+                cc[2] = c4.z;
+                cc[3] = c4.w;
+                for (int k = 0; k < 4; k++) {
+                    if (cc[k] < 0) continue;
+                    if (mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
+                    else nm |= 1u << k;
+                }
+            }
+            int myf = __popc(fm), myn = __popc(nm);
+            int pf = myf, pn = myn;  // inclusive warp scans
+            for (int o = 1; o < 32; o <<= 1) {
+                int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
+                if (lane >= o) {
+                    pf += tf;
+                    pn += tn;
+                }
+            }
+            int tf = __shfl_sync(full, pf, 31), tn = __shfl_sync(full, pn, 31);
+            if (pass) {
+                int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
+                for (int k = 0; k < 4; k++) {
+                    if ((fm >> k) & 1u) far_idx[a++] = cc[k];
+                    if ((nm >> k) & 1u) near_idx[b++] = cc[k];
+                }
+            }
+            nf += tf;
+            nn += tn;
+        }
+        if (!pass && lane == 0) {
+            ufar[u] = nf;
+            unear[u] = nn;
+        }
     }
 }
 
 // per node of the level: start (running total + first unit's offset) and count
 __global__ void k_mac_node_lists(int64_t s, int64_t e, const int64_t *uoff, const int64_t *ufo, const int64_t *uno,
-                                 int64_t far_tot, int64_t near_tot, int64_t *fstart, int32_t *fcnt, int64_t *nstart,
-                                 int32_t *ncnt) {
+                                 const int64_t *ctr, int64_t *fstart, int32_t *fcnt, int64_t *nstart, int32_t *ncnt) {
+    if (ctr[PC_OVF]) return;
     int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (x >= e) return;
     int64_t a = uoff[x - s], b = uoff[x - s + 1];
-    fstart[x] = far_tot + ufo[a];
-    nstart[x] = near_tot + uno[a];
+    fstart[x] = ctr[PC_FAR] + ufo[a];
+    nstart[x] = ctr[PC_NEAR] + uno[a];
     fcnt[x] = (int32_t)(ufo[b] - ufo[a]);
     ncnt[x] = (int32_t)(uno[b] - uno[a]);
+}
+
+// after a level: advance the running totals by the level's far / near counts
+__global__ void k_mac_advance(const int64_t *Uptr, const int64_t *ufo, const int64_t *uno, int64_t *ctr) {
+    if (ctr[PC_OVF]) return;
+    const int64_t U = *Uptr;
+    ctr[PC_FAR] += ufo[U];
+    ctr[PC_NEAR] += uno[U];
+    ctr[PC_NEAR_LAST] = uno[U];
 }
 
 // ---------------------------------------------------------------- balanced build
@@ -880,24 +928,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
     int32_t *fcnt = reinterpret_cast<int32_t *>(fstart + nn);
     int64_t *nstart = dptr<int64_t>(ctx->near_off);
     int32_t *ncnt = reinterpret_cast<int32_t *>(nstart + nn);
-    GX_CUDA(ctx, cudaMemsetAsync(fcnt, 0, sizeof(int32_t) * (size_t)nn, ctx->stream));
-    GX_CUDA(ctx, cudaMemsetAsync(ncnt, 0, sizeof(int32_t) * (size_t)nn, ctx->stream));
-    int64_t root = nn - 1;
-    // root: near itself
-    std::vector<int64_t> hstart(1, 0);
-    int32_t one = 1;
-    int32_t root32 = (int32_t)root;
-    int64_t far_tot = 0, near_tot = 1;
-    size_t near_cap = 1 << 20, far_cap = 1 << 20;
-    GX_TRY(gx_ensure(ctx, ctx->near_idx, sizeof(int32_t) * near_cap));
-    GX_TRY(gx_ensure(ctx, ctx->far_idx, sizeof(int32_t) * far_cap));
-    near_cap = ctx->near_idx.bytes / sizeof(int32_t);
-    far_cap = ctx->far_idx.bytes / sizeof(int32_t);
-    int64_t zero = 0;
-    GX_CUDA(ctx, cudaMemcpyAsync(nstart + root, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-    GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-    GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
-                                 ctx->stream));
+    const int64_t root = nn - 1;
     // FP32 MAC operands: (hi, lo) COMs (built with the tree aux) and radii rounded once
     const float thf = (float)ctx->theta;
     const float theta2 = thf * thf;
@@ -905,70 +936,77 @@ int gx_plan_accurate(gx_ctx *ctx) {
     float *R32 = dptr<float>(ctx->radius32);
     k_to_f32<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, R, R32);
     const float4 *hl = dptr<float4>(ctx->comhl);
-    for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
-        const int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
-        // units: chunks of each node's candidate list
-        GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(c + 1) * 2));
-        int64_t *nch = dptr<int64_t>(ctx->scratch_a), *uoff = nch + (c + 1);
-        GX_CUDA(ctx, cudaMemsetAsync(nch + c, 0, sizeof(int64_t), ctx->stream));
-        k_mac_nchunks<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, dptr<int32_t>(ctx->parent), ncnt, nch);
-        GX_TRY(gx_exclusive_scan_i64(ctx, nch, uoff, c + 1));
-        int64_t U = 0;
-        GX_CUDA(ctx, cudaMemcpyAsync(&U, uoff + c, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
-        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        // unit -> (node, chunk); per-unit counts, then their offsets
-        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int32_t) * (size_t)(U + 1) * 2));
-        GX_TRY(gx_ensure(ctx, ctx->scratch_e, sizeof(int64_t) * (size_t)(U + 1) * 4));
-        int32_t *unode = dptr<int32_t>(ctx->scratch_b), *uchunk = unode + (U + 1);
-        int64_t *ufar = dptr<int64_t>(ctx->scratch_e), *unear = ufar + (U + 1), *ufo = unear + (U + 1),
-                *uno = ufo + (U + 1);
-        k_mac_units<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, unode, uchunk);
-        GX_CUDA(ctx, cudaMemsetAsync(ufar + U, 0, sizeof(int64_t), ctx->stream));
-        GX_CUDA(ctx, cudaMemsetAsync(unear + U, 0, sizeof(int64_t), ctx->stream));
-        const unsigned gu = (unsigned)((U * 32 + 127) / 128);
-        if (U > 0)
-            k_mac<<<gu, 128, 0, ctx->stream>>>(U, 0, unode, uchunk, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
-                                               hl, R32, theta2, nstart, ncnt, dptr<int32_t>(ctx->near_idx), ufar,
-                                               unear, nullptr, nullptr);
-        GX_TRY(gx_exclusive_scan_i64(ctx, ufar, ufo, U + 1));
-        GX_TRY(gx_exclusive_scan_i64(ctx, unear, uno, U + 1));
-        int64_t ft = 0, nt = 0;
-        GX_CUDA(ctx, cudaMemcpyAsync(&ft, ufo + U, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
-        GX_CUDA(ctx, cudaMemcpyAsync(&nt, uno + U, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
-        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        // grow (preserving) the index arrays
-        auto grow = [&](DevBuf &b, size_t &cap, int64_t need) -> int {
-            if ((size_t)need <= cap) return GX_OK;
-            size_t nc = std::max((size_t)need, cap * 2);
-            void *p = nullptr;
-            if (cudaMalloc(&p, nc * sizeof(int32_t)) != cudaSuccess) return gx_fail(ctx, GX_ERR_ALLOC, "list storage");
-            cudaMemcpyAsync(p, b.p, cap * sizeof(int32_t), cudaMemcpyDeviceToDevice, ctx->stream);
-            cudaStreamSynchronize(ctx->stream);
-            cudaFree(b.p);
-            b.p = p;
-            b.bytes = nc * sizeof(int32_t);
-            cap = nc;
-            return GX_OK;
-        };
-        GX_TRY(grow(ctx->far_idx, far_cap, far_tot + ft + 1));
-        GX_TRY(grow(ctx->near_idx, near_cap, near_tot + nt + 1));
-        // fill: unit u writes at running total + its offset
-        GX_TRY(gx_add_offsets(ctx, ufo, ufar, U, far_tot));
-        GX_TRY(gx_add_offsets(ctx, uno, unear, U, near_tot));
-        if (U > 0)
-            k_mac<<<gu, 128, 0, ctx->stream>>>(U, 1, unode, uchunk, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child),
-                                               hl, R32, theta2, nstart, ncnt, dptr<int32_t>(ctx->near_idx), ufar,
-                                               unear, dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx));
-        k_mac_node_lists<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, ufo, uno, far_tot, near_tot, fstart,
-                                                                     fcnt, nstart, ncnt);
-        ctx->launches += 9;
-        GX_CUDA(ctx, cudaGetLastError());
-        far_tot += ft;
-        near_tot += nt;
-        if (lv == 0) {
-            ctx->n_near_pairs = nt;
+    int64_t cmax = 1;
+    for (int lv = 0; lv < ctx->n_levels; lv++)
+        cmax = std::max<int64_t>(cmax, ctx->level_start[lv + 1] - ctx->level_start[lv]);
+    // capacities: unit arrays and the far / near index arrays, kept from the last plan
+    if (ctx->mac_ucap < 1024) ctx->mac_ucap = std::max<int64_t>(1024, nn);
+    int64_t far_cap = std::max<int64_t>((int64_t)(ctx->far_idx.bytes / sizeof(int32_t)), std::max<int64_t>(1 << 20, 64 * nn));
+    int64_t near_cap = std::max<int64_t>((int64_t)(ctx->near_idx.bytes / sizeof(int32_t)), std::max<int64_t>(1 << 20, 64 * nn));
+    GX_TRY(gx_ensure(ctx, ctx->plan_ctr, sizeof(int64_t) * PC_N));
+    int64_t *ctr = dptr<int64_t>(ctx->plan_ctr);
+    int64_t hc[PC_N] = {0, 0, 0, 0};
+    const unsigned gmac = (unsigned)(ctx->sm_count > 0 ? ctx->sm_count * 16 : 2432);  // grid-stride k_mac
+    for (int attempt = 0;; attempt++) {
+        if (attempt == 8) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "accurate plan: list storage keeps overflowing");
+        const int64_t ucap = ctx->mac_ucap;
+        GX_TRY(gx_ensure(ctx, ctx->far_idx, sizeof(int32_t) * (size_t)far_cap));
+        GX_TRY(gx_ensure(ctx, ctx->near_idx, sizeof(int32_t) * (size_t)near_cap));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(cmax + 1) * 2));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int32_t) * (size_t)(ucap + 1) * 2));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_e, sizeof(int64_t) * (size_t)(ucap + 1) * 4));
+        int64_t *nch = dptr<int64_t>(ctx->scratch_a), *uoff = nch + (cmax + 1);
+        int32_t *unode = dptr<int32_t>(ctx->scratch_b), *uchunk = unode + (ucap + 1);
+        int64_t *ufar = dptr<int64_t>(ctx->scratch_e), *unear = ufar + (ucap + 1), *ufo = unear + (ucap + 1),
+                *uno = ufo + (ucap + 1);
+        GX_CUDA(ctx, cudaMemsetAsync(fcnt, 0, sizeof(int32_t) * (size_t)nn, ctx->stream));
+        GX_CUDA(ctx, cudaMemsetAsync(ncnt, 0, sizeof(int32_t) * (size_t)nn, ctx->stream));
+        // root: near itself (near list {root} at index 0)
+        hc[PC_FAR] = 0;
+        hc[PC_NEAR] = 1;
+        hc[PC_NEAR_LAST] = 0;
+        hc[PC_OVF] = 0;
+        const int64_t zero = 0;
+        const int32_t one = 1, root32 = (int32_t)root;
+        GX_CUDA(ctx, cudaMemcpyAsync(ctr, hc, sizeof(hc), cudaMemcpyHostToDevice, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(nstart + root, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
+                                     ctx->stream));
+        for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
+            const int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
+            // units: chunks of each node's candidate list
+            k_mac_nchunks<<<gx_blocks(c + 1, 256), 256, 0, ctx->stream>>>(s, e, dptr<int32_t>(ctx->parent), ncnt, nch,
+                                                                         ctr);
+            GX_TRY(gx_exclusive_scan_i64(ctx, nch, uoff, c + 1));
+            const int64_t *Ud = uoff + c;  // the level's unit count, on the device
+            k_mac_units<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, ucap, unode, uchunk, ufar, unear,
+                                                                   ctr);
+            k_mac<<<gmac, 128, 0, ctx->stream>>>(Ud, 0, unode, uchunk, dptr<int32_t>(ctx->parent),
+                                                 dptr<int4>(ctx->child), hl, R32, theta2, nstart, ncnt,
+                                                 dptr<int32_t>(ctx->near_idx), ufar, unear, nullptr, nullptr, far_cap,
+                                                 near_cap, ctr);
+            GX_TRY(gx_exclusive_scan_i64_devn(ctx, ufar, ufo, Ud, 1, ucap + 1));
+            GX_TRY(gx_exclusive_scan_i64_devn(ctx, unear, uno, Ud, 1, ucap + 1));
+            k_mac<<<gmac, 128, 0, ctx->stream>>>(Ud, 1, unode, uchunk, dptr<int32_t>(ctx->parent),
+                                                 dptr<int4>(ctx->child), hl, R32, theta2, nstart, ncnt,
+                                                 dptr<int32_t>(ctx->near_idx), ufo, uno, dptr<int32_t>(ctx->far_idx),
+                                                 dptr<int32_t>(ctx->near_idx), far_cap, near_cap, ctr);
+            k_mac_node_lists<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, ufo, uno, ctr, fstart, fcnt,
+                                                                        nstart, ncnt);
+            k_mac_advance<<<1, 1, 0, ctx->stream>>>(Ud, ufo, uno, ctr);
+            ctx->launches += 7;
+            GX_CUDA(ctx, cudaGetLastError());
         }
+        GX_CUDA(ctx, cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (!hc[PC_OVF]) break;
+        if (hc[PC_OVF] & OVF_UNITS) ctx->mac_ucap *= 4;
+        if (hc[PC_OVF] & OVF_FAR) far_cap *= 4;
+        if (hc[PC_OVF] & OVF_NEAR) near_cap *= 4;
     }
+    const int64_t far_tot = hc[PC_FAR];
+    ctx->n_near_pairs = ctx->n_levels > 1 ? hc[PC_NEAR_LAST] : 1;  // a one-leaf tree: the root near itself
     ctx->n_far_pairs = far_tot;
     GX_TRY(gx_ensure(ctx, ctx->has_far_acc, (size_t)nn));
     k_flag_i32<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, fcnt, dptr<uint8_t>(ctx->has_far_acc));

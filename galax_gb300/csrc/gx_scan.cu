@@ -101,6 +101,49 @@ __global__ void k_scan_apply(const T *in, T *out, int64_t n, const T *sums) {
     }
 }
 
+// Device-length forms: the length is *n_dev + n_add (at most n_cap), read on the
+// device, so a scan over a count produced by an earlier kernel needs no host round
+// trip.  Grids are sized for n_cap; blocks past the length do no work.
+__device__ __forceinline__ int64_t dev_len(const int64_t *n_dev, int64_t n_add, int64_t n_cap) {
+    int64_t n = *n_dev + n_add;
+    return n < n_cap ? n : n_cap;
+}
+
+__global__ void k_scan_sums_dn(const int64_t *in, const int64_t *n_dev, int64_t n_add, int64_t n_cap, int64_t *sums) {
+    __shared__ int64_t tot;
+    const int64_t n = dev_len(n_dev, n_add, n_cap);
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    int64_t s = 0;
+    if (base < n)
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            int64_t i = base + (int64_t)threadIdx.x * SCAN_ITEMS + k;
+            if (i < n) s += in[i];
+        }
+    block_exclusive_scan<int64_t>(s, &tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_apply_dn(const int64_t *in, int64_t *out, const int64_t *n_dev, int64_t n_add, int64_t n_cap,
+                                const int64_t *sums) {
+    __shared__ int64_t tot;
+    const int64_t n = dev_len(n_dev, n_add, n_cap);
+    int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    if (base >= n) return;  // uniform per block
+    int64_t v[SCAN_ITEMS];
+    int64_t s = 0;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        int64_t i = base + (int64_t)threadIdx.x * SCAN_ITEMS + k;
+        v[k] = (i < n) ? in[i] : 0;
+        s += v[k];
+    }
+    int64_t run = sums[blockIdx.x] + block_exclusive_scan<int64_t>(s, &tot);
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        int64_t i = base + (int64_t)threadIdx.x * SCAN_ITEMS + k;
+        if (i < n) out[i] = run;
+        run += v[k];
+    }
+}
+
 template <class T>
 int scan_impl(gx_ctx *ctx, const T *in, T *out, int64_t n, T *total_host) {
     if (n <= 0) {
@@ -202,6 +245,20 @@ __global__ void __launch_bounds__(RS_WARPS * 32) k_rs_scatter(const uint64_t *ki
 
 int gx_exclusive_scan_i64(gx_ctx *ctx, const int64_t *in, int64_t *out, int64_t n) {
     return scan_impl<int64_t>(ctx, in, out, n, nullptr);
+}
+
+int gx_exclusive_scan_i64_devn(gx_ctx *ctx, const int64_t *in, int64_t *out, const int64_t *n_dev, int64_t n_add,
+                               int64_t n_cap) {
+    if (n_cap <= 0) return GX_OK;
+    int64_t nb = (n_cap + SCAN_TILE - 1) / SCAN_TILE;
+    GX_TRY(gx_ensure(ctx, ctx->scratch_g, sizeof(int64_t) * (nb + 1)));
+    int64_t *sums = dptr<int64_t>(ctx->scratch_g);
+    k_scan_sums_dn<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(in, n_dev, n_add, n_cap, sums);
+    k_scan_single<int64_t><<<1, SCAN_THREADS, 0, ctx->stream>>>(sums, nb, sums + nb);
+    k_scan_apply_dn<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(in, out, n_dev, n_add, n_cap, sums);
+    ctx->launches += 3;
+    GX_CUDA(ctx, cudaGetLastError());
+    return GX_OK;
 }
 
 int gx_exclusive_scan_i32(gx_ctx *ctx, const int32_t *in, int32_t *out, int64_t n, int32_t *total_host) {
