@@ -138,7 +138,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->Lff32, &ctx->pos32, &ctx->part, &ctx->items_ref.leaf, &ctx->items_ref.qb, &ctx->items_ref.nq, &ctx->items_ref.off, &ctx->items_acc.leaf, &ctx->items_acc.qb, &ctx->items_acc.nq, &ctx->items_acc.off, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
                       &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush, &ctx->adj_lx, &ctx->adj_ly, &ctx->adj_lvx, &ctx->adj_lvy, &ctx->adj_lm, &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm, &ctx->adj_lax, &ctx->adj_lay, &ctx->adj_lf, &ctx->adj_dL, &ctx->adj_dM, &ctx->adj_dMleaf, &ctx->adj_lam32, &ctx->ckpt, &ctx->seg, &ctx->ids, &ctx->perm, &ctx->roll_perms, &ctx->radius32,
                       &ctx->m2l_units.node, &ctx->m2l_units.start, &ctx->m2l_units.len, &ctx->m2l_units.node_u,
-                      &ctx->m2l_part, &ctx->plan_ctr};
+                      &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state};
     for (DevBuf *b : bufs) free_buf(*b);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -555,10 +555,15 @@ int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64
     return GX_OK;
 }
 
-static int forces_and_check(gx_ctx *ctx, bool timed) {
+// Enqueue one evaluation (the plan first if it is stale).
+static int forces_launch(gx_ctx *ctx, bool timed) {
     GX_TRY(ensure_plan(ctx));
     GX_CUDA(ctx, cudaMemsetAsync(ctx->status.p, 0, sizeof(unsigned), ctx->stream));
-    GX_TRY(gx_forces_device(ctx, timed));
+    return gx_forces_device(ctx, timed);
+}
+
+// Wait for the stream, check the device status word, record the pass timings.
+static int forces_finish(gx_ctx *ctx, bool timed) {
     unsigned st = 0;
     GX_TRY(sync_status(ctx, &st));
     if (timed && ctx->n_nodes > 0) {
@@ -575,19 +580,24 @@ static int forces_and_check(gx_ctx *ctx, bool timed) {
     return GX_OK;
 }
 
+static int forces_and_check(gx_ctx *ctx, bool timed) {
+    GX_TRY(forces_launch(ctx, timed));
+    return forces_finish(ctx, timed);
+}
+
 int gx_compute_forces(gx_ctx *ctx, const double *x, const double *y, const double *m, double *ax, double *ay) {
     GX_TRY(check_ctx(ctx));
     if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree: call gx_build_tree or gx_upload_tree first");
     if (!x || !y || !m || !ax || !ay) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null array");
     int64_t n = ctx->n_bodies;
     GX_TRY(upload_bodies_impl(ctx, n, x, y, nullptr, nullptr, m, nullptr, nullptr, false));
-    GX_TRY(forces_and_check(ctx, true));
+    GX_TRY(forces_launch(ctx, true));
+    // the read-back is queued behind the evaluation: one wait for both, then the status
     if (n > 0) {
         GX_CUDA(ctx, cudaMemcpyAsync(ax, ctx->ax.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(ay, ctx->ay.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     }
-    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return GX_OK;
+    return forces_finish(ctx, true);
 }
 
 int gx_forces_resident(gx_ctx *ctx) {

@@ -122,6 +122,7 @@ struct gx_ctx {
     } m2l_units;
     DevBuf m2l_part;  // per-unit partial locals of nodes cut into several units
     DevBuf plan_ctr;       // ACCURATE plan: device running totals and overflow flags
+    DevBuf tree_state;     // tree build: device round state and level starts
     int64_t mac_ucap = 0;  // ACCURATE plan: capacity of the per-level unit arrays
     DevBuf part;                   // per-item partial accelerations
     int64_t max_leaf = 0;          // largest leaf body count
@@ -177,9 +178,10 @@ int gx_poly_table_host(int p, double eps, std::vector<double> &out);
 // gx_scan.cu
 int gx_exclusive_scan_i64(gx_ctx *ctx, const int64_t *in, int64_t *out, int64_t n);
 int gx_exclusive_scan_i32(gx_ctx *ctx, const int32_t *in, int32_t *out, int64_t n, int32_t *total_host);
-// exclusive scan of min(*n_dev + n_add, n_cap) entries, the length read on the device
+// exclusive scan of min(*n_dev + n_add, n_cap) entries, the length read on the device;
+// the grand total goes to *total_dev when given
 int gx_exclusive_scan_i64_devn(gx_ctx *ctx, const int64_t *in, int64_t *out, const int64_t *n_dev, int64_t n_add,
-                               int64_t n_cap);
+                               int64_t n_cap, int64_t *total_dev = nullptr);
 int gx_radix_sort_u64(gx_ctx *ctx, uint64_t *keys, uint32_t *vals, int64_t n, int begin_bit, int end_bit,
                       uint64_t *keys_alt, uint32_t *vals_alt, bool *result_in_alt);
 // gx_kdk.cu

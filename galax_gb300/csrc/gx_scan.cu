@@ -248,13 +248,13 @@ int gx_exclusive_scan_i64(gx_ctx *ctx, const int64_t *in, int64_t *out, int64_t 
 }
 
 int gx_exclusive_scan_i64_devn(gx_ctx *ctx, const int64_t *in, int64_t *out, const int64_t *n_dev, int64_t n_add,
-                               int64_t n_cap) {
+                               int64_t n_cap, int64_t *total_dev) {
     if (n_cap <= 0) return GX_OK;
     int64_t nb = (n_cap + SCAN_TILE - 1) / SCAN_TILE;
     GX_TRY(gx_ensure(ctx, ctx->scratch_g, sizeof(int64_t) * (nb + 1)));
     int64_t *sums = dptr<int64_t>(ctx->scratch_g);
     k_scan_sums_dn<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(in, n_dev, n_add, n_cap, sums);
-    k_scan_single<int64_t><<<1, SCAN_THREADS, 0, ctx->stream>>>(sums, nb, sums + nb);
+    k_scan_single<int64_t><<<1, SCAN_THREADS, 0, ctx->stream>>>(sums, nb, total_dev ? total_dev : sums + nb);
     k_scan_apply_dn<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(in, out, n_dev, n_add, n_cap, sums);
     ctx->launches += 3;
     GX_CUDA(ctx, cudaGetLastError());

@@ -92,41 +92,92 @@ __global__ void k_chunk_ranges(int64_t n, int64_t n_max, int64_t nl, int32_t *rs
 }
 
 // ---- parent rounds (lib.rs:269-354) ----
-__global__ void k_round_heads(int64_t s, int64_t c, const uint64_t *__restrict__ keys, const int32_t *__restrict__ bs,
-                              unsigned sh, int32_t *head) {
+// The rounds run without host round trips: the level bounds, the shift and the round's
+// segment and group counts live in a device state block, every kernel of a round reads
+// them there, and the host only waits once per batch of rounds.  A round whose new
+// level would not fit the node storage sets the overflow flag; the build is then redone
+// with more storage.
+enum { TS_S = 0, TS_E = 1, TS_C = 2, TS_SHIFT = 3, TS_NSEG = 4, TS_NG = 5, TS_FLAGS = 6, TS_ROUNDS = 7, TS_N = 8 };
+enum { TS_DONE = 1, TS_OVERFLOW = 2, TS_STUCK = 4 };
+constexpr int TS_MAX_ROUNDS = 400;  // level starts kept: TS_MAX_ROUNDS + 2
+
+__device__ __forceinline__ bool round_off(const int64_t *st) { return st[TS_FLAGS] != 0; }
+
+__global__ void k_round_heads(const int64_t *st, const uint64_t *__restrict__ keys, const int32_t *__restrict__ bs,
+                              int64_t *head) {
+    if (round_off(st)) return;
+    const int64_t s = st[TS_S], c = st[TS_C];
+    const unsigned sh = (unsigned)st[TS_SHIFT] & 63u;
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c) return;
     uint64_t g = keys[bs[s + i]] >> sh;
     head[i] = (i == 0) ? 1 : (g != (keys[bs[s + i - 1]] >> sh));
 }
 
-__global__ void k_seg_start(int64_t c, const int32_t *head, const int32_t *segex, int32_t *segstart) {
+__global__ void k_seg_start(const int64_t *st, const int64_t *head, const int64_t *segex, int64_t *segstart) {
+    if (round_off(st)) return;
+    const int64_t c = st[TS_C];
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c) return;
-    if (head[i]) segstart[segex[i]] = (int32_t)i;
+    if (head[i]) segstart[segex[i]] = i;
 }
 
-__global__ void k_seg_groups(int64_t nseg, int64_t c, const int32_t *segstart, int32_t *gcnt) {
+__global__ void k_seg_groups(const int64_t *st, const int64_t *segstart, int64_t *gcnt) {
+    if (round_off(st)) return;
+    const int64_t c = st[TS_C], nseg = st[TS_NSEG];
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nseg) return;
     int64_t len = ((k + 1 < nseg) ? segstart[k + 1] : c) - segstart[k];
-    gcnt[k] = (int32_t)((len + 3) / 4);
+    gcnt[k] = (len + 3) / 4;
 }
 
-__global__ void k_assign(int64_t s, int64_t e, int64_t c, const int32_t *head, const int32_t *segex,
-                         const int32_t *segstart, const int32_t *goff, int32_t *parent, int32_t *child) {
+// the new level must fit the node storage; its child slots start empty
+__global__ void k_round_open(int64_t *st, int64_t cap_nodes, int4 *child) {
+    if (round_off(st)) return;
+    const int64_t e = st[TS_E], ng = st[TS_NG];
+    if (e + ng > cap_nodes) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) st[TS_FLAGS] |= TS_OVERFLOW;
+        return;
+    }
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < ng) child[e + g] = make_int4(-1, -1, -1, -1);
+}
+
+__global__ void k_assign(const int64_t *st, const int64_t *head, const int64_t *segex, const int64_t *segstart,
+                         const int64_t *goff, int32_t *parent, int32_t *child) {
+    if (round_off(st)) return;
+    const int64_t s = st[TS_S], e = st[TS_E], c = st[TS_C];
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c) return;
-    int32_t seg = segex[i] + head[i] - 1;
-    int32_t pos = (int32_t)i - segstart[seg];
-    int64_t g = (int64_t)goff[seg] + pos / 4;
+    int64_t seg = segex[i] + head[i] - 1;
+    int64_t pos = i - segstart[seg];
+    int64_t g = goff[seg] + pos / 4;
     parent[s + i] = (int32_t)(e + g);
     child[(e + g) * 4 + (pos & 3)] = (int32_t)(s + i);
 }
 
-__global__ void k_parent_fields(int64_t e, int64_t ng, double *cx, double *cy, double *hw, double *mass, double *comx,
+// after a round: record the new level, move to it, and stop at a single node
+__global__ void k_round_close(int64_t *st, int64_t *level_start) {
+    if (round_off(st)) return;
+    const int64_t e = st[TS_E], ng = st[TS_NG];
+    if (st[TS_ROUNDS] >= TS_MAX_ROUNDS) {
+        st[TS_FLAGS] |= TS_STUCK;
+        return;
+    }
+    const int64_t r = ++st[TS_ROUNDS];
+    level_start[r + 1] = e + ng;
+    st[TS_S] = e;
+    st[TS_E] = e + ng;
+    st[TS_C] = ng;
+    st[TS_SHIFT] += 2;
+    if (ng <= 1) st[TS_FLAGS] |= TS_DONE;
+}
+
+__global__ void k_parent_fields(const int64_t *st, double *cx, double *cy, double *hw, double *mass, double *comx,
                                 double *comy, int32_t *bs, int32_t *be, const int4 *child, int32_t *parent,
                                 uint8_t *is_leaf) {
+    if (round_off(st)) return;
+    const int64_t e = st[TS_E], ng = st[TS_NG];
     int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     int64_t q = e + g;
@@ -193,60 +244,73 @@ static int ensure_nodes(gx_ctx *ctx, int64_t need) {
 // Builds nodes from leaf ranges already in scratch (rs, re as int32), using ctx->keys
 // (Morton keys of the tree-ordered bodies).
 static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, int64_t nl) {
-    int64_t guess = nl * 4 + 64;
-    GX_TRY(ensure_nodes(ctx, guess));
-    k_leaves<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(
-        dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->m), rs, re, nl, dptr<double>(ctx->cx),
-        dptr<double>(ctx->cy), dptr<double>(ctx->hw), dptr<double>(ctx->mass), dptr<double>(ctx->comx),
-        dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), dptr<int4>(ctx->child),
-        dptr<int32_t>(ctx->parent), dptr<uint8_t>(ctx->is_leaf));
-    ctx->launches++;
-    GX_CUDA(ctx, cudaGetLastError());
-    ctx->level_start.clear();
-    ctx->level_start.push_back(0);
-    int64_t s = 0, e = nl, nn = nl;
-    unsigned shift = 2;
-    // per-round scratch: head, segex, segstart, gcnt, goff (int32, <= count each)
-    GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int32_t) * (size_t)(nl + 1) * 5));
-    int rounds = 0;
-    while (e - s > 1) {
-        if (++rounds > 400) return gx_fail(ctx, GX_ERR_STATE, "tree build did not converge");
-        int64_t c = e - s;
-        int32_t *head = dptr<int32_t>(ctx->scratch_a);
-        int32_t *segex = head + c;
-        int32_t *segstart = segex + c;
-        int32_t *gcnt = segstart + c;
-        int32_t *goff = gcnt + c;
-        unsigned sh = shift & 63u;
-        k_round_heads<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, c, dptr<uint64_t>(ctx->keys),
-                                                                   dptr<int32_t>(ctx->bs), sh, head);
-        int32_t nseg = 0;
-        GX_TRY(gx_exclusive_scan_i32(ctx, head, segex, c, &nseg));
-        k_seg_start<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(c, head, segex, segstart);
-        k_seg_groups<<<gx_blocks(nseg, 256), 256, 0, ctx->stream>>>(nseg, c, segstart, gcnt);
-        int32_t ng = 0;
-        GX_TRY(gx_exclusive_scan_i32(ctx, gcnt, goff, nseg, &ng));
-        GX_TRY(ensure_nodes(ctx, nn + ng));
-        GX_CUDA(ctx, cudaMemsetAsync(dptr<int4>(ctx->child) + e, 0xFF, sizeof(int4) * (size_t)ng, ctx->stream));
-        k_assign<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, c, head, segex, segstart, goff,
-                                                             dptr<int32_t>(ctx->parent), dptr<int32_t>(ctx->child));
-        k_parent_fields<<<gx_blocks(ng, 128), 128, 0, ctx->stream>>>(
-            e, ng, dptr<double>(ctx->cx), dptr<double>(ctx->cy), dptr<double>(ctx->hw), dptr<double>(ctx->mass),
-            dptr<double>(ctx->comx), dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be),
-            dptr<int4>(ctx->child), dptr<int32_t>(ctx->parent), dptr<uint8_t>(ctx->is_leaf));
-        ctx->launches += 5;
-        GX_CUDA(ctx, cudaGetLastError());
-        ctx->level_start.push_back(e);
-        s = e;
-        e = e + ng;
-        nn = e;
-        shift += 2;
+    if (nl <= 0) return gx_fail(ctx, GX_ERR_STATE, "tree build: no leaves");
+    // node storage: the last build's node count (a rebuild every step keeps it), else a
+    // guess; a round that overflows it makes the build start again with more
+    int64_t cap = std::max<int64_t>(nl * 4 + 64, ctx->n_nodes + ctx->n_nodes / 8 + 64);
+    // per-round scratch: head, segex, segstart, gcnt, goff (int64, <= nl each)
+    GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(nl + 1) * 5));
+    GX_TRY(gx_ensure(ctx, ctx->tree_state, sizeof(int64_t) * (TS_N + TS_MAX_ROUNDS + 2)));
+    int64_t *st = dptr<int64_t>(ctx->tree_state);
+    int64_t *lstart = st + TS_N;  // level starts
+    int64_t *head = dptr<int64_t>(ctx->scratch_a);
+    int64_t *segex = head + (nl + 1), *segstart = segex + (nl + 1), *gcnt = segstart + (nl + 1),
+            *goff = gcnt + (nl + 1);
+    const unsigned gb = gx_blocks(nl, 256);
+    int64_t hs[TS_N];
+    for (int attempt = 0;; attempt++) {
+        if (attempt == 8) return gx_fail(ctx, GX_ERR_ALLOC, "tree build: node storage keeps overflowing");
+        GX_TRY(ensure_nodes(ctx, cap));
+        k_leaves<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(
+            dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->m), rs, re, nl, dptr<double>(ctx->cx),
+            dptr<double>(ctx->cy), dptr<double>(ctx->hw), dptr<double>(ctx->mass), dptr<double>(ctx->comx),
+            dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), dptr<int4>(ctx->child),
+            dptr<int32_t>(ctx->parent), dptr<uint8_t>(ctx->is_leaf));
+        ctx->launches++;
+        const int64_t init[TS_N] = {0, nl, nl, 2, 0, 0, nl > 1 ? 0 : TS_DONE, 0};
+        const int64_t ls01[2] = {0, nl};
+        GX_CUDA(ctx, cudaMemcpyAsync(st, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(lstart, ls01, sizeof(ls01), cudaMemcpyHostToDevice, ctx->stream));
+        // rounds in batches: the last build's round count first, then 8 at a time
+        int batch = std::max(8, ctx->n_levels > 0 ? ctx->n_levels : 8);
+        int issued = 0;
+        for (;;) {
+            for (int r = 0; r < batch; r++) {
+                k_round_heads<<<gb, 256, 0, ctx->stream>>>(st, dptr<uint64_t>(ctx->keys), dptr<int32_t>(ctx->bs), head);
+                GX_TRY(gx_exclusive_scan_i64_devn(ctx, head, segex, st + TS_C, 0, nl, st + TS_NSEG));
+                k_seg_start<<<gb, 256, 0, ctx->stream>>>(st, head, segex, segstart);
+                k_seg_groups<<<gb, 256, 0, ctx->stream>>>(st, segstart, gcnt);
+                GX_TRY(gx_exclusive_scan_i64_devn(ctx, gcnt, goff, st + TS_NSEG, 0, nl, st + TS_NG));
+                k_round_open<<<gb, 256, 0, ctx->stream>>>(st, cap, dptr<int4>(ctx->child));
+                k_assign<<<gb, 256, 0, ctx->stream>>>(st, head, segex, segstart, goff, dptr<int32_t>(ctx->parent),
+                                                      dptr<int32_t>(ctx->child));
+                k_parent_fields<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(
+                    st, dptr<double>(ctx->cx), dptr<double>(ctx->cy), dptr<double>(ctx->hw), dptr<double>(ctx->mass),
+                    dptr<double>(ctx->comx), dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be),
+                    dptr<int4>(ctx->child), dptr<int32_t>(ctx->parent), dptr<uint8_t>(ctx->is_leaf));
+                k_round_close<<<1, 1, 0, ctx->stream>>>(st, lstart);
+                ctx->launches += 7;
+            }
+            GX_CUDA(ctx, cudaGetLastError());
+            issued += batch;
+            GX_CUDA(ctx, cudaMemcpyAsync(hs, st, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+            GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            if (hs[TS_FLAGS] & TS_STUCK) return gx_fail(ctx, GX_ERR_STATE, "tree build did not converge");
+            if (hs[TS_FLAGS] != 0) break;
+            batch = 8;
+        }
+        if (!(hs[TS_FLAGS] & TS_OVERFLOW)) break;
+        cap *= 2;
     }
-    ctx->level_start.push_back(nn);
+    const int64_t rounds = hs[TS_ROUNDS];
+    std::vector<int64_t> ls((size_t)rounds + 2);
+    GX_CUDA(ctx, cudaMemcpyAsync(ls.data(), lstart, sizeof(int64_t) * ls.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->level_start.assign(ls.begin(), ls.end());
+    const int64_t nn = ls.back();
     ctx->n_nodes = nn;
     ctx->n_leaves = nl;
     ctx->n_levels = (int32_t)ctx->level_start.size() - 1;
-    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return GX_OK;
 }
 

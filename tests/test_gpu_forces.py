@@ -86,6 +86,33 @@ def test_accurate_mode_fp64_matches_oracle(G, oracle, preset, n):
     assert err.max() < TOL_FP64, f"max {err.max():.3e}"
 
 
+def test_accurate_plan_regrows_its_storage(G, oracle):
+    """A tiny opening angle (0.02) on 2500 leaves of 8 bodies: almost every leaf pair is
+    near (6.2M leaf near pairs, more list units and entries than the plan's first
+    capacities), so the plan overflows, grows its arrays and is redone.  The lists and
+    forces must equal the oracle's."""
+    from galax_gb300 import presets
+    n = 20_000
+    b = presets.uniform(n, seed=11)
+    ob, t, v, u, eps = oracle_case(oracle, b, 8, presets.BOUNDS["uniform"], 4)
+    R = oracle.node_radii(ob, t)
+    far, near = oracle.mac_lists_build(t, R, 0.02)
+    ref = ob.copy()
+    oracle.compute_fmm_force_mac(ref, t, far, near, 4, eps)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=4, eps64=eps))
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_FP64, 0.02)
+    ctx.upload_tree_data(t, v, u)
+    ctx.upload_bodies(G.Bodies.from_arrays(ob.x.copy(), ob.y.copy(), ob.mass.copy()))
+    ax, ay = np.zeros(n), np.zeros(n)
+    ctx.compute_forces(ob.x.copy(), ob.y.copy(), ob.mass.copy(), ax, ay)
+    n_far, n_near, _ = ctx.plan_info()
+    ctx.close()
+    assert n_far == far.off[-1]
+    assert n_near == int(np.diff(near.off)[: t.n_leaves].sum())
+    err = rel_vec_err(ax, ay, ref.ax, ref.ay)
+    assert err.max() < TOL_FP64, f"max {err.max():.3e}"
+
+
 @pytest.mark.parametrize("preset,n", [("uniform", 10_000), ("plummer", 30_000)])
 def test_mixed_precision_error_budget(G, oracle, preset, n):
     """Mixed form vs FP64 form, and both vs the exact FP64 N^2 sum on 1000 samples:
