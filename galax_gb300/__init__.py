@@ -129,6 +129,13 @@ def _f64(a) -> np.ndarray:
 N2_STATIC_MAX_SAMPLES = 4096
 
 
+def _mag_rel_err(ax, ay, ex, ey):
+    """||a| - |a*|| / max(|a*|, 1e-20) per body (validate_fmm, galax-core/src/lib.rs:1553-1557)."""
+    fm = np.sqrt(np.asarray(ax) ** 2 + np.asarray(ay) ** 2)
+    em = np.sqrt(np.asarray(ex) ** 2 + np.asarray(ey) ** 2)
+    return np.abs(fm - em) / np.maximum(np.abs(em), 1e-20)
+
+
 def n2_sampled_static(x_dev: int, y_dev: int, m_dev: int, n: int, eps: float, idx, stream: int = 0):
     """Exact FP64 softened forces on sampled targets from the caller's device arrays
     (addresses of n float64 values each), without a context and without allocating
@@ -378,6 +385,39 @@ class GpuContext:
         if mx > threshold:
             raise GpuError(0, f"GPU crosscheck max relative error {mx:.2e} exceeds threshold {threshold:.2e}")
         return mx, mean, rel.size
+
+    def validate_fmm(self, bodies: Bodies, sample_size: int, seed: int = 0):
+        """validate_fmm (galax-core/src/lib.rs:1502-1564): the FMM of the context's mode and
+        precision on all bodies, the exact FP64 softened sum (GPU) on ``sample_size`` bodies
+        drawn without replacement, and the magnitude error ||a| - |a*|| / max(|a*|, 1e-20)
+        of each.  Returns (sample_size, max, mean, 0.0) as the reference does.  The draw is
+        seeded here (the reference shuffles with an unseeded generator).  ``bodies`` must be
+        in the order the context's tree was built on; they become the resident bodies."""
+        n = len(bodies)
+        k = min(int(sample_size), n)
+        self.upload_bodies(bodies)
+        self.forces_resident()
+        out = Bodies.new(n)
+        self.download_bodies(out)
+        idx = np.sort(np.random.default_rng(seed).permutation(n)[:k]).astype(np.int64)
+        ex, ey = self.n2_sampled(idx)
+        rel = _mag_rel_err(out.ax[idx], out.ay[idx], ex, ey)
+        mean = float(rel.sum()) / k if k else float("nan")  # the reference divides by sample_size
+        return k, float(rel.max()) if k else 0.0, mean, 0.0
+
+    def n2_regression(self, bodies: Bodies) -> float:
+        """n2_regression (galax-core/src/lib.rs:1567-1598): the FMM against the exact FP64 sum
+        on every body (N <= 2000), largest magnitude error.  ``bodies`` as for validate_fmm."""
+        n = len(bodies)
+        if n > 2000:
+            raise ValueError("n2_regression only valid for N <= 2000")
+        self.upload_bodies(bodies)
+        self.forces_resident()
+        out = Bodies.new(n)
+        self.download_bodies(out)
+        ex, ey = self.n2_sampled(np.arange(n, dtype=np.int64))
+        rel = _mag_rel_err(out.ax, out.ay, ex, ey)
+        return float(rel.max()) if n else 0.0
 
     def n2_debug(self, bodies: Bodies):
         """n2_debug (galax-gpu/src/lib.rs:670-714): exact FP64 softened forces for every body."""

@@ -100,6 +100,46 @@ def test_sampled_n2_matches_oracle(G, oracle, preset, n):
     ctx.close()
 
 
+def test_validate_fmm_and_n2_regression_match_the_oracle(G, oracle):
+    """validate_fmm / n2_regression (galax-core/src/lib.rs:1502-1598) in REF mode: the
+    sampled magnitude errors equal the ones formed from the oracle's REF FMM and exact
+    sum on the same samples; n2_regression refuses N > 2000."""
+    from galax_gb300 import presets
+    n, p = 5_000, 4
+    b = presets.uniform(n, seed=21)
+    ob, t, v, u, eps = oracle_case(oracle, b, 32, presets.BOUNDS["uniform"], p)
+    ref = ob.copy()
+    oracle.compute_fmm_force(ref, t, v, u, p, eps, oracle.MODE_REF)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 20, p=p, eps64=eps))
+    gb = b.copy()
+    ctx.build_tree(gb, 32, presets.BOUNDS["uniform"])
+    k, mx, mean, zero = ctx.validate_fmm(gb, 400, seed=5)
+    idx = np.sort(np.random.default_rng(5).permutation(n)[:400])
+    rx, ry = oracle.n2_sampled(ob.x, ob.y, ob.mass, eps, idx)
+    rel = G._mag_rel_err(ref.ax[idx], ref.ay[idx], rx, ry)
+    assert (k, zero) == (400, 0.0)
+    assert mx == pytest.approx(float(rel.max()), rel=1e-8)
+    assert mean == pytest.approx(float(rel.mean()), rel=1e-8)
+    # N <= 2000: the full regression
+    m = 1_500
+    b2 = presets.uniform(m, seed=22)
+    ob2, t2, v2, u2, eps2 = oracle_case(oracle, b2, 32, presets.BOUNDS["uniform"], p)
+    ref2 = ob2.copy()
+    oracle.compute_fmm_force(ref2, t2, v2, u2, p, eps2, oracle.MODE_REF)
+    d2 = ob2.copy()
+    oracle.n2_force(d2, eps2)
+    c2 = G.GpuContext(G.GpuConfig(max_n=m, max_nodes=1 << 20, p=p, eps64=eps2))
+    g2 = b2.copy()
+    c2.build_tree(g2, 32, presets.BOUNDS["uniform"])
+    got = c2.n2_regression(g2)
+    want = float(G._mag_rel_err(ref2.ax, ref2.ay, d2.ax, d2.ay).max())
+    assert got == pytest.approx(want, rel=1e-8)
+    with pytest.raises(ValueError):
+        ctx.n2_regression(gb)
+    ctx.close()
+    c2.close()
+
+
 def test_accurate_mixed_kdk_conserves_momentum(G):
     """The mixed ACCURATE form over 20 steps of the galaxy preset: total momentum stays
     at its initial value relative to sum m|v| (the reference has no device check of this)."""
