@@ -949,8 +949,11 @@ __global__ void __launch_bounds__(128, 7) k_p2p32_items(int64_t n_items, const i
 // The same near field when every leaf holds at most 32 bodies (n_max <= 32): each
 // source leaf is one row, so the item's source-leaf table (first body, end, FP32
 // frame shift) is written to shared memory once per item and read back by broadcast
-// as the rows go, and there is no row loop.  Same arithmetic and accumulation order
-// as k_p2p32_items with one target chunk.
+// as the rows go, and there is no row loop.  Each lane takes two targets (t and t + 16)
+// and half of every row's sources (the quads 4h, 4h + 8, ... of half h), so one
+// broadcast load of four sources serves eight interactions; the two halves' sums of a
+// target are added (half 0 first) at the end of the item.  Same per-interaction
+// arithmetic as k_p2p32_items.
 __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const int32_t *__restrict__ item_leaf,
                                                     const int64_t *__restrict__ item_qb, const int32_t *__restrict__ item_nq,
                                                     const float4 *__restrict__ pos, const double *__restrict__ comx,
@@ -960,6 +963,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
     __shared__ __align__(16) float sx[4][32], sy[4][32], sm[4][32];
     __shared__ __align__(16) int4 meta[4][32];  // per source leaf: begin, end, shift x, shift y (FP32 bits)
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int half = lane >> 4, tl = lane & 15;  // lane: targets tl and tl + 16, source quads of its half
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
         const int32_t leaf = item_leaf[it];
@@ -977,11 +981,13 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
         const unsigned ownm = __ballot_sync(0xffffffffu, own_lane);
         const int kown = ownm ? __ffs(ownm) - 1 : -1;
         __syncwarp();
-        const int32_t i = t0 + lane;
-        const float4 me = i < t1 ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const uint64_t XI = pk2(me.x, me.x), YI = pk2(me.y, me.y), E2 = pk2(eps2, eps2);
-        uint64_t AXa = 0, AYa = 0, AXb = 0, AYb = 0;  // bit pattern 0 = (0.f, 0.f)
-        float axs = 0.f, ays = 0.f;
+        const int32_t iA = t0 + tl, iB = t0 + tl + 16;
+        const float4 mA = iA < t1 ? pos[iA] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 mB = iB < t1 ? pos[iB] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint64_t XA = pk2(mA.x, mA.x), YA = pk2(mA.y, mA.y), XB = pk2(mB.x, mB.x), YB = pk2(mB.y, mB.y);
+        const uint64_t E2 = pk2(eps2, eps2);
+        uint64_t AXA = 0, AYA = 0, AXB = 0, AYB = 0;
+        float sxA = 0.f, syA = 0.f, sxB = 0.f, syB = 0.f;
         auto fetch = [&](int4 m) -> float4 {
             int j = m.x + lane;
             float4 v = j < m.y ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -999,55 +1005,74 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
             __syncwarp();
             const int2 se = *reinterpret_cast<const int2 *>(&meta[w][k]);  // this row's begin, end
             const int ns = se.y - se.x;
-            auto quad = [&](int kk) {
-                float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
-                float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
-                float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
-                uint64_t dx0 = sub2(pk2(X.x, X.y), XI), dy0 = sub2(pk2(Y.x, Y.y), YI);
-                uint64_t dx1 = sub2(pk2(X.z, X.w), XI), dy1 = sub2(pk2(Y.z, Y.w), YI);
-                uint64_t r0 = fma2(dx0, dx0, fma2(dy0, dy0, E2));
-                uint64_t r1 = fma2(dx1, dx1, fma2(dy1, dy1, E2));
-                float ra, rb;
-                upk2(r0, ra, rb);
-                uint64_t i0 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
-                upk2(r1, ra, rb);
-                uint64_t i1 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
-                uint64_t f0 = mul2(pk2(Mq.x, Mq.y), mul2(mul2(i0, i0), i0));
-                uint64_t f1 = mul2(pk2(Mq.z, Mq.w), mul2(mul2(i1, i1), i1));
-                AXa = fma2(f0, dx0, AXa);
-                AYa = fma2(f0, dy0, AYa);
-                AXb = fma2(f1, dx1, AXb);
-                AYb = fma2(f1, dy1, AYb);
-            };
-            int k0 = 0;  // sources below k0 are done
-            if (k != kown) {
-                if (ns == 32) {
+            if (ns == 32 && k != kown) {
+                // full rows of other leaves on packed .f32x2: sources (2v, 2v + 1) per instruction
 #pragma unroll
-                    for (int kk = 0; kk < 32; kk += 4) quad(kk);
-                    k0 = 32;
-                } else {
-                    for (k0 = 0; k0 + 4 <= ns; k0 += 4) quad(k0);
+                for (int q = 0; q < 4; q++) {
+                    const int kk = 8 * q + 4 * half;
+                    float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
+                    float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
+                    float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
+                    const uint64_t X0 = pk2(X.x, X.y), X1 = pk2(X.z, X.w), Y0 = pk2(Y.x, Y.y), Y1 = pk2(Y.z, Y.w);
+                    const uint64_t M0 = pk2(Mq.x, Mq.y), M1 = pk2(Mq.z, Mq.w);
+                    auto pair = [&](uint64_t XS, uint64_t YS, uint64_t MS, uint64_t XI, uint64_t YI, uint64_t &AX,
+                                    uint64_t &AY) {
+                        uint64_t dx = sub2(XS, XI), dy = sub2(YS, YI);
+                        uint64_t r = fma2(dx, dx, fma2(dy, dy, E2));
+                        float ra, rb;
+                        upk2(r, ra, rb);
+                        uint64_t ir = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                        uint64_t fq = mul2(MS, mul2(mul2(ir, ir), ir));
+                        AX = fma2(fq, dx, AX);
+                        AY = fma2(fq, dy, AY);
+                    };
+                    pair(X0, Y0, M0, XA, YA, AXA, AYA);
+                    pair(X0, Y0, M0, XB, YB, AXB, AYB);
+                    pair(X1, Y1, M1, XA, YA, AXA, AYA);
+                    pair(X1, Y1, M1, XB, YB, AXB, AYB);
                 }
-            }
-            for (int kk = k0; kk < ns; kk++) {
-                float xi, yi, dum;
-                upk2(XI, xi, dum);
-                upk2(YI, yi, dum);
-                float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
-                float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
-                float fk = sm[w][kk] * (ir * ir * ir);
-                fk = (k == kown && se.x + kk == i) ? 0.f : fk;
-                axs = fmaf(fk, dx, axs);
-                ays = fmaf(fk, dy, ays);
+            } else {
+                // partial or own rows: scalar, each half its own quads
+                float xa, ya, xb, yb, d;
+                upk2(XA, xa, d);
+                upk2(YA, ya, d);
+                upk2(XB, xb, d);
+                upk2(YB, yb, d);
+                for (int q = 0; q < 4; q++)
+                    for (int u = 0; u < 4; u++) {
+                        const int kk = 8 * q + 4 * half + u;
+                        if (kk >= ns) continue;
+                        const float xj = sx[w][kk], yj = sy[w][kk], mj = sm[w][kk];
+                        float dx = xj - xa, dy = yj - ya;
+                        float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                        float fk = mj * (ir * ir * ir);
+                        fk = (k == kown && se.x + kk == iA) ? 0.f : fk;
+                        sxA = fmaf(fk, dx, sxA);
+                        syA = fmaf(fk, dy, syA);
+                        dx = xj - xb;
+                        dy = yj - yb;
+                        ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                        fk = mj * (ir * ir * ir);
+                        fk = (k == kown && se.x + kk == iB) ? 0.f : fk;
+                        sxB = fmaf(fk, dx, sxB);
+                        syB = fmaf(fk, dy, syB);
+                    }
             }
             cur = nxt;
         }
-        float a0, a1, a2, a3, b0, b1, b2, b3;
-        upk2(AXa, a0, a1);
-        upk2(AXb, a2, a3);
-        upk2(AYa, b0, b1);
-        upk2(AYb, b2, b3);
-        part[it * 32 + lane] = make_float2(((a0 + a1) + (a2 + a3)) + axs, ((b0 + b1) + (b2 + b3)) + ays);
+        float a0, a1, b0, b1, c0, c1, e0, e1;
+        upk2(AXA, a0, a1);
+        upk2(AYA, b0, b1);
+        upk2(AXB, c0, c1);
+        upk2(AYB, e0, e1);
+        float xA = (a0 + a1) + sxA, yA = (b0 + b1) + syA, xB = (c0 + c1) + sxB, yB = (e0 + e1) + syB;
+        // the two halves hold the same targets over different sources: half 0 + half 1
+        const float oxA = __shfl_xor_sync(0xffffffffu, xA, 16), oyA = __shfl_xor_sync(0xffffffffu, yA, 16);
+        const float oxB = __shfl_xor_sync(0xffffffffu, xB, 16), oyB = __shfl_xor_sync(0xffffffffu, yB, 16);
+        float2 res;
+        if (half == 0) res = make_float2(xA + oxA, yA + oyA);  // target tl
+        else res = make_float2(oxB + xB, oyB + yB);             // target tl + 16 (half 0's part first)
+        part[it * 32 + lane] = res;
     }
 }
 

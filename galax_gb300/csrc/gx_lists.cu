@@ -393,11 +393,6 @@ __global__ void k_u8_to_i64(const uint8_t *in, int64_t *out, int64_t n) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = in[i];
 }
-__global__ void k_i32_to_i64(const int32_t *in, int64_t *out, int64_t n) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = in[i];
-}
-
 // ---------------------------------------------------------------- accurate mode
 // sqrt(dx*dx + dy*dy) with separately rounded operations: the same bits as the
 // oracle, so near/far decisions agree exactly.
