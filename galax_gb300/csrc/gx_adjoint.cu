@@ -270,6 +270,10 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
     auto seg_l = [&](int64_t j) { return static_cast<void *>(seg + (size_t)j * seg_stride + seg_arr); };
     const bool RB = ctx->roll_rebuild != 0;
     const uint32_t *perms = dptr<uint32_t>(ctx->roll_perms);
+    // under the rebuild policy, the trees (and plans) built while a segment is
+    // recomputed are kept and taken back by the reverse sweep instead of rebuilt
+    const bool keep_trees = RB && K > 1;
+    if (keep_trees && (int64_t)ctx->tp_cache.size() < K - 1) ctx->tp_cache.resize((size_t)(K - 1));
     // make (px, py, pm) the resident state and, under the rebuild policy, rebuild its
     // tree (the positions are already in that tree's order, so the bodies stay put)
     auto set_state = [&](const double *px, const double *py, const double *pm) -> int {
@@ -330,6 +334,7 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
                 GX_CUDA(ctx, cudaMemcpyAsync(seg_x(j) + n, ctx->y.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
                 GX_CUDA(ctx, cudaMemcpyAsync(seg_x(j) + 2 * n, ctx->m.p, b, cudaMemcpyDeviceToDevice, ctx->stream));
                 GX_CUDA(ctx, cudaMemcpyAsync(seg_l(j), current_lf(ctx), lfb, cudaMemcpyDeviceToDevice, ctx->stream));
+                if (keep_trees) gx_tree_plan_swap(ctx, ctx->tp_cache[(size_t)j]);  // keep state s+1's tree
             }
         }
         // reverse through the segment: state s+1 for s = s1-1 .. s0
@@ -347,7 +352,16 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
                 pm = seg_x(s - s0) + 2 * n;
                 pl = seg_l(s - s0);
             }
-            GX_TRY(set_state(px, py, pm));
+            if (keep_trees && s + 1 != s1) {
+                // state s+1 with the tree kept when it was recomputed: its bodies are in that
+                // tree's order, so a rebuild would reproduce the same tree and plan
+                GX_CUDA(ctx, cudaMemcpyAsync(ctx->x.p, px, b, cudaMemcpyDeviceToDevice, ctx->stream));
+                GX_CUDA(ctx, cudaMemcpyAsync(ctx->y.p, py, b, cudaMemcpyDeviceToDevice, ctx->stream));
+                GX_CUDA(ctx, cudaMemcpyAsync(ctx->m.p, pm, b, cudaMemcpyDeviceToDevice, ctx->stream));
+                gx_tree_plan_swap(ctx, ctx->tp_cache[(size_t)(s - s0)]);
+            } else {
+                GX_TRY(set_state(px, py, pm));
+            }
             const double c = (s + 1 == T) ? h : dt;  // a_{s+1} feeds one half kick at T, two elsewhere
             if (RB) {
                 // cotangents of state s+1 are in its (rebuilt) order until the force VJP is done
@@ -388,6 +402,8 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
         size_t tot = ctx->ckpt.bytes + ctx->seg.bytes + ctx->adj_dL.bytes + ctx->adj_dM.bytes + ctx->adj_dMleaf.bytes +
                      ctx->adj_lam32.bytes + (ctx->roll_rebuild ? ctx->roll_perms.bytes : 0);
         for (DevBuf *d : bufs) tot += d->bytes;
+        if (keep_trees)
+            for (const gx_tree_plan &t : ctx->tp_cache) tot += gx_tree_plan_bytes(t);
         *peak_bytes = (int64_t)tot;
     }
     return GX_OK;

@@ -54,6 +54,56 @@ static void free_buf(DevBuf &b) {
 
 static int check_ctx(gx_ctx *ctx) { return ctx ? GX_OK : GX_ERR_INVALID_ARG; }
 
+// the context's members that make up a gx_tree_plan, in a fixed order
+static void tree_plan_members(gx_ctx *ctx, DevBuf *(&m)[gx_tree_plan::N_BUFS]) {
+    DevBuf *l[gx_tree_plan::N_BUFS] = {
+        &ctx->cx, &ctx->cy, &ctx->hw, &ctx->mass, &ctx->comx, &ctx->comy, &ctx->bs, &ctx->be, &ctx->child,
+        &ctx->parent, &ctx->is_leaf, &ctx->keys, &ctx->radius, &ctx->radius32, &ctx->anc, &ctx->has_far_acc,
+        &ctx->comhl, &ctx->far_off, &ctx->far_idx, &ctx->near_off, &ctx->near_idx, &ctx->items_acc.leaf,
+        &ctx->items_acc.qb, &ctx->items_acc.nq, &ctx->items_acc.off, &ctx->m2l_units.node, &ctx->m2l_units.start,
+        &ctx->m2l_units.len, &ctx->m2l_units.node_u};
+    for (int k = 0; k < gx_tree_plan::N_BUFS; k++) m[k] = l[k];
+}
+
+void gx_tree_plan_swap(gx_ctx *ctx, gx_tree_plan &t) {
+    DevBuf *m[gx_tree_plan::N_BUFS];
+    tree_plan_members(ctx, m);
+    for (int k = 0; k < gx_tree_plan::N_BUFS; k++) std::swap(*m[k], t.b[k]);
+    std::swap(ctx->level_start, t.level_start);
+    std::swap(ctx->n_nodes, t.n_nodes);
+    std::swap(ctx->n_leaves, t.n_leaves);
+    std::swap(ctx->max_leaf, t.max_leaf);
+    std::swap(ctx->n_far_pairs, t.n_far_pairs);
+    std::swap(ctx->n_near_pairs, t.n_near_pairs);
+    std::swap(ctx->n_p2p_inter, t.n_p2p_inter);
+    std::swap(ctx->items_acc.n, t.items_n);
+    std::swap(ctx->m2l_units.n, t.units_n);
+    std::swap(ctx->n_levels, t.n_levels);
+    std::swap(ctx->have_tree, t.have_tree);
+    std::swap(ctx->aux_valid, t.aux_valid);
+    std::swap(ctx->plan_acc_valid, t.plan_acc_valid);
+    std::swap(ctx->plan_ref_valid, t.plan_ref_valid);
+    std::swap(ctx->ref_lists_valid, t.ref_lists_valid);
+    std::swap(ctx->items_acc.valid, t.items_valid);
+    std::swap(ctx->plan_p, t.plan_p);
+    std::swap(ctx->plan_eps, t.plan_eps);
+    std::swap(ctx->plan_theta, t.plan_theta);
+}
+
+size_t gx_tree_plan_bytes(const gx_tree_plan &t) {
+    size_t s = 0;
+    for (const DevBuf &d : t.b) s += d.bytes;
+    return s;
+}
+
+void gx_tree_plan_free(gx_tree_plan &t) {
+    for (DevBuf &d : t.b) {
+        if (d.p) cudaFree(d.p);
+        d.p = nullptr;
+        d.bytes = 0;
+    }
+}
+
 static int sync_status(gx_ctx *ctx, unsigned *out) {
     GX_CUDA(ctx, cudaMemcpyAsync(out, ctx->status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -140,6 +190,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->m2l_units.node, &ctx->m2l_units.start, &ctx->m2l_units.len, &ctx->m2l_units.node_u,
                       &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state};
     for (DevBuf *b : bufs) free_buf(*b);
+    for (gx_tree_plan &t : ctx->tp_cache) gx_tree_plan_free(t);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->stream2) {

@@ -21,7 +21,28 @@ struct DevBuf {
 };
 
 // Host-side error helper: records the message in the context and returns the code.
+// One tree with its ACCURATE plan, held outside the context: the node arrays, the
+// Morton keys, the per-tree auxiliaries, the near/far lists, the P2P items and the M2L
+// units, with their counts and validity flags.  gx_tree_plan_swap exchanges it with the
+// context's own (pointer swaps, no copies): a reverse rollout keeps the trees it builds
+// while recomputing a segment and takes them back instead of rebuilding.
+struct gx_tree_plan {
+    static constexpr int N_BUFS = 29;
+    DevBuf b[N_BUFS];
+    std::vector<int64_t> level_start;
+    int64_t n_nodes = 0, n_leaves = 0, max_leaf = 0, n_far_pairs = 0, n_near_pairs = 0, n_p2p_inter = 0;
+    int64_t items_n = 0, units_n = 0;
+    int32_t n_levels = 0;
+    bool have_tree = false, aux_valid = false, plan_acc_valid = false, plan_ref_valid = false,
+         ref_lists_valid = false, items_valid = false;
+    int plan_p = -1;
+    double plan_eps = -1.0, plan_theta = -1.0;
+};
+
 struct gx_ctx;
+void gx_tree_plan_swap(gx_ctx *ctx, gx_tree_plan &t);
+size_t gx_tree_plan_bytes(const gx_tree_plan &t);
+void gx_tree_plan_free(gx_tree_plan &t);
 int gx_fail(gx_ctx *ctx, int code, const std::string &msg);
 int gx_cuda_check(gx_ctx *ctx, cudaError_t e, const char *what);
 
@@ -122,6 +143,9 @@ struct gx_ctx {
     } m2l_units;
     DevBuf m2l_part;  // per-unit partial locals of nodes cut into several units
     DevBuf plan_ctr;       // ACCURATE plan: device running totals and overflow flags
+    // sizes of the last tree and plan: the first capacities of the next build and plan
+    // (their arrays may be fresh ones swapped in from a gx_tree_plan)
+    int64_t hint_nodes = 0, hint_far = 0, hint_near = 0;
     DevBuf tree_state;     // tree build: device round state and level starts
     int64_t mac_ucap = 0;  // ACCURATE plan: capacity of the per-level unit arrays
     DevBuf part;                   // per-item partial accelerations
@@ -143,6 +167,7 @@ struct gx_ctx {
     int64_t roll_rebuild = 0;
     DevBuf roll_perms;  // uint32 [T+1][n]: the permutation of every rebuild of a rollout
     bool roll_valid = false;
+    std::vector<gx_tree_plan> tp_cache;  // reverse rollout: the trees of a segment's states
 
     // scratch
     DevBuf scratch_a, scratch_b, scratch_c, scratch_d, scratch_e, scratch_f, scratch_g;

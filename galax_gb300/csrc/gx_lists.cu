@@ -936,8 +936,10 @@ int gx_plan_accurate(gx_ctx *ctx) {
         cmax = std::max<int64_t>(cmax, ctx->level_start[lv + 1] - ctx->level_start[lv]);
     // capacities: unit arrays and the far / near index arrays, kept from the last plan
     if (ctx->mac_ucap < 1024) ctx->mac_ucap = std::max<int64_t>(1024, nn);
-    int64_t far_cap = std::max<int64_t>((int64_t)(ctx->far_idx.bytes / sizeof(int32_t)), std::max<int64_t>(1 << 20, 64 * nn));
-    int64_t near_cap = std::max<int64_t>((int64_t)(ctx->near_idx.bytes / sizeof(int32_t)), std::max<int64_t>(1 << 20, 64 * nn));
+    int64_t far_cap = std::max<int64_t>({(int64_t)(ctx->far_idx.bytes / sizeof(int32_t)), int64_t(1) << 20, 64 * nn,
+                                         ctx->hint_far + ctx->hint_far / 8});
+    int64_t near_cap = std::max<int64_t>({(int64_t)(ctx->near_idx.bytes / sizeof(int32_t)), int64_t(1) << 20, 64 * nn,
+                                          ctx->hint_near + ctx->hint_near / 8});
     GX_TRY(gx_ensure(ctx, ctx->plan_ctr, sizeof(int64_t) * PC_N));
     int64_t *ctr = dptr<int64_t>(ctx->plan_ctr);
     int64_t hc[PC_N] = {0, 0, 0, 0};
@@ -1001,6 +1003,8 @@ int gx_plan_accurate(gx_ctx *ctx) {
         if (hc[PC_OVF] & OVF_NEAR) near_cap *= 4;
     }
     const int64_t far_tot = hc[PC_FAR];
+    ctx->hint_far = far_tot;
+    ctx->hint_near = hc[PC_NEAR];
     ctx->n_near_pairs = ctx->n_levels > 1 ? hc[PC_NEAR_LAST] : 1;  // a one-leaf tree: the root near itself
     ctx->n_far_pairs = far_tot;
     GX_TRY(gx_ensure(ctx, ctx->has_far_acc, (size_t)nn));

@@ -247,7 +247,7 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
     if (nl <= 0) return gx_fail(ctx, GX_ERR_STATE, "tree build: no leaves");
     // node storage: the last build's node count (a rebuild every step keeps it), else a
     // guess; a round that overflows it makes the build start again with more
-    int64_t cap = std::max<int64_t>(nl * 4 + 64, ctx->n_nodes + ctx->n_nodes / 8 + 64);
+    int64_t cap = std::max<int64_t>(nl * 4 + 64, ctx->hint_nodes + ctx->hint_nodes / 8 + 64);
     // per-round scratch: head, segex, segstart, gcnt, goff (int64, <= nl each)
     GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(nl + 1) * 5));
     GX_TRY(gx_ensure(ctx, ctx->tree_state, sizeof(int64_t) * (TS_N + TS_MAX_ROUNDS + 2)));
@@ -309,6 +309,7 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
     ctx->level_start.assign(ls.begin(), ls.end());
     const int64_t nn = ls.back();
     ctx->n_nodes = nn;
+    ctx->hint_nodes = nn;
     ctx->n_leaves = nl;
     ctx->n_levels = (int32_t)ctx->level_start.size() - 1;
     return GX_OK;
