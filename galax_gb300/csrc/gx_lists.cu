@@ -494,13 +494,15 @@ __global__ void k_mac_units(int64_t s, int64_t e, const int64_t *uoff, int64_t u
     }
 }
 
-// pass 0: per-unit counts (ufar, unear); pass 1: write at the running totals plus the
-// per-unit offsets.  A grid-stride loop over the level's units, one warp per unit.
+// pass 0: per-unit counts (ufar, unear), and each candidate's decisions (far mask in
+// the low nibble, near mask in the high one, one bit per child slot) in dec; pass 1:
+// the children written at the running totals plus the per-unit offsets, from dec
+// without testing again.  A grid-stride loop over the level's units, one warp per unit.
 __global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const int32_t *uchunk, const int32_t *parent,
                       const int4 *child, const float4 *hl, const float *R32, float theta2,
                       const int64_t *near_start, const int32_t *near_cnt, const int32_t *near_idx_in, int64_t *ufar,
                       int64_t *unear, int32_t *far_idx, int32_t *near_idx, int64_t far_cap, int64_t near_cap,
-                      int64_t *ctr) {
+                      uint8_t *dec, int64_t *ctr) {
     const unsigned full = 0xffffffffu;
     if (ctr[PC_OVF]) return;
     const int64_t n_units = *Uptr;
@@ -533,10 +535,18 @@ __global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const
                 cc[1] = c4.y;
                 cc[2] = c4.z;
                 cc[3] = c4.w;
-                for (int k = 0; k < 4; k++) {
-                    if (cc[k] < 0) continue;
-                    if (mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
-                    else nm |= 1u << k;
+                uint8_t *dq = dec + u * MAC_CHUNK + (q - qa);
+                if (pass) {
+                    const unsigned d = *dq;
+                    fm = d & 15u;
+                    nm = d >> 4;
+                } else {
+                    for (int k = 0; k < 4; k++) {
+                        if (cc[k] < 0) continue;
+                        if (mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
+                        else nm |= 1u << k;
+                    }
+                    *dq = (uint8_t)(fm | (nm << 4));
                 }
             }
             int myf = __popc(fm), myn = __popc(nm);
@@ -952,6 +962,8 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(cmax + 1) * 2));
         GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int32_t) * (size_t)(ucap + 1) * 2));
         GX_TRY(gx_ensure(ctx, ctx->scratch_e, sizeof(int64_t) * (size_t)(ucap + 1) * 4));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_d, (size_t)(ucap + 1) * MAC_CHUNK));
+        uint8_t *dec = dptr<uint8_t>(ctx->scratch_d);
         int64_t *nch = dptr<int64_t>(ctx->scratch_a), *uoff = nch + (cmax + 1);
         int32_t *unode = dptr<int32_t>(ctx->scratch_b), *uchunk = unode + (ucap + 1);
         int64_t *ufar = dptr<int64_t>(ctx->scratch_e), *unear = ufar + (ucap + 1), *ufo = unear + (ucap + 1),
@@ -982,13 +994,13 @@ int gx_plan_accurate(gx_ctx *ctx) {
             k_mac<<<gmac, 128, 0, ctx->stream>>>(Ud, 0, unode, uchunk, dptr<int32_t>(ctx->parent),
                                                  dptr<int4>(ctx->child), hl, R32, theta2, nstart, ncnt,
                                                  dptr<int32_t>(ctx->near_idx), ufar, unear, nullptr, nullptr, far_cap,
-                                                 near_cap, ctr);
+                                                 near_cap, dec, ctr);
             GX_TRY(gx_exclusive_scan_i64_devn(ctx, ufar, ufo, Ud, 1, ucap + 1));
             GX_TRY(gx_exclusive_scan_i64_devn(ctx, unear, uno, Ud, 1, ucap + 1));
             k_mac<<<gmac, 128, 0, ctx->stream>>>(Ud, 1, unode, uchunk, dptr<int32_t>(ctx->parent),
                                                  dptr<int4>(ctx->child), hl, R32, theta2, nstart, ncnt,
                                                  dptr<int32_t>(ctx->near_idx), ufo, uno, dptr<int32_t>(ctx->far_idx),
-                                                 dptr<int32_t>(ctx->near_idx), far_cap, near_cap, ctr);
+                                                 dptr<int32_t>(ctx->near_idx), far_cap, near_cap, dec, ctr);
             k_mac_node_lists<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, ufo, uno, ctr, fstart, fcnt,
                                                                         nstart, ncnt);
             k_mac_advance<<<1, 1, 0, ctx->stream>>>(Ud, ufo, uno, ctr);
