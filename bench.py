@@ -15,8 +15,10 @@ adjoint/forward time of reverse-mode rollouts.
   e2e        the same through the C ABI call gx_compute_forces with pinned host
              buffers: each step copies x, y, m host->device and ax, ay back
   roofline   the dominant kernel (P2P, FP32 pipe): algorithmic FLOPs (14 per
-             body-body interaction) per launch / its event-timed duration, against
-             the FP32 FMA peak measured on this GPU in the same run
+             body-body interaction) per launch / its event-timed duration in the
+             timed evaluations (where it shares the SMs with the far-field chain),
+             against the FP32 FMA peak measured on this GPU in the same run; the
+             *_alone keys time it again started after that chain
   cpu_baseline  the oracle (C restatement of galax-core's CPU FMM, REF semantics,
              OpenMP where the reference uses Rayon) on the host cores
   kdk_steps  leapfrog steps/s, static tree and tree rebuilt every step
@@ -571,6 +573,8 @@ def run_ours(args, rank, world, local, pg):
         e2e_t.append(time.perf_counter() - t0)
     _barrier(pg)
     e2e_ms = _max_over_ranks(pg, float(np.mean(e2e_t)) * 1e3)
+    # the P2P kernel once more, started after the far-field chain so that it runs alone
+    _, k_alone = ctx.bench_forces(max(3, args.steps // 2), True, 2)
     peak32 = ctx.probe_fp32_tflops()
 
     # whole steps (kick, drift, forces, kick) with the static tree and with the tree
@@ -629,6 +633,9 @@ def run_ours(args, rank, world, local, pg):
                      "kernel": "k_p2p32_rows (P2P, packed FP32; timed on its own stream while it shares the SMs "
                                "with M2L)",
                      "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)",
+                     "kernel_ms": kms, "kernel_ms_alone": float(np.mean(k_alone)),
+                     "achieved_alone": flops / (float(np.mean(k_alone)) * 1e-3) / 1e12,
+                     "frac_alone": flops / (float(np.mean(k_alone)) * 1e-3) / 1e12 / peak32 if peak32 else None,
                      "evaluation_tflops": eval_tflops, "evaluation_frac": eval_tflops / peak32 if peak32 else None},
         "gpu_launches": int(sum(r["launches"] * (r["steps"] + 1) for r in res.values())),
         "clocks": clocks,

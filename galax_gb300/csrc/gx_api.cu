@@ -705,12 +705,18 @@ int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each
     GX_TRY(ensure_plan(ctx));
     size_t flush_bytes = (size_t)256 << 20;  // twice the 129 MB L2
     if (flush_l2) GX_TRY(gx_ensure(ctx, ctx->flush, flush_bytes));
+    ctx->near_after_far = which == 2;
     for (int r = 0; r < reps; r++) {
         if (flush_l2) GX_CUDA(ctx, cudaMemsetAsync(ctx->flush.p, r & 0xff, flush_bytes, ctx->stream));
-        GX_TRY(forces_and_check(ctx, true));
+        const int rc = forces_and_check(ctx, true);
+        if (rc != GX_OK) {
+            ctx->near_after_far = false;
+            return rc;
+        }
         if (ms_each) ms_each[r] = ctx->last_ms[0];
         if (kernel_ms_each) kernel_ms_each[r] = which == 1 ? ctx->last_ms[4] : ctx->last_p2p_ms;
     }
+    ctx->near_after_far = false;
     return GX_OK;
 }
 

@@ -1218,6 +1218,7 @@ int run_forces(gx_ctx *ctx, bool timed) {
         // that L2P sums in order after the join.
         const size_t pbytes = (mixed ? sizeof(float2) : sizeof(double2)) * 32 * (size_t)tchunks * (size_t)(I.n + 1);
         GX_TRY(gx_ensure(ctx, ctx->part, pbytes));
+        auto near_field = [&]() -> int {
         GX_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
         GX_CUDA(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
         if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[14], ctx->stream2));
@@ -1238,6 +1239,11 @@ int run_forces(gx_ctx *ctx, bool timed) {
         }
         if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[15], ctx->stream2));
         GX_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->stream2));
+        return GX_OK;
+        };
+        // the near field starts beside the far-field chain; for a measurement of the
+        // near field alone (gx_bench_forces) it starts after the chain
+        if (!ctx->near_after_far) GX_TRY(near_field());
         // M2M, bottom-up by level
         for (int lv = 1; lv < ctx->n_levels; lv++) {
             int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
@@ -1291,6 +1297,7 @@ int run_forces(gx_ctx *ctx, bool timed) {
             Lleaf = Lf;
         }
         tm.mark();  // 5
+        if (ctx->near_after_far) GX_TRY(near_field());
         // join the near field, then L2P + ordered sum of the P2P partials
         GX_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
         if (mixed) {

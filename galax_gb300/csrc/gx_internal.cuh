@@ -146,6 +146,7 @@ struct gx_ctx {
     // sizes of the last tree and plan: the first capacities of the next build and plan
     // (their arrays may be fresh ones swapped in from a gx_tree_plan)
     int64_t hint_nodes = 0, hint_far = 0, hint_near = 0;
+    bool near_after_far = false;  // measurement only: the near field after the far-field chain
     DevBuf tree_state;     // tree build: device round state and level starts
     int64_t mac_ucap = 0;  // ACCURATE plan: capacity of the per-level unit arrays
     DevBuf part;                   // per-item partial accelerations

@@ -210,8 +210,10 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
 int gx_last_timings(gx_ctx *ctx, double out[7]);
 /* Runs `reps` force evaluations on the resident bodies and returns the CUDA-event
  * time of each on the context stream (ms) and the time of one kernel of it
- * (`which`: 0 = the P2P kernel, timed on its own stream; 1 = the M2L pass).  With flush_l2 != 0 a 256 MB buffer (twice
- * the L2) is written before each evaluation, outside its timed interval. */
+ * (`which`: 0 = the P2P kernel, timed on its own stream beside the far-field chain;
+ * 1 = the M2L pass; 2 = the P2P kernel started after the far-field chain, so that it
+ * runs alone).  With flush_l2 != 0 a 256 MB buffer (twice the L2) is written before
+ * each evaluation, outside its timed interval. */
 int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each, int32_t which,
                     double *kernel_ms_each);
 /* Number of kernels the last force evaluation launched. */

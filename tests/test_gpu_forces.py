@@ -186,3 +186,24 @@ def test_mixed_high_order_dense_cluster_stays_finite(G, p):
     assert np.all(np.isfinite(out["mixed"][0])) and np.all(np.isfinite(out["mixed"][1]))
     d = rel_vec_err(out["mixed"][0], out["mixed"][1], out["fp64"][0], out["fp64"][1])
     assert np.median(d) < 1e-5, np.median(d)
+
+
+def test_near_field_alone_gives_the_same_forces(G):
+    """gx_bench_forces(which=2) starts the near field after the far-field chain instead of
+    beside it: a measurement mode that must not change a single bit of the result."""
+    from galax_gb300 import presets
+    n = 50_000
+    b = presets.plummer(n, seed=31)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=4, eps64=0.05))
+    ctx.build_tree(b, 32, presets.BOUNDS["plummer"])
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    ctx.upload_bodies(b)
+    ctx.forces_resident()
+    r0 = G.Bodies.new(n)
+    ctx.download_bodies(r0)
+    ms, kms = ctx.bench_forces(2, False, 2)
+    r1 = G.Bodies.new(n)
+    ctx.download_bodies(r1)
+    ctx.close()
+    assert np.all(kms > 0) and np.all(ms >= kms)
+    assert np.array_equal(r0.ax, r1.ax) and np.array_equal(r0.ay, r1.ay)
