@@ -313,23 +313,34 @@ __global__ void k_scrub(int64_t n, T *v) {
 // One derivative order N of the fused M2L: the recurrence for the N+1 terms of order N
 // (from the unscaled orders N-1 and N-2) and every contraction term they complete.
 // A compile-time order keeps every index constant, so the arrays stay in registers.
+// k! l! as a compile-time constant once the loops are unrolled
+__host__ __device__ constexpr double ff_const(int k, int l) {
+    double r = 1.0;
+    for (int i = 2; i <= k; i++) r *= i;
+    for (int i = 2; i <= l; i++) r *= i;
+    return r;
+}
+
 template <int P, int N, class T>
 __device__ __forceinline__ void m2l_order(T dx, T dy, T ir2, T *a, const T *in, T *out) {
     if constexpr (N <= 2 * P) {
         const T in_ = tab_inv<T>(N) * ir2;
+        // c1 (dx a_{k-1,l} + dy a_{k,l-1}) + c2 (a_{k-2,l} + a_{k,l-2}) with c1 dx, c1 dy
+        // formed once per order: one multiply fewer per term
         const T c1 = -(T)(2 * N - 1) * in_, c2 = -(T)(N - 1) * in_;
+        const T c1x = c1 * dx, c1y = c1 * dy;
 #pragma unroll
         for (int k = 0; k <= N; k++) {
             const int l = N - k;
-            T s1, s2 = T(0);
-            if (k >= 1 && l >= 1) s1 = dx * a[gx_mi(k - 1, l)] + dy * a[gx_mi(k, l - 1)];
-            else if (k >= 1) s1 = dx * a[gx_mi(k - 1, l)];
-            else s1 = dy * a[gx_mi(k, l - 1)];
-            if (k >= 2) s2 += a[gx_mi(k - 2, l)];
-            if (l >= 2) s2 += a[gx_mi(k, l - 2)];
-            const T v = N >= 2 ? c1 * s1 + c2 * s2 : c1 * s1;
+            T v;
+            if (k >= 1 && l >= 1) v = c1x * a[gx_mi(k - 1, l)] + c1y * a[gx_mi(k, l - 1)];
+            else if (k >= 1) v = c1x * a[gx_mi(k - 1, l)];
+            else v = c1y * a[gx_mi(k, l - 1)];
+            if (k >= 2 && l >= 2) v += c2 * (a[gx_mi(k - 2, l)] + a[gx_mi(k, l - 2)]);
+            else if (k >= 2) v += c2 * a[gx_mi(k - 2, l)];
+            else if (l >= 2) v += c2 * a[gx_mi(k, l - 2)];
             a[gx_mi(k, l)] = v;
-            const T Av = N >= 2 ? v * tab_ff<T>(k, l) : v;
+            const T Av = (k <= 1 && l <= 1) ? v : v * (T)ff_const(k, l);
             // all splits (k, l) = X + Y with |X| <= p, |Y| <= p
 #pragma unroll
             for (int yi = (k > P ? k - P : 0); yi <= (k < P ? k : P); yi++)
