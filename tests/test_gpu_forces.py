@@ -207,3 +207,34 @@ def test_near_field_alone_gives_the_same_forces(G):
     ctx.close()
     assert np.all(kms > 0) and np.all(ms >= kms)
     assert np.array_equal(r0.ax, r1.ax) and np.array_equal(r0.ay, r1.ay)
+
+
+@pytest.mark.parametrize("mode,prec", [(0, 0), (2, 1)])
+def test_compute_forces_into_pinned_arrays(G, mode, prec):
+    """Page-locked and pageable host arrays give the same bits through
+    gx_compute_forces, on a tree built here and again after a device rebuild."""
+    from galax_gb300 import presets
+    n = 30_001
+    b = presets.plummer(n, seed=41)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=4, eps64=0.05))
+    ctx.build_tree(b, 32, presets.BOUNDS["plummer"])
+    ctx.set_mode(mode, prec, 0.5)
+    ctx.upload_bodies(b)
+    hx, hy, hm, pax, pay = (G.HostArray(n) for _ in range(5))
+    for rnd in range(2):
+        if rnd == 1:
+            b.x += 0.01 * np.sin(b.y)
+            ctx.upload_bodies(b)
+            perm = ctx.rebuild_resident(32, presets.BOUNDS["plummer"], want_perm=True)
+            for k in ("x", "y", "mass", "vx", "vy"):
+                setattr(b, k, getattr(b, k)[perm])
+        ax, ay = np.zeros(n), np.zeros(n)
+        ctx.compute_forces(b.x, b.y, b.mass, ax, ay)
+        hx.array[:] = b.x
+        hy.array[:] = b.y
+        hm.array[:] = b.mass
+        pax.array[:] = np.nan
+        pay.array[:] = np.nan
+        ctx.compute_forces(hx.array, hy.array, hm.array, pax.array, pay.array)
+        assert np.array_equal(ax, pax.array) and np.array_equal(ay, pay.array)
+    ctx.close()
