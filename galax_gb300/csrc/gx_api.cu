@@ -79,6 +79,7 @@ void gx_tree_plan_swap(gx_ctx *ctx, gx_tree_plan &t) {
     std::swap(ctx->items_acc.n, t.items_n);
     std::swap(ctx->m2l_units.n, t.units_n);
     std::swap(ctx->n_levels, t.n_levels);
+    std::swap(ctx->chain_levels, t.chain_levels);
     std::swap(ctx->have_tree, t.have_tree);
     std::swap(ctx->aux_valid, t.aux_valid);
     std::swap(ctx->plan_acc_valid, t.plan_acc_valid);

@@ -292,6 +292,46 @@ __global__ void __launch_bounds__(128) k_m2m(int64_t s, int64_t e, const int4 *_
     for (int k = 0; k < NCr; k++) M[node * NS + k] = out[k];
 }
 
+// Levels 1 .. L of single-child chains over the leaves (Morton rounds that grouped
+// nothing): the level-L ancestor of leaf x is node x + L nl and holds the same bodies,
+// so its moments are the leaf's shifted once to its COM (translations compose exactly);
+// the chain nodes in between have no far interactions in the ACCURATE lists and their
+// moments are never read.
+template <int P, class T>
+__global__ void __launch_bounds__(128) k_m2m_chain(int64_t nl, int64_t up, const double *__restrict__ comx,
+                                                   const double *__restrict__ comy, T *__restrict__ M) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nl) return;
+    const int64_t node = c + up;
+    T dx = (T)(comx[c] - comx[node]), dy = (T)(comy[c] - comy[node]);
+    T px[P + 1], py[P + 1];
+    px[0] = T(1);
+    py[0] = T(1);
+#pragma unroll
+    for (int k = 1; k <= PP; k++) {
+        px[k] = px[k - 1] * dx * tab_inv<T>(k);
+        py[k] = py[k - 1] * dy * tab_inv<T>(k);
+    }
+    T mc[NC], out[NC];
+    load_row<NC>(M + c * NS, mc);
+#pragma unroll
+    for (int k = 0; k < NCr; k++) out[k] = T(0);
+#pragma unroll
+    for (int oi = 0; oi <= PP; oi++)
+#pragma unroll
+        for (int oj = 0; oj <= PP - oi; oj++)
+#pragma unroll
+            for (int i = 0; i <= oi; i++)
+#pragma unroll
+                for (int j = 0; j <= oj; j++) out[gx_mi(oi, oj)] += mc[gx_mi(i, j)] * px[oi - i] * py[oj - j];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) M[node * NS + k] = out[k];
+}
+
 template <class T>
 __global__ void k_scrub(int64_t n, T *v) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1255,8 +1295,16 @@ int run_forces(gx_ctx *ctx, bool timed) {
         // the near field starts beside the far-field chain; for a measurement of the
         // near field alone (gx_bench_forces) it starts after the chain
         if (!ctx->near_after_far) GX_TRY(near_field());
-        // M2M, bottom-up by level
-        for (int lv = 1; lv < ctx->n_levels; lv++) {
+        // M2M, bottom-up by level; in ACCURATE mode the single-child chain levels over the
+        // leaves are one direct shift (their nodes have no far lists)
+        int lv_m2m = 1;
+        if (mode == GX_MODE_ACCURATE && ctx->chain_levels >= 2) {
+            const int64_t up = ctx->level_start[ctx->chain_levels];
+            k_m2m_chain<P, T><<<gx_blocks(nl, 128), 128, 0, st>>>(nl, up, comx, comy, M);
+            ctx->launches++;
+            lv_m2m = ctx->chain_levels + 1;
+        }
+        for (int lv = lv_m2m; lv < ctx->n_levels; lv++) {
             int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
             k_m2m<P, T><<<gx_blocks(e - s, 128), 128, 0, st>>>(s, e, child, comx, comy, M);
             ctx->launches++;

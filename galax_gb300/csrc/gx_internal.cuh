@@ -33,6 +33,7 @@ struct gx_tree_plan {
     int64_t n_nodes = 0, n_leaves = 0, max_leaf = 0, n_far_pairs = 0, n_near_pairs = 0, n_p2p_inter = 0;
     int64_t items_n = 0, units_n = 0;
     int32_t n_levels = 0;
+    int chain_levels = 0;
     bool have_tree = false, aux_valid = false, plan_acc_valid = false, plan_ref_valid = false,
          ref_lists_valid = false, items_valid = false;
     int plan_p = -1;
@@ -146,6 +147,10 @@ struct gx_ctx {
     // sizes of the last tree and plan: the first capacities of the next build and plan
     // (their arrays may be fresh ones swapped in from a gx_tree_plan)
     int64_t hint_nodes = 0, hint_far = 0, hint_near = 0;
+    // ACCURATE plan: levels 1 .. chain_levels are single-child chains over the leaves
+    // (level l holds node x + l nl above leaf x); with chain_levels >= 2 the plan and M2M
+    // skip levels 1 .. chain_levels - 1 (no far lists there), else 0
+    int chain_levels = 0;
     bool near_after_far = false;  // measurement only: the near field after the far-field chain
     DevBuf tree_state;     // tree build: device round state and level starts
     int64_t mac_ucap = 0;  // ACCURATE plan: capacity of the per-level unit arrays

@@ -512,6 +512,9 @@ __global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const
     for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n_units; u += nwarps) {
         int32_t x = unode[u];
         int32_t P = parent[x];
+        // x is its parent's only child: against the only child of a near entry of P the
+        // pair holds the parents' bodies and stays near without a test
+        const bool only_child = child[P].y < 0;
         int64_t qa = near_start[P] + (int64_t)uchunk[u] * MAC_CHUNK;
         int64_t qe = min(near_start[P] + (int64_t)near_cnt[P], qa + MAC_CHUNK);
         int64_t nf = 0, nn = 0;
@@ -541,9 +544,10 @@ __global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const
                     fm = d & 15u;
                     nm = d >> 4;
                 } else {
+                    const bool inherit = only_child && cc[1] < 0;
                     for (int k = 0; k < 4; k++) {
                         if (cc[k] < 0) continue;
-                        if (mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
+                        if (!inherit && mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
                         else nm |= 1u << k;
                     }
                     *dq = (uint8_t)(fm | (nm << 4));
@@ -574,6 +578,37 @@ __global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const
             unear[u] = nn;
         }
     }
+}
+
+// Leaves below single-child chain levels 1 .. L: by the only-child rule every level
+// under L keeps all of its parent's near entries (each mapped to its only child) and has
+// no far entries, so a leaf's near list is its level-L ancestor's (node x + up) shifted
+// down by up.  The level-L lists are the last block written; the leaf lists go after it.
+// One warp per leaf.
+__global__ void k_chain_leaf_lists(int64_t nl, int64_t up, int64_t *nstart, int32_t *ncnt, int32_t *near_idx,
+                                   int64_t near_cap, int64_t *ctr) {
+    if (ctr[PC_OVF]) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (x >= nl) return;
+    const int64_t a = x + up;
+    const int64_t block = ctr[PC_NEAR] - ctr[PC_NEAR_LAST];  // first entry of level L's lists
+    const int64_t src = nstart[a], cnt = ncnt[a];
+    const int64_t dst = ctr[PC_NEAR] + (src - block);
+    if (dst + cnt > near_cap) {
+        if (lane == 0) atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF), (unsigned long long)OVF_NEAR);
+        return;
+    }
+    for (int64_t q = lane; q < cnt; q += 32) near_idx[dst + q] = (int32_t)(near_idx[src + q] - up);
+    if (lane == 0) {
+        nstart[x] = dst;
+        ncnt[x] = (int32_t)cnt;
+    }
+}
+
+__global__ void k_chain_leaf_close(int64_t *ctr) {
+    if (ctr[PC_OVF]) return;
+    ctr[PC_NEAR] += ctr[PC_NEAR_LAST];  // the leaf lists are as long as level L's
 }
 
 // per node of the level: start (running total + first unit's offset) and count
@@ -944,6 +979,13 @@ int gx_plan_accurate(gx_ctx *ctx) {
     int64_t cmax = 1;
     for (int lv = 0; lv < ctx->n_levels; lv++)
         cmax = std::max<int64_t>(cmax, ctx->level_start[lv + 1] - ctx->level_start[lv]);
+    // levels 1 .. L of single-child chains over the leaves: a level with as many nodes as
+    // the one below groups nothing (each node is the one child of the node above it)
+    const int64_t nl0 = ctx->level_start[1];
+    int L = 0;
+    while (L + 1 < ctx->n_levels && ctx->level_start[L + 2] - ctx->level_start[L + 1] == nl0) L++;
+    ctx->chain_levels = L >= 2 ? L : 0;
+    const int lv_low = ctx->chain_levels;  // the lowest level the loop below processes
     // capacities: unit arrays and the far / near index arrays, kept from the last plan
     if (ctx->mac_ucap < 1024) ctx->mac_ucap = std::max<int64_t>(1024, nn);
     int64_t far_cap = std::max<int64_t>({(int64_t)(ctx->far_idx.bytes / sizeof(int32_t)), int64_t(1) << 20, 64 * nn,
@@ -982,7 +1024,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
                                      ctx->stream));
-        for (int lv = ctx->n_levels - 2; lv >= 0; lv--) {
+        for (int lv = ctx->n_levels - 2; lv >= lv_low; lv--) {
             const int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
             // units: chunks of each node's candidate list
             k_mac_nchunks<<<gx_blocks(c + 1, 256), 256, 0, ctx->stream>>>(s, e, dptr<int32_t>(ctx->parent), ncnt, nch,
@@ -1005,6 +1047,14 @@ int gx_plan_accurate(gx_ctx *ctx) {
                                                                         nstart, ncnt);
             k_mac_advance<<<1, 1, 0, ctx->stream>>>(Ud, ufo, uno, ctr);
             ctx->launches += 7;
+            GX_CUDA(ctx, cudaGetLastError());
+        }
+        if (lv_low >= 2) {
+            const int64_t up = ctx->level_start[lv_low];
+            k_chain_leaf_lists<<<(unsigned)((nl0 * 32 + 127) / 128), 128, 0, ctx->stream>>>(
+                nl0, up, nstart, ncnt, dptr<int32_t>(ctx->near_idx), near_cap, ctr);
+            k_chain_leaf_close<<<1, 1, 0, ctx->stream>>>(ctr);
+            ctx->launches += 2;
             GX_CUDA(ctx, cudaGetLastError());
         }
         GX_CUDA(ctx, cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));

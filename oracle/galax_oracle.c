@@ -1419,15 +1419,22 @@ void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_c
         hl[i].yl = (float)(t->comy[i] - (double)yh);
         R32[i] = (float)R[i];
     }
+    /* A node that is its parent's only child, against a candidate that is the only child
+     * of its parent, holds the same bodies as the parent pair (y, P), which was near:
+     * the pair stays near without a test (its COMs and radii differ from the parents'
+     * only by rounding).  Morton rounds leave whole levels of such single-child chains
+     * over the leaves; the device plan skips them with this rule. */
     for (int64_t id = nn - 1; id >= 0; id--) {
         int32_t P = t->parent[id];
         if (P < 0) continue;
+        const int only_child = t->child[4 * P + 1] < 0;
         for (int64_t q = 0; q < nv[P].n; q++) {
             int32_t y = nv[P].v[q];
+            const int y_single = t->child[4 * y + 1] < 0;
             for (int k = 0; k < 4; k++) {
                 int32_t c = t->child[4 * y + k];
                 if (c < 0) continue;
-                if (mac_far(hl, R32, id, c, theta2)) iv_push(&fv[id], c);
+                if (!(only_child && y_single) && mac_far(hl, R32, id, c, theta2)) iv_push(&fv[id], c);
                 else iv_push(&nv[id], c);
             }
         }
