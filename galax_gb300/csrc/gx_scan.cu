@@ -185,7 +185,7 @@ __global__ void k_rs_hist(const uint64_t *keys, int64_t n, int shift, unsigned m
     for (int d = threadIdx.x; d < RS_BINS; d += blockDim.x) hist[(int64_t)d * nb + blockIdx.x] = h[d];
 }
 
-// flag = 1 if every key has the same digit (the pass can be skipped)
+// flag = 1 if every key has the same digit (the pass copies instead of scattering)
 __global__ void k_rs_uniform(const unsigned *offs, int64_t nb, int64_t n, unsigned *flag) {
     int d = threadIdx.x;
     if (d >= RS_BINS) return;
@@ -197,7 +197,15 @@ __global__ void k_rs_uniform(const unsigned *offs, int64_t nb, int64_t n, unsign
 __global__ void __launch_bounds__(RS_WARPS * 32) k_rs_scatter(const uint64_t *kin, const uint32_t *vin,
                                                              uint64_t *kout, uint32_t *vout, int64_t n,
                                                              int shift, unsigned mask, const unsigned *offs,
-                                                             int64_t nb) {
+                                                             int64_t nb, const unsigned *uniform) {
+    if (*uniform) {  // every key has the same digit: the stable order is the present one
+        for (int64_t i = (int64_t)blockIdx.x * RS_TILE + threadIdx.x; i < n && i < (int64_t)(blockIdx.x + 1) * RS_TILE;
+             i += blockDim.x) {
+            kout[i] = kin[i];
+            vout[i] = vin[i];
+        }
+        return;
+    }
     __shared__ unsigned cnt[RS_WARPS][RS_BINS];
     for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += blockDim.x) (&cnt[0][0])[i] = 0;
     __syncthreads();
@@ -290,12 +298,10 @@ int gx_radix_sort_u64(gx_ctx *ctx, uint64_t *keys, uint32_t *vals, int64_t n, in
         GX_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(unsigned), ctx->stream));
         k_rs_uniform<<<1, RS_BINS, 0, ctx->stream>>>(hist, nb, n, flag);
         ctx->launches++;
-        unsigned hflag = 0;
-        GX_CUDA(ctx, cudaMemcpyAsync(&hflag, flag, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
-        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         (void)total;
-        if (hflag) continue;  // every key has the same digit: order is unchanged
-        k_rs_scatter<<<(unsigned)nb, RS_WARPS * 32, 0, ctx->stream>>>(ki, vi, ko, vo, n, shift, mask, hist, nb);
+        // the uniform-digit case is decided on the device (a copy instead of the scatter),
+        // so the passes run without a host round trip
+        k_rs_scatter<<<(unsigned)nb, RS_WARPS * 32, 0, ctx->stream>>>(ki, vi, ko, vo, n, shift, mask, hist, nb, flag);
         ctx->launches++;
         GX_CUDA(ctx, cudaGetLastError());
         uint64_t *tk = ki; ki = ko; ko = tk;
