@@ -147,6 +147,7 @@ struct gx_ctx {
     // sizes of the last tree and plan: the first capacities of the next build and plan
     // (their arrays may be fresh ones swapped in from a gx_tree_plan)
     int64_t hint_nodes = 0, hint_far = 0, hint_near = 0;
+    int hint_big_rounds = 0;  // tree build: rounds of the last build run by the multi-block kernels
     // ACCURATE plan: levels 1 .. chain_levels are single-child chains over the leaves
     // (level l holds node x + l nl above leaf x); with chain_levels >= 2 the plan and M2M
     // skip levels 1 .. chain_levels - 1 (no far lists there), else 0

@@ -101,7 +101,9 @@ enum { TS_S = 0, TS_E = 1, TS_C = 2, TS_SHIFT = 3, TS_NSEG = 4, TS_NG = 5, TS_FL
 enum { TS_DONE = 1, TS_OVERFLOW = 2, TS_STUCK = 4 };
 constexpr int TS_MAX_ROUNDS = 400;  // level starts kept: TS_MAX_ROUNDS + 2
 
-__device__ __forceinline__ bool round_off(const int64_t *st) { return st[TS_FLAGS] != 0; }
+constexpr int TS_SMALL = 2048;  // levels of at most this many nodes: k_rounds_small
+// the multi-block round kernels do nothing once the build is over or the level is small
+__device__ __forceinline__ bool round_off(const int64_t *st) { return st[TS_FLAGS] != 0 || st[TS_C] <= TS_SMALL; }
 
 __global__ void k_round_heads(const int64_t *st, const uint64_t *__restrict__ keys, const int32_t *__restrict__ bs,
                               int64_t *head) {
@@ -173,14 +175,11 @@ __global__ void k_round_close(int64_t *st, int64_t *level_start) {
     if (ng <= 1) st[TS_FLAGS] |= TS_DONE;
 }
 
-__global__ void k_parent_fields(const int64_t *st, double *cx, double *cy, double *hw, double *mass, double *comx,
-                                double *comy, int32_t *bs, int32_t *be, const int4 *child, int32_t *parent,
-                                uint8_t *is_leaf) {
-    if (round_off(st)) return;
-    const int64_t e = st[TS_E], ng = st[TS_NG];
-    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= ng) return;
-    int64_t q = e + g;
+// One parent of a round (lib.rs:298-335): mass, COM from the children's com x mass,
+// centre of the union of the children's boxes, hw = 2 x the largest child hw, body range.
+__device__ __forceinline__ void parent_fields_one(int64_t q, double *cx, double *cy, double *hw, double *mass,
+                                                  double *comx, double *comy, int32_t *bs, int32_t *be,
+                                                  const int4 *child, int32_t *parent, uint8_t *is_leaf) {
     int4 c4 = child[q];
     int cc[4] = {c4.x, c4.y, c4.z, c4.w};
     double ms = 0.0, sx = 0.0, sy = 0.0, mh = 0.0;
@@ -211,6 +210,146 @@ __global__ void k_parent_fields(const int64_t *st, double *cx, double *cy, doubl
     be[q] = be[last];
     parent[q] = -1;
     is_leaf[q] = 0;
+}
+
+__global__ void k_parent_fields(const int64_t *st, double *cx, double *cy, double *hw, double *mass, double *comx,
+                                double *comy, int32_t *bs, int32_t *be, const int4 *child, int32_t *parent,
+                                uint8_t *is_leaf) {
+    if (round_off(st)) return;
+    const int64_t e = st[TS_E], ng = st[TS_NG];
+    int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    parent_fields_one(e + g, cx, cy, hw, mass, comx, comy, bs, be, child, parent, is_leaf);
+}
+
+// The rounds of levels of at most TS_SMALL nodes, all in one block: each phase of a
+// round is a loop over the level with a block barrier after it, so the tail of the
+// tree (a dozen rounds at 1M) costs one launch instead of a dozen per round.
+constexpr int RS_SMALL_THREADS = 1024;
+
+__device__ int64_t block_excl_scan_small(int v, int *warp_tot, int *total) {
+    // exclusive scan of one int per thread over RS_SMALL_THREADS threads
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int s = warp_tot[lane];
+        int si = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, si, o);
+            if (lane >= o) si += t;
+        }
+        warp_tot[lane] = si - s;
+        if (lane == 31) *total = si;
+    }
+    __syncthreads();
+    int r = warp_tot[w] + inc - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(RS_SMALL_THREADS) k_rounds_small(int64_t *st, int64_t *level_start, int64_t cap_nodes,
+                                                                  const uint64_t *__restrict__ keys, double *cx,
+                                                                  double *cy, double *hw, double *mass, double *comx,
+                                                                  double *comy, int32_t *bs, int32_t *be, int32_t *child,
+                                                                  int32_t *parent, uint8_t *is_leaf) {
+    constexpr int PER = TS_SMALL / RS_SMALL_THREADS;  // items per thread
+    __shared__ int head[TS_SMALL], segex[TS_SMALL], segstart[TS_SMALL], goff[TS_SMALL];
+    __shared__ int warp_tot[32], tot;
+    __shared__ int64_t sh_s, sh_e, sh_c, sh_flags, sh_rounds;
+    __shared__ unsigned sh_shift;
+    const int t = threadIdx.x;
+    for (;;) {
+        if (t == 0) {
+            sh_s = st[TS_S];
+            sh_e = st[TS_E];
+            sh_c = st[TS_C];
+            sh_flags = st[TS_FLAGS];
+            sh_rounds = st[TS_ROUNDS];
+            sh_shift = (unsigned)st[TS_SHIFT] & 63u;
+        }
+        __syncthreads();
+        const int64_t s = sh_s, e = sh_e, c = sh_c;
+        if (sh_flags != 0 || c > TS_SMALL) return;
+        // heads and their exclusive scan (segment of each node)
+        int loc[PER], lsum = 0;
+        for (int k = 0; k < PER; k++) {
+            const int i = t * PER + k;
+            int h = 0;
+            if (i < c) {
+                const uint64_t g = keys[bs[s + i]] >> sh_shift;
+                h = (i == 0) ? 1 : (g != (keys[bs[s + i - 1]] >> sh_shift));
+                head[i] = h;
+            }
+            loc[k] = h;
+            lsum += h;
+        }
+        int run = (int)block_excl_scan_small(lsum, warp_tot, &tot);
+        const int nseg = tot;
+        for (int k = 0; k < PER; k++) {
+            const int i = t * PER + k;
+            if (i < c) segex[i] = run;
+            run += loc[k];
+        }
+        __syncthreads();
+        for (int k = 0; k < PER; k++) {
+            const int i = t * PER + k;
+            if (i < c && head[i]) segstart[segex[i]] = i;
+        }
+        __syncthreads();
+        // groups of at most 4 per segment and their exclusive scan
+        lsum = 0;
+        for (int k = 0; k < PER; k++) {
+            const int j = t * PER + k;
+            int g = 0;
+            if (j < nseg) g = (int)((((j + 1 < nseg) ? segstart[j + 1] : (int)c) - segstart[j] + 3) / 4);
+            loc[k] = g;
+            lsum += g;
+        }
+        run = (int)block_excl_scan_small(lsum, warp_tot, &tot);
+        const int ng = tot;
+        for (int k = 0; k < PER; k++) {
+            const int j = t * PER + k;
+            if (j < nseg) goff[j] = run;
+            run += loc[k];
+        }
+        if (e + ng > cap_nodes || sh_rounds >= TS_MAX_ROUNDS) {
+            if (t == 0) st[TS_FLAGS] |= (e + ng > cap_nodes) ? TS_OVERFLOW : TS_STUCK;
+            return;  // uniform: every thread saw the same counts
+        }
+        for (int g = t; g < ng; g += RS_SMALL_THREADS)
+            reinterpret_cast<int4 *>(child)[e + g] = make_int4(-1, -1, -1, -1);
+        __syncthreads();
+        for (int k = 0; k < PER; k++) {
+            const int i = t * PER + k;
+            if (i >= c) continue;
+            const int seg = segex[i] + head[i] - 1;
+            const int pos = i - segstart[seg];
+            const int64_t g = goff[seg] + pos / 4;
+            parent[s + i] = (int32_t)(e + g);
+            child[(e + g) * 4 + (pos & 3)] = (int32_t)(s + i);
+        }
+        __syncthreads();
+        for (int g = t; g < ng; g += RS_SMALL_THREADS)
+            parent_fields_one(e + g, cx, cy, hw, mass, comx, comy, bs, be, reinterpret_cast<const int4 *>(child),
+                              parent, is_leaf);
+        __syncthreads();
+        if (t == 0) {
+            const int64_t r = ++st[TS_ROUNDS];
+            level_start[r + 1] = e + ng;
+            st[TS_S] = e;
+            st[TS_E] = e + ng;
+            st[TS_C] = ng;
+            st[TS_SHIFT] += 2;
+            if (ng <= 1) st[TS_FLAGS] |= TS_DONE;
+        }
+        __syncthreads();
+    }
 }
 
 // ---- build_constrained helpers (lib.rs:541-694) ----
@@ -272,7 +411,9 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
         GX_CUDA(ctx, cudaMemcpyAsync(st, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(lstart, ls01, sizeof(ls01), cudaMemcpyHostToDevice, ctx->stream));
         // rounds in batches: the last build's round count first, then 8 at a time
-        int batch = std::max(8, ctx->n_levels > 0 ? ctx->n_levels : 8);
+        // multi-block rounds in batches (the last build's count first), each batch followed
+        // by the single-block kernel for the small levels
+        int batch = std::max(4, ctx->hint_big_rounds + 1);
         int issued = 0;
         for (;;) {
             for (int r = 0; r < batch; r++) {
@@ -291,6 +432,12 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
                 k_round_close<<<1, 1, 0, ctx->stream>>>(st, lstart);
                 ctx->launches += 7;
             }
+            k_rounds_small<<<1, RS_SMALL_THREADS, 0, ctx->stream>>>(
+                st, lstart, cap, dptr<uint64_t>(ctx->keys), dptr<double>(ctx->cx), dptr<double>(ctx->cy),
+                dptr<double>(ctx->hw), dptr<double>(ctx->mass), dptr<double>(ctx->comx), dptr<double>(ctx->comy),
+                dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), dptr<int32_t>(ctx->child), dptr<int32_t>(ctx->parent),
+                dptr<uint8_t>(ctx->is_leaf));
+            ctx->launches++;
             GX_CUDA(ctx, cudaGetLastError());
             issued += batch;
             GX_CUDA(ctx, cudaMemcpyAsync(hs, st, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
@@ -307,6 +454,9 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
     GX_CUDA(ctx, cudaMemcpyAsync(ls.data(), lstart, sizeof(int64_t) * ls.size(), cudaMemcpyDeviceToHost, ctx->stream));
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->level_start.assign(ls.begin(), ls.end());
+    ctx->hint_big_rounds = 0;
+    for (size_t l = 0; l + 2 < ls.size(); l++)
+        if (ls[l + 1] - ls[l] > TS_SMALL) ctx->hint_big_rounds++;
     const int64_t nn = ls.back();
     ctx->n_nodes = nn;
     ctx->hint_nodes = nn;
