@@ -611,6 +611,161 @@ __global__ void k_chain_leaf_close(int64_t *ctr) {
     ctr[PC_NEAR] += ctr[PC_NEAR_LAST];  // the leaf lists are as long as level L's
 }
 
+// The top levels of the tree (at most PLAN_SMALL nodes each, down to the first larger
+// level) in one block: per level, each thread counts the far and near entries of its
+// nodes, a block scan places them, and a second pass writes them in the same order as
+// the multi-block pass (parent's near entry, child slot), with block barriers between
+// the steps instead of a dozen launches per level.
+constexpr int PLAN_SMALL = 256;
+constexpr int PLAN_SMALL_THREADS = 256;
+struct PlanLevels {
+    int64_t start[66];  // level_start of levels lo .. hi + 1 (relative index lv - lo)
+    int lo, hi;
+};
+
+__device__ int plan_block_scan(int v, int *warp_tot, int *total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int inc = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) warp_tot[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        int s = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+        int si = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, si, o);
+            if (lane >= o) si += t;
+        }
+        if (lane < (int)(blockDim.x >> 5)) warp_tot[lane] = si - s;
+        if (lane == 31) *total = si;
+    }
+    __syncthreads();
+    int r = warp_tot[w] + inc - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(PLAN_SMALL_THREADS) k_mac_small_levels(
+    PlanLevels L, const int32_t *__restrict__ parent, const int4 *__restrict__ child, const float4 *__restrict__ hl,
+    const float *__restrict__ R32, float theta2, int64_t *fstart, int32_t *fcnt, int64_t *nstart, int32_t *ncnt,
+    int32_t *far_idx, int32_t *near_idx, int64_t far_cap, int64_t near_cap, int64_t *ctr) {
+    constexpr int PER = PLAN_SMALL / PLAN_SMALL_THREADS;
+    constexpr int NW = PLAN_SMALL_THREADS / 32;
+    const unsigned full = 0xffffffffu;
+    __shared__ int cnt_f[PLAN_SMALL], cnt_n[PLAN_SMALL];
+    __shared__ int warp_tot[32], tot_f, tot_n;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    // one warp walks node x's candidates 32 entries at a time (as k_mac does); pass 0
+    // counts, pass 1 writes from (fb, nb) in list order
+    auto walk = [&](int64_t x, int pass, int64_t fb, int64_t nb, int &nf_out, int &nn_out) {
+        const int32_t P = parent[x];
+        const bool only_child = child[P].y < 0;
+        const int64_t qa = nstart[P], qe = qa + ncnt[P];
+        int nf = 0, nn = 0;
+        for (int64_t qb = qa; qb < qe; qb += 32) {
+            const int64_t q = qb + lane;
+            int cc[4] = {-1, -1, -1, -1};
+            unsigned fm = 0, nm = 0;
+            if (q < qe) {
+                const int4 c4 = child[near_idx[q]];
+                cc[0] = c4.x;
+                cc[1] = c4.y;
+                cc[2] = c4.z;
+                cc[3] = c4.w;
+                const bool inherit = only_child && cc[1] < 0;
+                for (int k = 0; k < 4; k++) {
+                    if (cc[k] < 0) continue;
+                    if (!inherit && mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
+                    else nm |= 1u << k;
+                }
+            }
+            const int myf = __popc(fm), myn = __popc(nm);
+            int pf = myf, pn = myn;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
+                if (lane >= o) {
+                    pf += tf;
+                    pn += tn;
+                }
+            }
+            if (pass) {
+                int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
+                for (int k = 0; k < 4; k++) {
+                    if ((fm >> k) & 1u) far_idx[a++] = cc[k];
+                    if ((nm >> k) & 1u) near_idx[b++] = cc[k];
+                }
+            }
+            nf += __shfl_sync(full, pf, 31);
+            nn += __shfl_sync(full, pn, 31);
+        }
+        nf_out = nf;
+        nn_out = nn;
+    };
+    for (int lv = L.hi; lv >= L.lo; lv--) {
+        if (ctr[PC_OVF]) return;  // uniform: written by thread 0 before a barrier
+        const int64_t s = L.start[lv - L.lo], e = L.start[lv - L.lo + 1], c = e - s;
+        for (int64_t i = w; i < c; i += NW) {
+            int nf, nn;
+            walk(s + i, 0, 0, 0, nf, nn);
+            if (lane == 0) {
+                cnt_f[i] = nf;
+                cnt_n[i] = nn;
+            }
+        }
+        __syncthreads();
+        // exclusive offsets of the nodes' entries (PER nodes per thread)
+        int lf = 0, ln = 0, vf[PER], vn[PER];
+        for (int k = 0; k < PER; k++) {
+            const int64_t i = (int64_t)t * PER + k;
+            vf[k] = i < c ? cnt_f[i] : 0;
+            vn[k] = i < c ? cnt_n[i] : 0;
+            lf += vf[k];
+            ln += vn[k];
+        }
+        int of = plan_block_scan(lf, warp_tot, &tot_f);
+        int on = plan_block_scan(ln, warp_tot, &tot_n);
+        for (int k = 0; k < PER; k++) {
+            const int64_t i = (int64_t)t * PER + k;
+            if (i < c) {
+                cnt_f[i] = of;  // now the node's offset within the level
+                cnt_n[i] = on;
+            }
+            of += vf[k];
+            on += vn[k];
+        }
+        __syncthreads();
+        const int64_t base_f = ctr[PC_FAR], base_n = ctr[PC_NEAR];
+        if (base_f + tot_f > far_cap || base_n + tot_n > near_cap) {
+            if (t == 0)
+                atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF),
+                         (unsigned long long)((base_f + tot_f > far_cap ? OVF_FAR : 0) |
+                                              (base_n + tot_n > near_cap ? OVF_NEAR : 0)));
+            return;
+        }
+        for (int64_t i = w; i < c; i += NW) {
+            const int64_t fb = base_f + cnt_f[i], nb = base_n + cnt_n[i];
+            int nf, nn;
+            walk(s + i, 1, fb, nb, nf, nn);
+            if (lane == 0) {
+                fstart[s + i] = fb;
+                fcnt[s + i] = nf;
+                nstart[s + i] = nb;
+                ncnt[s + i] = nn;
+            }
+        }
+        __syncthreads();
+        if (t == 0) {
+            ctr[PC_FAR] = base_f + tot_f;
+            ctr[PC_NEAR] = base_n + tot_n;
+            ctr[PC_NEAR_LAST] = tot_n;
+        }
+        __syncthreads();
+    }
+}
+
 // per node of the level: start (running total + first unit's offset) and count
 __global__ void k_mac_node_lists(int64_t s, int64_t e, const int64_t *uoff, const int64_t *ufo, const int64_t *uno,
                                  const int64_t *ctr, int64_t *fstart, int32_t *fcnt, int64_t *nstart, int32_t *ncnt) {
@@ -1024,7 +1179,22 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
                                      ctx->stream));
-        for (int lv = ctx->n_levels - 2; lv >= lv_low; lv--) {
+        // the top levels of at most PLAN_SMALL nodes in one block, then the rest
+        int lv_big = ctx->n_levels - 2;
+        while (lv_big >= lv_low && ctx->level_start[lv_big + 1] - ctx->level_start[lv_big] <= PLAN_SMALL) lv_big--;
+        if (lv_big < ctx->n_levels - 2) {
+            PlanLevels PL;
+            PL.lo = lv_big + 1;
+            PL.hi = ctx->n_levels - 2;
+            if (PL.hi - PL.lo + 2 > 66) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "accurate plan: too many levels");
+            for (int lv = PL.lo; lv <= PL.hi + 1; lv++) PL.start[lv - PL.lo] = ctx->level_start[lv];
+            k_mac_small_levels<<<1, PLAN_SMALL_THREADS, 0, ctx->stream>>>(
+                PL, dptr<int32_t>(ctx->parent), dptr<int4>(ctx->child), hl, R32, theta2, fstart, fcnt, nstart, ncnt,
+                dptr<int32_t>(ctx->far_idx), dptr<int32_t>(ctx->near_idx), far_cap, near_cap, ctr);
+            ctx->launches++;
+            GX_CUDA(ctx, cudaGetLastError());
+        }
+        for (int lv = lv_big; lv >= lv_low; lv--) {
             const int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1], c = e - s;
             // units: chunks of each node's candidate list
             k_mac_nchunks<<<gx_blocks(c + 1, 256), 256, 0, ctx->stream>>>(s, e, dptr<int32_t>(ctx->parent), ncnt, nch,
