@@ -997,6 +997,110 @@ __global__ void __launch_bounds__(128, 7) k_p2p32_items(int64_t n_items, const i
     }
 }
 
+// The one-row kernel with one target per lane and every source of the row, for leaves
+// of at most 16 bodies (n_max <= 16), where the second target of k_p2p32_rows would be
+// empty and a row holds only half a warp of sources: partial rows run their whole
+// quads packed and the rest scalar.
+__global__ void __launch_bounds__(128, 8) k_p2p32_rows1(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                    const int64_t *__restrict__ item_qb, const int32_t *__restrict__ item_nq,
+                                                    const float4 *__restrict__ pos, const double *__restrict__ comx,
+                                                    const double *__restrict__ comy, const int32_t *__restrict__ bs,
+                                                    const int32_t *__restrict__ be, const int32_t *__restrict__ src_idx,
+                                                    float eps2, float2 *__restrict__ part) {
+    __shared__ __align__(16) float sx[4][32], sy[4][32], sm[4][32];
+    __shared__ __align__(16) int4 meta[4][32];  // per source leaf: begin, end, shift x, shift y (FP32 bits)
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
+        const int32_t leaf = item_leaf[it];
+        const int nq = item_nq[it];
+        const int32_t t0 = bs[leaf], t1 = be[leaf];
+        bool own_lane = false;
+        __syncwarp();  // the previous item's reads of meta[w] are done
+        if (lane < nq) {
+            int32_t sl = src_idx[item_qb[it] + lane];
+            double tcx = comx[leaf], tcy = comy[leaf];
+            meta[w][lane] = make_int4(bs[sl], be[sl], __float_as_int((float)(comx[sl] - tcx)),
+                                      __float_as_int((float)(comy[sl] - tcy)));
+            own_lane = sl == leaf;
+        }
+        const unsigned ownm = __ballot_sync(0xffffffffu, own_lane);
+        const int kown = ownm ? __ffs(ownm) - 1 : -1;
+        __syncwarp();
+        const int32_t i = t0 + lane;
+        const float4 me = i < t1 ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint64_t XI = pk2(me.x, me.x), YI = pk2(me.y, me.y), E2 = pk2(eps2, eps2);
+        uint64_t AXa = 0, AYa = 0, AXb = 0, AYb = 0;  // bit pattern 0 = (0.f, 0.f)
+        float axs = 0.f, ays = 0.f;
+        auto fetch = [&](int4 m) -> float4 {
+            int j = m.x + lane;
+            float4 v = j < m.y ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            v.x += __int_as_float(m.z);
+            v.y += __int_as_float(m.w);
+            return v;
+        };
+        float4 cur = nq > 0 ? fetch(meta[w][0]) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int k = 0; k < nq; k++) {
+            const float4 nxt = k + 1 < nq ? fetch(meta[w][k + 1]) : make_float4(0.f, 0.f, 0.f, 0.f);
+            __syncwarp();
+            sx[w][lane] = cur.x;
+            sy[w][lane] = cur.y;
+            sm[w][lane] = cur.z;
+            __syncwarp();
+            const int2 se = *reinterpret_cast<const int2 *>(&meta[w][k]);  // this row's begin, end
+            const int ns = se.y - se.x;
+            auto quad = [&](int kk) {
+                float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
+                float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
+                float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
+                uint64_t dx0 = sub2(pk2(X.x, X.y), XI), dy0 = sub2(pk2(Y.x, Y.y), YI);
+                uint64_t dx1 = sub2(pk2(X.z, X.w), XI), dy1 = sub2(pk2(Y.z, Y.w), YI);
+                uint64_t r0 = fma2(dx0, dx0, fma2(dy0, dy0, E2));
+                uint64_t r1 = fma2(dx1, dx1, fma2(dy1, dy1, E2));
+                float ra, rb;
+                upk2(r0, ra, rb);
+                uint64_t i0 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                upk2(r1, ra, rb);
+                uint64_t i1 = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                uint64_t f0 = mul2(pk2(Mq.x, Mq.y), mul2(mul2(i0, i0), i0));
+                uint64_t f1 = mul2(pk2(Mq.z, Mq.w), mul2(mul2(i1, i1), i1));
+                AXa = fma2(f0, dx0, AXa);
+                AYa = fma2(f0, dy0, AYa);
+                AXb = fma2(f1, dx1, AXb);
+                AYb = fma2(f1, dy1, AYb);
+            };
+            int k0 = 0;  // sources below k0 are done
+            if (k != kown) {
+                if (ns == 32) {
+#pragma unroll
+                    for (int kk = 0; kk < 32; kk += 4) quad(kk);
+                    k0 = 32;
+                } else {
+                    for (k0 = 0; k0 + 4 <= ns; k0 += 4) quad(k0);
+                }
+            }
+            for (int kk = k0; kk < ns; kk++) {
+                float xi, yi, dum;
+                upk2(XI, xi, dum);
+                upk2(YI, yi, dum);
+                float dx = sx[w][kk] - xi, dy = sy[w][kk] - yi;
+                float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                float fk = sm[w][kk] * (ir * ir * ir);
+                fk = (k == kown && se.x + kk == i) ? 0.f : fk;
+                axs = fmaf(fk, dx, axs);
+                ays = fmaf(fk, dy, ays);
+            }
+            cur = nxt;
+        }
+        float a0, a1, a2, a3, b0, b1, b2, b3;
+        upk2(AXa, a0, a1);
+        upk2(AXb, a2, a3);
+        upk2(AYa, b0, b1);
+        upk2(AYb, b2, b3);
+        part[it * 32 + lane] = make_float2(((a0 + a1) + (a2 + a3)) + axs, ((b0 + b1) + (b2 + b3)) + ays);
+    }
+}
+
 // The same near field when every leaf holds at most 32 bodies (n_max <= 32): each
 // source leaf is one row, so the item's source-leaf table (first body, end, FP32
 // frame shift) is written to shared memory once per item and read back by broadcast
@@ -1274,7 +1378,13 @@ int run_forces(gx_ctx *ctx, bool timed) {
         GX_CUDA(ctx, cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
         if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[14], ctx->stream2));
         if (I.n > 0) {
-            if (mixed && tchunks == 1)
+            // two targets per lane pays when leaves fill most of a row; with leaves of at
+            // most 16 bodies (n_max <= 16) the second target would be empty
+            if (mixed && tchunks == 1 && ctx->max_leaf <= 16)
+                k_p2p32_rows1<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                            dptr<int32_t>(I.nq), pos, comx, comy, bs, be, src_idx,
+                                                            (float)eps2, dptr<float2>(ctx->part));
+            else if (mixed && tchunks == 1)
                 k_p2p32_rows<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
                                                            dptr<int32_t>(I.nq), pos, comx, comy, bs, be, src_idx,
                                                            (float)eps2, dptr<float2>(ctx->part));

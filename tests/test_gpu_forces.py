@@ -238,3 +238,26 @@ def test_compute_forces_into_pinned_arrays(G, mode, prec):
         ctx.compute_forces(hx.array, hy.array, hm.array, pax.array, pay.array)
         assert np.array_equal(ax, pax.array) and np.array_equal(ay, pay.array)
     ctx.close()
+
+
+@pytest.mark.parametrize("n_max", [8, 16, 64])
+def test_mixed_form_with_other_leaf_sizes(G, n_max):
+    """Leaves of at most 16 bodies take the one-target P2P kernel, larger leaves than a
+    warp the chunked one: the mixed form stays within FP32 rounding of the FP64 form."""
+    from galax_gb300 import presets
+    n = 40_000
+    b = presets.plummer(n, seed=51)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=4, eps64=0.05))
+    ctx.build_tree(b, n_max, presets.BOUNDS["plummer"])
+    ctx.upload_bodies(b)
+    out = {}
+    for prec in (G.PREC_FP64, G.PREC_MIXED):
+        ctx.set_mode(G.MODE_ACCURATE, prec, 0.5)
+        ctx.forces_resident()
+        r = G.Bodies.new(n)
+        ctx.download_bodies(r)
+        out[prec] = r
+    ctx.close()
+    d = rel_vec_err(out[G.PREC_MIXED].ax, out[G.PREC_MIXED].ay, out[G.PREC_FP64].ax, out[G.PREC_FP64].ay)
+    assert np.isfinite(d).all()
+    assert np.median(d) < 2e-6 and np.percentile(d, 99) < 1e-4
