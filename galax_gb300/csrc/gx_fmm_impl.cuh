@@ -743,27 +743,6 @@ __global__ void __launch_bounds__(128) k_l2l_ref_leaves(int64_t nl, const int32_
     for (int k = 0; k < NCr; k++) Lout[leaf * NS + k] = out[k];
 }
 
-// top-down: L[x] += shift(L[parent(x)]) for the nodes of one level
-template <int P, class T>
-__global__ void __launch_bounds__(128) k_l2l_level(int64_t s, int64_t e, const int32_t *__restrict__ parent,
-                                                   const double *__restrict__ comx, const double *__restrict__ comy,
-                                                   T *__restrict__ L) {
-    constexpr int NC = nc2(P);
-    constexpr int NS = row_stride<T>(NC);
-    const int PP = gx_rt_order(P);
-    const int NCr = (PP + 1) * (PP + 2) / 2;
-    int64_t x = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= e) return;
-    int32_t par = parent[x];
-    if (par < 0) return;
-    T out[NC];
-#pragma unroll
-    for (int k = 0; k < NCr; k++) out[k] = L[x * NS + k];
-    l2l_shift<P, T>(L + (int64_t)par * NS, (T)(comx[x] - comx[par]), (T)(comy[x] - comy[par]), out);
-#pragma unroll
-    for (int k = 0; k < NCr; k++) L[x * NS + k] = out[k];
-}
-
 // ---------------------------------------------------------------- L2P + P2P
 // One warp per target leaf, one lane per target body (chunks of 32 for larger
 // leaves).  The source-leaf list is read 32 entries at a time (one coalesced load)
