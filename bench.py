@@ -55,8 +55,8 @@ sys.path.insert(0, ROOT)
 METRIC = "FMM bodies/s (1M, p=4) mixed vs FP64 at equal force error; adjoint/fwd time"
 N_DEFAULT = 1_000_000
 # DRAM bytes (read 46.78 MB + written 20.44 MB) of one k_p2p32_rows launch at the
-# default workload, from the one-pass ncu capture summarised in
-# profiles/k_p2p32_rows_plummer200k.md (the kernel works out of L2)
+# default workload, from a one-pass ncu capture (dram__bytes_read.sum +
+# dram__bytes_write.sum) of this workload: the kernel works out of L2
 P2P_TRAFFIC_1M = 67.22e6
 P, N_MAX, THETA = 4, 32, 0.5
 
