@@ -27,6 +27,7 @@ MODE_REF, MODE_EXACT, MODE_ACCURATE = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 LIST_V, LIST_U = 0, 1
 BUILD_BALANCED = 1
+STATUS_SANITIZED = 1  # gx_last_status: invalid positions / masses were replaced
 LIST_CAP = 64
 
 STATUS_NAMES = {
@@ -95,6 +96,7 @@ def lib():
         "gx_last_timings": (C.c_int, [_VP, _D]),
         "gx_bench_forces": (C.c_int, [_VP, C.c_int32, C.c_int32, _D, C.c_int32, _D]),
         "gx_last_launch_count": (C.c_int, [_VP, _I64]),
+        "gx_last_status": (C.c_int, [_VP, C.POINTER(C.c_uint32)]),
         "gx_probe_fp32_tflops": (C.c_int, [_VP, _D]),
         "gx_n2_sampled_static": (C.c_int, [_VP, _VP, _VP, C.c_int64, C.c_double, _I64, C.c_int64, _D, _D, _VP]),
         "gx_force_vjp": (C.c_int, [_VP, _D, _D, _D, _D, _D]),
@@ -502,6 +504,13 @@ class GpuContext:
         c = C.c_int64()
         self._check(lib().gx_last_launch_count(self._h, C.byref(c)))
         return c.value
+
+    def last_status(self) -> int:
+        """Status bits of the last force evaluation (STATUS_SANITIZED: inputs were sanitised
+        as compute_fmm_force does, galax-core/src/lib.rs:1474-1482)."""
+        s = C.c_uint32()
+        self._check(lib().gx_last_status(self._h, C.byref(s)))
+        return s.value
 
     # -- reverse mode (ACCURATE)
     def _resident_n(self, *arrays) -> int:

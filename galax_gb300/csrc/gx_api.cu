@@ -618,6 +618,7 @@ static int forces_launch(gx_ctx *ctx, bool timed) {
 static int forces_finish(gx_ctx *ctx, bool timed) {
     unsigned st = 0;
     GX_TRY(sync_status(ctx, &st));
+    ctx->last_status = st;
     if (timed && ctx->n_nodes > 0) {
         float ms = 0;
         cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[6]);
@@ -690,6 +691,13 @@ int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, do
 int gx_last_timings(gx_ctx *ctx, double out[7]) {
     GX_TRY(check_ctx(ctx));
     for (int k = 0; k < 7; k++) out[k] = ctx->last_ms[k];
+    return GX_OK;
+}
+
+int gx_last_status(gx_ctx *ctx, uint32_t *status) {
+    GX_TRY(check_ctx(ctx));
+    if (!status) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null output");
+    *status = ctx->last_status & GX_STATUS_SANITIZED;
     return GX_OK;
 }
 

@@ -30,7 +30,7 @@ typedef enum gx_status {
     GX_ERR_KERNEL_LOAD = 2,   /* the sm_103a image does not load on this device */
     GX_ERR_ALLOC = 3,         /* device or pinned-host allocation failed */
     GX_ERR_INVALID_ARG = 4,   /* bad pointer, size, order p, mode ... */
-    GX_ERR_NONFINITE = 5,     /* non-finite values were met (reported, not fatal) */
+    GX_ERR_NONFINITE = 5,     /* non-finite values were met (not fatal; see gx_last_status) */
     GX_ERR_CAP_EXCEEDED = 6,  /* a size is beyond the configured maximum */
     GX_ERR_TIMEOUT = 7,       /* a bounded device wait gave up */
     GX_ERR_STATE = 8,         /* call out of order (e.g. forces before a tree) */
@@ -218,6 +218,12 @@ int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each
                     double *kernel_ms_each);
 /* Number of kernels the last force evaluation launched. */
 int gx_last_launch_count(gx_ctx *ctx, int64_t *count);
+/* Device status bits of the last force evaluation: GX_STATUS_SANITIZED when
+ * non-finite or out-of-range positions were zeroed and non-positive or non-finite
+ * masses set to 1 before it, as compute_fmm_force does (galax-core/src/lib.rs:1474-1482:
+ * the reference does it silently; the evaluation still returns GX_OK). */
+#define GX_STATUS_SANITIZED 1u
+int gx_last_status(gx_ctx *ctx, uint32_t *status);
 
 /* FP32 FMA throughput of this GPU in TFLOP/s (best of 5 timed launches of a
  * kernel of independent FMA chains): the ceiling used for the FP32 P2P pass. */

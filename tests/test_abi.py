@@ -57,6 +57,7 @@ def test_invalid_arguments_are_rejected_without_a_device(G):
     assert L.gx_force_vjp(None, None, None, None, None, None) == 4
     assert L.gx_rollout_forward(None, 1, 0.1, 1, 0) == 4
     assert L.gx_rollout_backward(None, *([None] * 10)) == 4
+    assert L.gx_last_status(None, None) == 4
 
 
 def test_no_device_reports_init_failure(G):

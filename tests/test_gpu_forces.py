@@ -147,6 +147,15 @@ def test_sanitised_inputs_match_oracle(G, oracle):
     ax, ay = _run_gpu(G, bad, t, v, u, 4, eps, G.MODE_REF)
     err = rel_vec_err(ax, ay, ref.ax, ref.ay)
     assert np.all(np.isfinite(ax)) and err.max() < TOL_FP64
+    # the sanitising is reported by gx_last_status, and a clean call clears it
+    ctx = G.GpuContext(G.GpuConfig(max_n=len(bad.x), max_nodes=1 << 20, p=4, eps64=eps))
+    ctx.upload_tree_data(t, v, u)
+    ax2, ay2 = np.zeros(len(bad.x)), np.zeros(len(bad.x))
+    ctx.compute_forces(bad.x.copy(), bad.y.copy(), bad.mass.copy(), ax2, ay2)
+    assert ctx.last_status() == G.STATUS_SANITIZED
+    ctx.compute_forces(ob.x.copy(), ob.y.copy(), ob.mass.copy(), ax2, ay2)
+    assert ctx.last_status() == 0
+    ctx.close()
 
 
 def test_p2p_only_at_p0_equals_p2p(G, oracle):
