@@ -458,7 +458,7 @@ constexpr int MAC_CHUNK = 128;
 // every later kernel of the attempt returns at once, and the host grows the arrays
 // and plans again.
 enum { PC_FAR = 0, PC_NEAR = 1, PC_NEAR_LAST = 2, PC_OVF = 3, PC_N = 4 };
-enum { OVF_UNITS = 1, OVF_FAR = 2, OVF_NEAR = 4 };
+enum { OVF_UNITS = 1, OVF_FAR = 2, OVF_NEAR = 4, OVF_CHAIN = 8 };
 
 __global__ void k_mac_nchunks(int64_t s, int64_t e, const int32_t *parent, const int32_t *near_cnt, int64_t *nch,
                               const int64_t *ctr) {
@@ -603,6 +603,21 @@ __global__ void k_chain_leaf_lists(int64_t nl, int64_t up, int64_t *nstart, int3
     if (lane == 0) {
         nstart[x] = dst;
         ncnt[x] = (int32_t)cnt;
+    }
+}
+
+// The chain shortcut needs node x + l nl (levels 1 .. L) to have the single child
+// x + (l - 1) nl, as Tree::build numbers them; a tree given from the host that does not
+// flags OVF_CHAIN and is planned without the shortcut.
+__global__ void k_chain_check(int64_t nl, int L, const int4 *child, int64_t *ctr) {
+    int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nl) return;
+    for (int l = 1; l <= L; l++) {
+        const int4 c = child[x + l * nl];
+        if (c.x != x + (l - 1) * nl || c.y >= 0) {
+            atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF), (unsigned long long)OVF_CHAIN);
+            return;
+        }
     }
 }
 
@@ -1140,7 +1155,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
     int L = 0;
     while (L + 1 < ctx->n_levels && ctx->level_start[L + 2] - ctx->level_start[L + 1] == nl0) L++;
     ctx->chain_levels = L >= 2 ? L : 0;
-    const int lv_low = ctx->chain_levels;  // the lowest level the loop below processes
+    int lv_low = ctx->chain_levels;  // the lowest level the loop below processes
     // capacities: unit arrays and the far / near index arrays, kept from the last plan
     if (ctx->mac_ucap < 1024) ctx->mac_ucap = std::max<int64_t>(1024, nn);
     int64_t far_cap = std::max<int64_t>({(int64_t)(ctx->far_idx.bytes / sizeof(int32_t)), int64_t(1) << 20, 64 * nn,
@@ -1179,6 +1194,10 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_CUDA(ctx, cudaMemcpyAsync(ncnt + root, &one, sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(dptr<int32_t>(ctx->near_idx), &root32, sizeof(int32_t), cudaMemcpyHostToDevice,
                                      ctx->stream));
+        if (lv_low >= 2) {
+            k_chain_check<<<gx_blocks(nl0, 256), 256, 0, ctx->stream>>>(nl0, lv_low, dptr<int4>(ctx->child), ctr);
+            ctx->launches++;
+        }
         // the top levels of at most PLAN_SMALL nodes in one block, then the rest
         int lv_big = ctx->n_levels - 2;
         while (lv_big >= lv_low && ctx->level_start[lv_big + 1] - ctx->level_start[lv_big] <= PLAN_SMALL) lv_big--;
@@ -1230,6 +1249,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_CUDA(ctx, cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (!hc[PC_OVF]) break;
+        if (hc[PC_OVF] & OVF_CHAIN) ctx->chain_levels = lv_low = 0;  // no shortcut for this tree
         if (hc[PC_OVF] & OVF_UNITS) ctx->mac_ucap *= 4;
         if (hc[PC_OVF] & OVF_FAR) far_cap *= 4;
         if (hc[PC_OVF] & OVF_NEAR) near_cap *= 4;
