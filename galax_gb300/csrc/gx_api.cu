@@ -189,7 +189,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->Lff32, &ctx->pos32, &ctx->part, &ctx->items_ref.leaf, &ctx->items_ref.qb, &ctx->items_ref.nq, &ctx->items_ref.off, &ctx->items_acc.leaf, &ctx->items_acc.qb, &ctx->items_acc.nq, &ctx->items_acc.off, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
                       &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush, &ctx->adj_lx, &ctx->adj_ly, &ctx->adj_lvx, &ctx->adj_lvy, &ctx->adj_lm, &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm, &ctx->adj_lax, &ctx->adj_lay, &ctx->adj_lf, &ctx->adj_dL, &ctx->adj_dM, &ctx->adj_dMleaf, &ctx->adj_lam32, &ctx->ckpt, &ctx->seg, &ctx->ids, &ctx->perm, &ctx->roll_perms, &ctx->radius32,
                       &ctx->m2l_units.node, &ctx->m2l_units.start, &ctx->m2l_units.len, &ctx->m2l_units.node_u,
-                      &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state};
+                      &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state, &ctx->m2l_cnt};
     for (DevBuf *b : bufs) free_buf(*b);
     for (gx_tree_plan &t : ctx->tp_cache) gx_tree_plan_free(t);
     for (auto &e : ctx->ev)

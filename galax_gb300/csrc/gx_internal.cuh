@@ -143,6 +143,7 @@ struct gx_ctx {
         int64_t n = 0;
     } m2l_units;
     DevBuf m2l_part;  // per-unit partial locals of nodes cut into several units
+    DevBuf m2l_cnt;   // plan scratch: units per node
     DevBuf plan_ctr;       // ACCURATE plan: device running totals and overflow flags
     // sizes of the last tree and plan: the first capacities of the next build and plan
     // (their arrays may be fresh ones swapped in from a gx_tree_plan)

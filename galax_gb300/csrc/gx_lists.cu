@@ -1262,7 +1262,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
     GX_TRY(gx_ensure(ctx, ctx->has_far_acc, (size_t)nn));
     k_flag_i32<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, fcnt, dptr<uint8_t>(ctx->has_far_acc));
     ctx->launches++;
-    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    GX_CUDA(ctx, cudaGetLastError());
     ctx->plan_acc_valid = true;
     ctx->plan_p = ctx->p;
     ctx->plan_eps = ctx->eps;
@@ -1408,48 +1408,49 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
         start = dptr<int64_t>(ctx->p2p_off);
         cnt = nullptr;
     }
+    // the P2P items and (ACCURATE) the M2L units: counts and scans of both, one wait for
+    // their two totals, then both fills
     GX_TRY(gx_ensure(ctx, I.off, sizeof(int64_t) * (size_t)(nl + 1)));
     GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nl + 1)));
     int64_t *nit = dptr<int64_t>(ctx->scratch_c);
     k_items_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, start, cnt, nit);
     GX_TRY(gx_exclusive_scan_i64(ctx, nit, dptr<int64_t>(I.off), nl + 1));
-    int64_t tot = 0;
-    GX_CUDA(ctx, cudaMemcpyAsync(&tot, dptr<int64_t>(I.off) + nl, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    int64_t tot[2] = {0, 0};
+    GX_CUDA(ctx, cudaMemcpyAsync(&tot[0], dptr<int64_t>(I.off) + nl, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    gx_ctx::M2LUnits &U = ctx->m2l_units;
+    const int64_t *fstart = accurate ? dptr<int64_t>(ctx->far_off) : nullptr;
+    const int32_t *fcnt = accurate ? reinterpret_cast<const int32_t *>(fstart + nn) : nullptr;
+    if (accurate) {
+        GX_TRY(gx_ensure(ctx, U.node_u, sizeof(int64_t) * (size_t)(nn + 1)));
+        GX_TRY(gx_ensure(ctx, ctx->m2l_cnt, sizeof(int64_t) * (size_t)(nn + 1)));
+        int64_t *nu = dptr<int64_t>(ctx->m2l_cnt);
+        k_m2l_units_count<<<gx_blocks(nn + 1, 256), 256, 0, ctx->stream>>>(nn, fcnt, nu);
+        GX_TRY(gx_exclusive_scan_i64(ctx, nu, dptr<int64_t>(U.node_u), nn + 1));
+        GX_CUDA(ctx, cudaMemcpyAsync(&tot[1], dptr<int64_t>(U.node_u) + nn, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        ctx->launches++;
+    }
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    GX_TRY(gx_ensure(ctx, I.leaf, sizeof(int32_t) * (size_t)(tot + 1)));
-    GX_TRY(gx_ensure(ctx, I.qb, sizeof(int64_t) * (size_t)(tot + 1)));
-    GX_TRY(gx_ensure(ctx, I.nq, sizeof(int32_t) * (size_t)(tot + 1)));
+    GX_TRY(gx_ensure(ctx, I.leaf, sizeof(int32_t) * (size_t)(tot[0] + 1)));
+    GX_TRY(gx_ensure(ctx, I.qb, sizeof(int64_t) * (size_t)(tot[0] + 1)));
+    GX_TRY(gx_ensure(ctx, I.nq, sizeof(int32_t) * (size_t)(tot[0] + 1)));
     k_items_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, start, cnt, dptr<int64_t>(I.off), dptr<int32_t>(I.leaf),
                                                               dptr<int64_t>(I.qb), dptr<int32_t>(I.nq));
     ctx->launches += 2;
-    GX_CUDA(ctx, cudaGetLastError());
-    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    I.n = tot;
+    I.n = tot[0];
     if (accurate) {
-        // M2L units of the far lists
-        gx_ctx::M2LUnits &U = ctx->m2l_units;
-        const int64_t *fstart = dptr<int64_t>(ctx->far_off);
-        const int32_t *fcnt = reinterpret_cast<const int32_t *>(fstart + nn);
-        GX_TRY(gx_ensure(ctx, U.node_u, sizeof(int64_t) * (size_t)(nn + 1)));
-        GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nn + 1)));
-        int64_t *nu = dptr<int64_t>(ctx->scratch_c);
-        k_m2l_units_count<<<gx_blocks(nn + 1, 256), 256, 0, ctx->stream>>>(nn, fcnt, nu);
-        GX_TRY(gx_exclusive_scan_i64(ctx, nu, dptr<int64_t>(U.node_u), nn + 1));
-        int64_t nun = 0;
-        GX_CUDA(ctx, cudaMemcpyAsync(&nun, dptr<int64_t>(U.node_u) + nn, sizeof(int64_t), cudaMemcpyDeviceToHost,
-                                     ctx->stream));
-        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        const int64_t nun = tot[1];
         GX_TRY(gx_ensure(ctx, U.node, sizeof(int32_t) * (size_t)(nun + 1)));
         GX_TRY(gx_ensure(ctx, U.start, sizeof(int64_t) * (size_t)(nun + 1)));
         GX_TRY(gx_ensure(ctx, U.len, sizeof(int32_t) * (size_t)(nun + 1)));
         k_m2l_units_fill<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, fstart, fcnt, dptr<int64_t>(U.node_u),
                                                                       dptr<int32_t>(U.node), dptr<int64_t>(U.start),
                                                                       dptr<int32_t>(U.len));
-        ctx->launches += 2;
-        GX_CUDA(ctx, cudaGetLastError());
-        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        ctx->launches++;
         U.n = nun;
     }
+    GX_CUDA(ctx, cudaGetLastError());
     I.valid = true;
     return GX_OK;
 }
@@ -1467,7 +1468,6 @@ int gx_plan_tree_aux(gx_ctx *ctx) {
                                                              dptr<float4>(ctx->comhl));
         ctx->launches += 2;
         GX_CUDA(ctx, cudaGetLastError());
-        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     }
     ctx->aux_valid = true;
     return GX_OK;
