@@ -616,24 +616,32 @@ __global__ void __launch_bounds__(128) k_adj_p2p_reduce(int64_t nl, const int32_
     for (int tc = 0; tc < tchunks && t0 + tc * 32 < t1; tc++) {
         int32_t i = t0 + tc * 32 + lane;
         if (i >= t1) continue;
-        // four independent accumulators keep the loads of long item ranges in flight
+        // four independent accumulators keep the loads of long slot ranges in flight;
+        // the slots of a long item range are mostly group sums (k_fold_items)
         S ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, am[4] = {0, 0, 0, 0};
-        int64_t it = item_off[leaf];
-        const int64_t ie = item_off[leaf + 1];
-        for (; it + 4 <= ie; it += 4) {
+        const ItemSlots sl(item_off[leaf], item_off[leaf + 1]);
+        int64_t j = 0;
+        for (; j + 4 <= sl.n; j += 4) {
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                V v = part[((it + u) * tchunks + tc) * 32 + lane];
+                V v = part[(sl[j + u] * tchunks + tc) * 32 + lane];
                 ax[u] += v.x;
                 ay[u] += v.y;
                 am[u] += v.z;
             }
         }
-        for (; it < ie; it++) {
-            V v = part[(it * tchunks + tc) * 32 + lane];
-            ax[0] += v.x;
-            ay[0] += v.y;
-            am[0] += v.z;
+        if (j < sl.n) {  // the last round predicated: its loads in flight together
+            V v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (j + u < sl.n) v[u] = part[(sl[j + u] * tchunks + tc) * 32 + lane];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (j + u < sl.n) {
+                    ax[u] += v[u].x;
+                    ay[u] += v[u].y;
+                    am[u] += v[u].z;
+                }
         }
         const S sx = (ax[0] + ax[1]) + (ax[2] + ax[3]), sy = (ay[0] + ay[1]) + (ay[2] + ay[3]),
                 smm = (am[0] + am[1]) + (am[2] + am[3]);
@@ -699,6 +707,15 @@ int run_force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf_
                                                           dptr<int32_t>(I.nq), X, Y, Mb, lx, ly, bs, be,
                                                           dptr<int32_t>(ctx->near_idx), eps2, tchunks,
                                                           dptr<double4>(ctx->part));
+        if (I.n > GX_FOLD_MIN) {
+            const unsigned gf = (unsigned)(((I.n + GX_FOLD - 1) / GX_FOLD * 32 + 127) / 128);
+            if (F32)
+                k_fold_items<float4><<<gf, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.off),
+                                                                   tchunks, dptr<float4>(ctx->part));
+            else
+                k_fold_items<double4><<<gf, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.off),
+                                                                    tchunks, dptr<double4>(ctx->part));
+        }
     }
     GX_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->stream2));
     // A2: L2L^T upward, level by level (leaves are level 0)
@@ -731,7 +748,7 @@ int run_force_vjp(gx_ctx *ctx, const double *X, const double *Y, const void *lf_
     else
         k_adj_p2p_reduce<double4, double><<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks,
                                                               dptr<double4>(ctx->part), gx, gy, gm);
-    ctx->launches += 6 + (ctx->n_levels - 1);
+    ctx->launches += 6 + (ctx->n_levels - 1) + (I.n > GX_FOLD_MIN ? 1 : 0);
     GX_CUDA(ctx, cudaGetLastError());
     return GX_OK;
 }

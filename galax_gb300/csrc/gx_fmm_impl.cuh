@@ -1210,26 +1210,105 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
     }
 }
 
-// Sum of a leaf's P2P partials over its items [i0, i1) for one lane: eight independent
-// accumulators so the loads are in flight together (a wide halo leaf can have ~1000
-// items, and a single dependent chain made that one warp the whole kernel's length).
+// Folding of long item ranges.  A wide halo leaf can have ~1000 P2P items (977 at 1M
+// Plummer, p = 4, n_max = 32, against a median of 5), and one warp summing them in
+// order was the whole length of the reduce (its loads are dependent rounds of a few
+// hundred cycles each).  So before the reduce, k_fold_items sums, in place, every full
+// group of GX_FOLD items that starts at a multiple of GX_FOLD inside a leaf with more
+// than GX_FOLD_MIN items; the reduce of such a leaf then reads its head items, the group
+// sums and its tail items, in item order.  The groups depend only on the plan, so the
+// sums are deterministic.
+constexpr int GX_FOLD = 16, GX_FOLD_MIN = 32;
+
+// The partial slots of a leaf's items [i0, i1): slot j < nh is item i0 + j, then ng group
+// sums at h, h + GX_FOLD, ..., then the items [f, i1).  Unfolded leaves: nh = i1 - i0.
+struct ItemSlots {
+    int64_t i0, h, f, nh, ng, n;
+    __device__ __forceinline__ ItemSlots(int64_t i0_, int64_t i1) : i0(i0_) {
+        if (i1 - i0 > GX_FOLD_MIN) {
+            h = (i0 + GX_FOLD - 1) / GX_FOLD * GX_FOLD;  // < i1: the leaf has more than 2 groups of items
+            f = i1 / GX_FOLD * GX_FOLD;                  // >= h for the same reason
+        } else {
+            h = f = i1;
+        }
+        nh = h - i0;
+        ng = (f - h) / GX_FOLD;
+        n = nh + ng + (i1 - f);
+    }
+    __device__ __forceinline__ int64_t operator[](int64_t j) const {
+        return j < nh ? i0 + j : (j < nh + ng ? h + (j - nh) * GX_FOLD : f + (j - nh - ng));
+    }
+};
+
+__device__ __forceinline__ void vadd(float2 &a, const float2 &b) { a.x += b.x; a.y += b.y; }
+__device__ __forceinline__ void vadd(double2 &a, const double2 &b) { a.x += b.x; a.y += b.y; }
+__device__ __forceinline__ void vadd(float4 &a, const float4 &b) { a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w; }
+__device__ __forceinline__ void vadd(double4 &a, const double4 &b) { a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w; }
+
+// One warp per group of GX_FOLD items starting at a multiple of GX_FOLD; only groups
+// wholly inside a leaf with more than GX_FOLD_MIN items are summed (into the group's
+// first slot, for every target chunk): u and u + 8 pairwise, then a fixed tree.
+template <class V>
+__global__ void __launch_bounds__(128) k_fold_items(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                    const int64_t *__restrict__ item_off, int tchunks,
+                                                    V *__restrict__ part) {
+    static_assert(GX_FOLD == 16, "the sum below is written for groups of 16");
+    const int lane = threadIdx.x & 31;
+    const int64_t g0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * GX_FOLD;
+    if (g0 >= n_items) return;
+    const int32_t leaf = item_leaf[g0];
+    const int64_t i0 = item_off[leaf], i1 = item_off[leaf + 1];
+    if (i1 - i0 <= GX_FOLD_MIN || g0 + GX_FOLD > i1) return;
+    for (int tc = 0; tc < tchunks; tc++) {
+        V a[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            a[u] = part[((g0 + u) * tchunks + tc) * 32 + lane];
+            vadd(a[u], part[((g0 + 8 + u) * tchunks + tc) * 32 + lane]);
+        }
+        vadd(a[0], a[1]);
+        vadd(a[2], a[3]);
+        vadd(a[4], a[5]);
+        vadd(a[6], a[7]);
+        vadd(a[0], a[2]);
+        vadd(a[4], a[6]);
+        vadd(a[0], a[4]);
+        part[(g0 * tchunks + tc) * 32 + lane] = a[0];
+    }
+}
+
+// Sum of a leaf's P2P partials over its item slots for one lane: eight independent
+// accumulators (slot j into accumulator j mod 8), and the last (or only: the median
+// leaf has 5 items) round of fewer than eight slots predicated rather than looped, so
+// that the loads of a round are in flight together.
 template <class V, class S>
 __device__ __forceinline__ void sum_items(const V *__restrict__ part, int64_t i0, int64_t i1, int tchunks, int tc,
                                           int lane, S &sx, S &sy) {
     S ax[8] = {0, 0, 0, 0, 0, 0, 0, 0}, ay[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int64_t it = i0;
-    for (; it + 8 <= i1; it += 8) {
+    const ItemSlots sl(i0, i1);
+    const V *base = part + tc * 32 + lane;
+    const int64_t row = (int64_t)tchunks * 32;
+    int64_t j = 0;
+    for (; j + 8 <= sl.n; j += 8) {
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-            V v = part[((it + u) * tchunks + tc) * 32 + lane];
+            V v = base[sl[j + u] * row];
             ax[u] += v.x;
             ay[u] += v.y;
         }
     }
-    for (; it < i1; it++) {
-        V v = part[(it * tchunks + tc) * 32 + lane];
-        ax[0] += v.x;
-        ay[0] += v.y;
+    if (j < sl.n) {
+        const int r = (int)(sl.n - j);
+        V v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (u < r) v[u] = base[sl[j + u] * row];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (u < r) {
+                ax[u] += v[u].x;
+                ay[u] += v[u].y;
+            }
     }
     sx = ((ax[0] + ax[1]) + (ax[2] + ax[3])) + ((ax[4] + ax[5]) + (ax[6] + ax[7]));
     sy = ((ay[0] + ay[1]) + (ay[2] + ay[3])) + ((ay[4] + ay[5]) + (ay[6] + ay[7]));
@@ -1261,14 +1340,34 @@ __global__ void __launch_bounds__(128) k_l2p_reduce64(int64_t nl, const double *
     }
 }
 
+// Mixed form, in two kernels: the L2P of every body on the main stream while the near
+// field still runs (fl = the local expansion's (fx, fy) in FP32), and after the join the
+// ordered sum of the P2P partials, a = sum - f in FP64.  The sum kernel has nothing but
+// its loads to wait for, so more of its warps are resident and its loads (the leaf's
+// item range, then the partials and fl together) are two dependent rounds.
 template <int P>
-__global__ void __launch_bounds__(128) k_l2p_reduce32(int64_t nl, const float4 *__restrict__ pos,
-                                                      const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
-                                                      const float *__restrict__ Lf, const int64_t *__restrict__ item_off,
-                                                      int tchunks, const float2 *__restrict__ part,
-                                                      double *__restrict__ ax, double *__restrict__ ay) {
+__global__ void __launch_bounds__(128) k_l2p32(int64_t nl, const float4 *__restrict__ pos,
+                                               const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                               const float *__restrict__ Lf, float2 *__restrict__ fl) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<float>(NC);
+    int lane = threadIdx.x & 31;
+    int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (leaf >= nl) return;
+    int32_t t0 = bs[leaf], t1 = be[leaf];
+    for (int32_t i = t0 + lane; i < t1; i += 32) {
+        float4 me = pos[i];
+        float fx, fy;
+        l2p_eval<P, float>(Lf + leaf * NS, me.x, me.y, fx, fy);
+        fl[i] = make_float2(fx, fy);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_reduce32(int64_t nl, const int32_t *__restrict__ bs,
+                                                  const int32_t *__restrict__ be, const int64_t *__restrict__ item_off,
+                                                  int tchunks, const float2 *__restrict__ part,
+                                                  const float2 *__restrict__ fl, double *__restrict__ ax,
+                                                  double *__restrict__ ay) {
     int lane = threadIdx.x & 31;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nl) return;
@@ -1277,13 +1376,11 @@ __global__ void __launch_bounds__(128) k_l2p_reduce32(int64_t nl, const float4 *
     for (int tc = 0; tc < tchunks && t0 + tc * 32 < t1; tc++) {
         int32_t i = t0 + tc * 32 + lane;
         if (i >= t1) continue;
-        float4 me = pos[i];
-        float fx, fy;
-        l2p_eval<P, float>(Lf + leaf * NS, me.x, me.y, fx, fy);
+        const float2 f = fl[i];
         float sx, sy;
         sum_items<float2, float>(part, i0, i1, tchunks, tc, lane, sx, sy);
-        ax[i] = (double)sx - (double)fx;
-        ay[i] = (double)sy - (double)fy;
+        ax[i] = (double)sx - (double)f.x;
+        ay[i] = (double)sy - (double)f.y;
     }
 }
 
@@ -1378,6 +1475,16 @@ int run_forces(gx_ctx *ctx, bool timed) {
             ctx->launches++;
         }
         if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[15], ctx->stream2));
+        if (I.n > GX_FOLD_MIN) {
+            const unsigned gf = (unsigned)(((I.n + GX_FOLD - 1) / GX_FOLD * 32 + 127) / 128);
+            if (mixed)
+                k_fold_items<float2><<<gf, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.off),
+                                                                   tchunks, dptr<float2>(ctx->part));
+            else
+                k_fold_items<double2><<<gf, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.off),
+                                                                    tchunks, dptr<double2>(ctx->part));
+            ctx->launches++;
+        }
         GX_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->stream2));
         return GX_OK;
         };
@@ -1444,14 +1551,20 @@ int run_forces(gx_ctx *ctx, bool timed) {
             ctx->launches++;
             Lleaf = Lf;
         }
+        float2 *fl = nullptr;
+        if (mixed) {  // L2P beside the near field
+            GX_TRY(gx_ensure(ctx, ctx->fl32, sizeof(float2) * (size_t)n));
+            fl = dptr<float2>(ctx->fl32);
+            k_l2p32<P><<<gw, 128, 0, st>>>(nl, pos, bs, be, reinterpret_cast<const float *>(Lleaf), fl);
+            ctx->launches++;
+        }
         tm.mark();  // 5
         if (ctx->near_after_far) GX_TRY(near_field());
-        // join the near field, then L2P + ordered sum of the P2P partials
+        // join the near field, then the ordered sum of the P2P partials (+ L2P in FP64)
         GX_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
         if (mixed) {
-            k_l2p_reduce32<P><<<gw, 128, 0, st>>>(nl, pos, bs, be, reinterpret_cast<const float *>(Lleaf),
-                                                  dptr<int64_t>(I.off), tchunks, dptr<float2>(ctx->part),
-                                                  dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+            k_reduce32<<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks, dptr<float2>(ctx->part), fl,
+                                           dptr<double>(ctx->ax), dptr<double>(ctx->ay));
         } else {
             k_l2p_reduce64<P><<<gw, 128, 0, st>>>(nl, X, Y, comx, comy, bs, be, reinterpret_cast<const double *>(Lleaf),
                                                   dptr<int64_t>(I.off), tchunks, dptr<double2>(ctx->part),

@@ -165,6 +165,7 @@ struct gx_ctx {
     DevBuf M, L, Lf;
     DevBuf Mf32, Lf32, Lff32;
     DevBuf pos32;  // mixed form: bodies as FP32 (x - com_leaf, y - com_leaf, m, 0)
+    DevBuf fl32;   // mixed form: the L2P (fx, fy) of every body, summed with the P2P partials after the join
 
     // adjoint: cotangents, VJP outputs, transposed expansions, checkpoints
     DevBuf adj_lx, adj_ly, adj_lvx, adj_lvy, adj_lm, adj_gx, adj_gy, adj_gm, adj_lax, adj_lay, adj_lf;
