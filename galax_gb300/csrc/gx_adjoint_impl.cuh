@@ -620,11 +620,11 @@ __global__ void __launch_bounds__(128) k_adj_p2p_reduce(int64_t nl, const int32_
         // the slots of a long item range are mostly group sums (k_fold_items)
         S ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0}, am[4] = {0, 0, 0, 0};
         const ItemSlots sl(item_off[leaf], item_off[leaf + 1]);
-        int64_t j = 0;
+        int j = 0;
         for (; j + 4 <= sl.n; j += 4) {
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                V v = part[(sl[j + u] * tchunks + tc) * 32 + lane];
+                V v = part[((int64_t)sl[j + u] * tchunks + tc) * 32 + lane];
                 ax[u] += v.x;
                 ay[u] += v.y;
                 am[u] += v.z;
@@ -634,7 +634,7 @@ __global__ void __launch_bounds__(128) k_adj_p2p_reduce(int64_t nl, const int32_
             V v[4];
 #pragma unroll
             for (int u = 0; u < 4; u++)
-                if (j + u < sl.n) v[u] = part[(sl[j + u] * tchunks + tc) * 32 + lane];
+                if (j + u < sl.n) v[u] = part[((int64_t)sl[j + u] * tchunks + tc) * 32 + lane];
 #pragma unroll
             for (int u = 0; u < 4; u++)
                 if (j + u < sl.n) {

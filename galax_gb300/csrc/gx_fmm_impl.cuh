@@ -1222,9 +1222,11 @@ constexpr int GX_FOLD = 16, GX_FOLD_MIN = 32;
 
 // The partial slots of a leaf's items [i0, i1): slot j < nh is item i0 + j, then ng group
 // sums at h, h + GX_FOLD, ..., then the items [f, i1).  Unfolded leaves: nh = i1 - i0.
+// Item indices fit in 31 bits (the partials of 2^31 items would take 512 GB).
 struct ItemSlots {
-    int64_t i0, h, f, nh, ng, n;
-    __device__ __forceinline__ ItemSlots(int64_t i0_, int64_t i1) : i0(i0_) {
+    int i0, h, f, nh, ng, n;
+    __device__ __forceinline__ ItemSlots(int64_t i0_, int64_t i1_) : i0((int)i0_) {
+        const int i1 = (int)i1_;
         if (i1 - i0 > GX_FOLD_MIN) {
             h = (i0 + GX_FOLD - 1) / GX_FOLD * GX_FOLD;  // < i1: the leaf has more than 2 groups of items
             f = i1 / GX_FOLD * GX_FOLD;                  // >= h for the same reason
@@ -1235,7 +1237,7 @@ struct ItemSlots {
         ng = (f - h) / GX_FOLD;
         n = nh + ng + (i1 - f);
     }
-    __device__ __forceinline__ int64_t operator[](int64_t j) const {
+    __device__ __forceinline__ int operator[](int j) const {
         return j < nh ? i0 + j : (j < nh + ng ? h + (j - nh) * GX_FOLD : f + (j - nh - ng));
     }
 };
@@ -1288,7 +1290,7 @@ __device__ __forceinline__ void sum_items(const V *__restrict__ part, int64_t i0
     const ItemSlots sl(i0, i1);
     const V *base = part + tc * 32 + lane;
     const int64_t row = (int64_t)tchunks * 32;
-    int64_t j = 0;
+    int j = 0;
     for (; j + 8 <= sl.n; j += 8) {
 #pragma unroll
         for (int u = 0; u < 8; u++) {
@@ -1298,7 +1300,7 @@ __device__ __forceinline__ void sum_items(const V *__restrict__ part, int64_t i0
         }
     }
     if (j < sl.n) {
-        const int r = (int)(sl.n - j);
+        const int r = sl.n - j;
         V v[8];
 #pragma unroll
         for (int u = 0; u < 8; u++)

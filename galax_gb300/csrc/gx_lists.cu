@@ -1432,6 +1432,8 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
         ctx->launches++;
     }
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    // the partial sums index items in 31 bits
+    if (tot[0] >= ((int64_t)1 << 31)) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "more than 2^31 P2P work items");
     GX_TRY(gx_ensure(ctx, I.leaf, sizeof(int32_t) * (size_t)(tot[0] + 1)));
     GX_TRY(gx_ensure(ctx, I.qb, sizeof(int64_t) * (size_t)(tot[0] + 1)));
     GX_TRY(gx_ensure(ctx, I.nq, sizeof(int32_t) * (size_t)(tot[0] + 1)));
