@@ -90,7 +90,7 @@ def test_accurate_plan_regrows_its_storage(G, oracle):
     """A tiny opening angle (0.02) on 2500 leaves of 8 bodies: almost every leaf pair is
     near (6.2M leaf near pairs, more list units and entries than the plan's first
     capacities), so the plan overflows, grows its arrays and is redone.  The lists and
-    forces must equal the oracle's."""
+    forces must equal the oracle's, in the FP64 and the mixed form."""
     from galax_gb300 import presets
     n = 20_000
     b = presets.uniform(n, seed=11)
@@ -106,11 +106,19 @@ def test_accurate_plan_regrows_its_storage(G, oracle):
     ax, ay = np.zeros(n), np.zeros(n)
     ctx.compute_forces(ob.x.copy(), ob.y.copy(), ob.mass.copy(), ax, ay)
     n_far, n_near, _ = ctx.plan_info()
+    # the mixed form on the same plan: every leaf has ~80 P2P items (> 32), so its
+    # partials are folded in groups before the ordered sum
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.02)
+    mx, my = np.zeros(n), np.zeros(n)
+    ctx.compute_forces(ob.x.copy(), ob.y.copy(), ob.mass.copy(), mx, my)
     ctx.close()
     assert n_far == far.off[-1]
     assert n_near == int(np.diff(near.off)[: t.n_leaves].sum())
+    assert n_near > 32 * 32 * t.n_leaves  # more than 32 items of 32 source leaves per leaf on average
     err = rel_vec_err(ax, ay, ref.ax, ref.ay)
     assert err.max() < TOL_FP64, f"max {err.max():.3e}"
+    e32 = rel_vec_err(mx, my, ref.ax, ref.ay)
+    assert np.median(e32) < 1e-5 and e32.max() < 1e-3, (np.median(e32), e32.max())
 
 
 @pytest.mark.parametrize("preset,n", [("uniform", 10_000), ("plummer", 30_000)])
