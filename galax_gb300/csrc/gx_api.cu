@@ -607,6 +607,19 @@ int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64
     return GX_OK;
 }
 
+// The device address of a page-locked host array of n doubles (cudaHostAlloc or
+// cudaHostRegister), or null for any other memory.
+static double *mapped_host(double *p, int64_t n) {
+    if (!p || n <= 0) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // pageable memory on older runtimes: not an error of the call
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return static_cast<double *>(at.devicePointer);
+}
+
 // Enqueue one evaluation (the plan first if it is stale).
 static int forces_launch(gx_ctx *ctx, bool timed) {
     GX_TRY(ensure_plan(ctx));
@@ -644,9 +657,19 @@ int gx_compute_forces(gx_ctx *ctx, const double *x, const double *y, const doubl
     if (!x || !y || !m || !ax || !ay) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null array");
     int64_t n = ctx->n_bodies;
     GX_TRY(upload_bodies_impl(ctx, n, x, y, nullptr, nullptr, m, nullptr, nullptr, false));
-    GX_TRY(forces_launch(ctx, true));
-    // the read-back is queued behind the evaluation: one wait for both, then the status
-    if (n > 0) {
+    // page-locked outputs are written by the evaluation's last kernel itself, so the
+    // transfer over the host link overlaps that kernel instead of following it
+    double *hax = mapped_host(ax, n), *hay = mapped_host(ay, n);
+    const bool direct = hax && hay && ctx->n_nodes > 0;
+    if (direct) {
+        ctx->out_ax = hax;
+        ctx->out_ay = hay;
+    }
+    const int rc = forces_launch(ctx, true);
+    ctx->out_ax = ctx->out_ay = nullptr;
+    GX_TRY(rc);
+    // otherwise the read-back is queued behind the evaluation: one wait for both
+    if (n > 0 && !direct) {
         GX_CUDA(ctx, cudaMemcpyAsync(ax, ctx->ax.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(ay, ctx->ay.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     }

@@ -1322,7 +1322,8 @@ __global__ void __launch_bounds__(128) k_l2p_reduce64(int64_t nl, const double *
                                                       const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
                                                       const double *__restrict__ Lf, const int64_t *__restrict__ item_off,
                                                       int tchunks, const double2 *__restrict__ part,
-                                                      double *__restrict__ ax, double *__restrict__ ay) {
+                                                      double *__restrict__ ax, double *__restrict__ ay,
+                                                      double *__restrict__ hax, double *__restrict__ hay) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<double>(NC);
     int lane = threadIdx.x & 31;
@@ -1339,6 +1340,10 @@ __global__ void __launch_bounds__(128) k_l2p_reduce64(int64_t nl, const double *
         sum_items<double2, double>(part, i0, i1, tchunks, tc, lane, sx, sy);
         ax[i] = sx - fx;
         ay[i] = sy - fy;
+        if (hax) {
+            hax[i] = sx - fx;
+            hay[i] = sy - fy;
+        }
     }
 }
 
@@ -1369,7 +1374,8 @@ __global__ void __launch_bounds__(128) k_reduce32(int64_t nl, const int32_t *__r
                                                   const int32_t *__restrict__ be, const int64_t *__restrict__ item_off,
                                                   int tchunks, const float2 *__restrict__ part,
                                                   const float2 *__restrict__ fl, double *__restrict__ ax,
-                                                  double *__restrict__ ay) {
+                                                  double *__restrict__ ay, double *__restrict__ hax,
+                                                  double *__restrict__ hay) {
     int lane = threadIdx.x & 31;
     int64_t leaf = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (leaf >= nl) return;
@@ -1381,8 +1387,13 @@ __global__ void __launch_bounds__(128) k_reduce32(int64_t nl, const int32_t *__r
         const float2 f = fl[i];
         float sx, sy;
         sum_items<float2, float>(part, i0, i1, tchunks, tc, lane, sx, sy);
-        ax[i] = (double)sx - (double)f.x;
-        ay[i] = (double)sy - (double)f.y;
+        const double rx = (double)sx - (double)f.x, ry = (double)sy - (double)f.y;
+        ax[i] = rx;
+        ay[i] = ry;
+        if (hax) {  // the caller's page-locked arrays, written over the host link as the sums finish
+            hax[i] = rx;
+            hay[i] = ry;
+        }
     }
 }
 
@@ -1566,11 +1577,12 @@ int run_forces(gx_ctx *ctx, bool timed) {
         GX_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
         if (mixed) {
             k_reduce32<<<gw, 128, 0, st>>>(nl, bs, be, dptr<int64_t>(I.off), tchunks, dptr<float2>(ctx->part), fl,
-                                           dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+                                           dptr<double>(ctx->ax), dptr<double>(ctx->ay), ctx->out_ax, ctx->out_ay);
         } else {
             k_l2p_reduce64<P><<<gw, 128, 0, st>>>(nl, X, Y, comx, comy, bs, be, reinterpret_cast<const double *>(Lleaf),
                                                   dptr<int64_t>(I.off), tchunks, dptr<double2>(ctx->part),
-                                                  dptr<double>(ctx->ax), dptr<double>(ctx->ay));
+                                                  dptr<double>(ctx->ax), dptr<double>(ctx->ay), ctx->out_ax,
+                                                  ctx->out_ay);
         }
         ctx->launches++;
         tm.mark();  // 6

@@ -154,6 +154,9 @@ struct gx_ctx {
     // skip levels 1 .. chain_levels - 1 (no far lists there), else 0
     int chain_levels = 0;
     bool near_after_far = false;  // measurement only: the near field after the far-field chain
+    // gx_compute_forces into page-locked host arrays: their device addresses, written by
+    // the final sum of the evaluation being enqueued (null otherwise)
+    double *out_ax = nullptr, *out_ay = nullptr;
     unsigned last_status = 0;     // device status bits of the last force evaluation
     DevBuf tree_state;     // tree build: device round state and level starts
     int64_t mac_ucap = 0;  // ACCURATE plan: capacity of the per-level unit arrays
