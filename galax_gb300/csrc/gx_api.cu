@@ -609,7 +609,7 @@ int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64
 
 // The device address of a page-locked host array of n doubles (cudaHostAlloc or
 // cudaHostRegister), or null for any other memory.
-static double *mapped_host(double *p, int64_t n) {
+static double *mapped_host(const double *p, int64_t n) {
     if (!p || n <= 0) return nullptr;
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -618,6 +618,13 @@ static double *mapped_host(double *p, int64_t n) {
     }
     if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
     return static_cast<double *>(at.devicePointer);
+}
+
+// Whether ensure_plan has nothing to do (the plan of the current tree and mode exists).
+static bool plan_current(const gx_ctx *ctx) {
+    if (!ctx->have_tree || !ctx->have_bodies || !ctx->aux_valid) return false;
+    if (ctx->mode == GX_MODE_ACCURATE) return ctx->plan_acc_valid && ctx->plan_theta == ctx->theta;
+    return ctx->ref_lists_valid && ctx->plan_ref_valid && ctx->plan_p == ctx->p && ctx->plan_eps == ctx->eps;
 }
 
 // Enqueue one evaluation (the plan first if it is stale).
@@ -656,17 +663,28 @@ int gx_compute_forces(gx_ctx *ctx, const double *x, const double *y, const doubl
     if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree: call gx_build_tree or gx_upload_tree first");
     if (!x || !y || !m || !ax || !ay) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null array");
     int64_t n = ctx->n_bodies;
-    GX_TRY(upload_bodies_impl(ctx, n, x, y, nullptr, nullptr, m, nullptr, nullptr, false));
-    // page-locked outputs are written by the evaluation's last kernel itself, so the
-    // transfer over the host link overlaps that kernel instead of following it
+    // page-locked inputs are read by the evaluation's first kernel itself (no separate
+    // copies), page-locked outputs written by its last one, so that the transfers over
+    // the host link overlap those kernels instead of preceding or following them
+    const double *hx = mapped_host(x, n), *hy = mapped_host(y, n), *hm = mapped_host(m, n);
     double *hax = mapped_host(ax, n), *hay = mapped_host(ay, n);
+    const bool direct_in = hx && hy && hm && plan_current(ctx);  // a plan built now would read the old positions
     const bool direct = hax && hay && ctx->n_nodes > 0;
+    if (direct_in) {
+        GX_TRY(upload_bodies_impl(ctx, n, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, false));
+        ctx->in_x = hx;
+        ctx->in_y = hy;
+        ctx->in_m = hm;
+    } else {
+        GX_TRY(upload_bodies_impl(ctx, n, x, y, nullptr, nullptr, m, nullptr, nullptr, false));
+    }
     if (direct) {
         ctx->out_ax = hax;
         ctx->out_ay = hay;
     }
     const int rc = forces_launch(ctx, true);
     ctx->out_ax = ctx->out_ay = nullptr;
+    ctx->in_x = ctx->in_y = ctx->in_m = nullptr;
     GX_TRY(rc);
     // otherwise the read-back is queued behind the evaluation: one wait for both
     if (n > 0 && !direct) {

@@ -203,6 +203,32 @@ __global__ void k_prepare(int64_t n, double *x, double *y, double *m, double *ax
     ay[i] = 0.0;
 }
 
+// The same from the caller's page-locked host arrays (hx, hy, hm: their device
+// addresses), read over the host link straight into the resident arrays.
+__global__ void k_prepare_from(int64_t n, const double *__restrict__ hx, const double *__restrict__ hy,
+                               const double *__restrict__ hm, double *x, double *y, double *m, double *ax, double *ay,
+                               unsigned *status) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double xi = hx[i], yi = hy[i], mi = hm[i];
+    bool bad = false;
+    if (fabs(xi) > 1e100 || fabs(yi) > 1e100 || !isfinite(xi) || !isfinite(yi)) {
+        xi = 0.0;
+        yi = 0.0;
+        bad = true;
+    }
+    if (!isfinite(mi) || mi <= 0.0) {
+        mi = 1.0;
+        bad = true;
+    }
+    if (bad) atomicOr(status, GX_DEV_NONFINITE_INPUT);
+    x[i] = xi;
+    y[i] = yi;
+    m[i] = mi;
+    ax[i] = 0.0;
+    ay[i] = 0.0;
+}
+
 // ---------------------------------------------------------------- P2M
 template <int P, class T>
 __global__ void __launch_bounds__(128) k_p2m(int64_t nl, const double *__restrict__ x, const double *__restrict__ y,
@@ -1417,8 +1443,13 @@ int run_forces(gx_ctx *ctx, bool timed) {
     Timer tm{ctx, timed};
     int64_t launches0 = ctx->launches;
     tm.mark();  // 0
-    k_prepare<<<gx_blocks(n, 256), 256, 0, st>>>(n, dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->m),
-                                                 dptr<double>(ctx->ax), dptr<double>(ctx->ay), dptr<unsigned>(ctx->status));
+    if (ctx->in_x)
+        k_prepare_from<<<gx_blocks(n, 256), 256, 0, st>>>(n, ctx->in_x, ctx->in_y, ctx->in_m, dptr<double>(ctx->x),
+                                                          dptr<double>(ctx->y), dptr<double>(ctx->m), dptr<double>(ctx->ax),
+                                                          dptr<double>(ctx->ay), dptr<unsigned>(ctx->status));
+    else
+        k_prepare<<<gx_blocks(n, 256), 256, 0, st>>>(n, dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->m),
+                                                     dptr<double>(ctx->ax), dptr<double>(ctx->ay), dptr<unsigned>(ctx->status));
     ctx->launches++;
     tm.mark();  // 1
     if (nn == 0) {

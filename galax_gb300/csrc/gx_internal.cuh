@@ -157,6 +157,7 @@ struct gx_ctx {
     // gx_compute_forces into page-locked host arrays: their device addresses, written by
     // the final sum of the evaluation being enqueued (null otherwise)
     double *out_ax = nullptr, *out_ay = nullptr;
+    const double *in_x = nullptr, *in_y = nullptr, *in_m = nullptr;  // the same for the inputs, read by k_prepare
     unsigned last_status = 0;     // device status bits of the last force evaluation
     DevBuf tree_state;     // tree build: device round state and level starts
     int64_t mac_ucap = 0;  // ACCURATE plan: capacity of the per-level unit arrays

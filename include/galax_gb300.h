@@ -127,7 +127,8 @@ int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64
  * x, y, m (tree order), runs the six passes, writes ax, ay.  Inputs are sanitised
  * on the device like compute_fmm_force (lib.rs:1474-1482).  Page-locked ax, ay
  * (gx_host_alloc, cudaHostAlloc, cudaHostRegister) are written by the device
- * directly; other memory gets a copy after the evaluation. */
+ * directly, and page-locked x, y, m read directly once the plan exists; other
+ * memory is copied before and after the evaluation. */
 int gx_compute_forces(gx_ctx *ctx, const double *x, const double *y, const double *m, double *ax, double *ay);
 
 /* Device-resident state (no per-step host traffic). */

@@ -229,7 +229,9 @@ def test_near_field_alone_gives_the_same_forces(G):
 @pytest.mark.parametrize("mode,prec", [(0, 0), (2, 1)])
 def test_compute_forces_into_pinned_arrays(G, mode, prec):
     """Page-locked and pageable host arrays give the same bits through
-    gx_compute_forces, on a tree built here and again after a device rebuild."""
+    gx_compute_forces (the page-locked ones are read and written by the kernels
+    themselves once the plan exists), on a tree built here and again after a device
+    rebuild, and inputs to sanitise are sanitised the same way."""
     from galax_gb300 import presets
     n = 30_001
     b = presets.plummer(n, seed=41)
@@ -253,6 +255,17 @@ def test_compute_forces_into_pinned_arrays(G, mode, prec):
         pax.array[:] = np.nan
         pay.array[:] = np.nan
         ctx.compute_forces(hx.array, hy.array, hm.array, pax.array, pay.array)
+        assert np.array_equal(ax, pax.array) and np.array_equal(ay, pay.array)
+        assert ctx.last_status() == 0
+        # a non-finite position and a negative mass, through both routes
+        xin, min_ = b.x.copy(), b.mass.copy()
+        xin[5], min_[7] = np.nan, -1.0
+        ctx.compute_forces(xin, b.y, min_, ax, ay)
+        assert ctx.last_status() == G.STATUS_SANITIZED
+        hx.array[:] = xin
+        hm.array[:] = min_
+        ctx.compute_forces(hx.array, hy.array, hm.array, pax.array, pay.array)
+        assert ctx.last_status() == G.STATUS_SANITIZED
         assert np.array_equal(ax, pax.array) and np.array_equal(ay, pay.array)
     ctx.close()
 
