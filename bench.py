@@ -13,7 +13,9 @@ adjoint/forward time of reverse-mode rollouts.
              context stream, L2 flushed by a 256 MB write before every step,
              outside the step's timed interval)
   e2e        the same through the C ABI call gx_compute_forces with pinned host
-             buffers: each step copies x, y, m host->device and ax, ay back
+             buffers: each step moves x, y, m host->device and ax, ay back over
+             the host link (read and written by the first and last kernels of
+             the evaluation, the arrays being page-locked), timed on the host
   roofline   the dominant kernel (P2P, FP32 pipe): algorithmic FLOPs (14 per
              body-body interaction) per launch / its event-timed duration in the
              timed evaluations (where it shares the SMs with the far-field chain),
