@@ -685,6 +685,9 @@ int gx_compute_forces(gx_ctx *ctx, const double *x, const double *y, const doubl
     const int rc = forces_launch(ctx, true);
     ctx->out_ax = ctx->out_ay = nullptr;
     ctx->in_x = ctx->in_y = ctx->in_m = nullptr;
+    // kernels enqueued before a failure may still read or write the caller's arrays:
+    // let them finish before the call returns
+    if (rc != GX_OK && (direct || direct_in)) cudaStreamSynchronize(ctx->stream);
     GX_TRY(rc);
     // otherwise the read-back is queued behind the evaluation: one wait for both
     if (n > 0 && !direct) {
