@@ -153,12 +153,13 @@ def _cpu_baseline(bodies_sorted, bounds, eps, n_evals: int = 2):
     t = O.tree_build(ob, N_MAX, bounds)
     v, u = O.vlist_build(t), O.ulist_build(t)
     times = []
+    bb = None
     for _ in range(n_evals):
         bb = ob.copy()
         t0 = time.perf_counter()
         O.compute_fmm_force(bb, t, v, u, P, eps, O.MODE_REF)
         times.append(time.perf_counter() - t0)
-    return ob, t, v, u, times, O.get_threads()
+    return ob, t, v, u, times, O.get_threads(), bb
 
 
 def run_reference(args, rank, world, pg):
@@ -349,19 +350,26 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
     T, dt = args.adj_steps, 1e-3
     Rp = _rot(float(np.random.default_rng(args.seed + 8).uniform(0, 2 * np.pi)))
     ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
+    # the stated device-memory budget of the checkpointed rollout: checkpoints, the
+    # kept trees of a segment, permutations and adjoint buffers must fit in it
+    budget = args.hbm_budget_gb * 1e9
     sweep = {}
     for k in args.adj_k:
         _adjoint_run(G, ctx1m, b1m, 3, dt, k, Rp, rebuild=1)  # warm-up (allocations)
         tf, tb, g, peak, L = _adjoint_run(G, ctx1m, b1m, T, dt, k, Rp, rebuild=1)
         sweep[str(k)] = {"fwd_s": tf, "bwd_s": tb, "adjoint_over_forward": tb / tf, "peak_bytes": peak,
+                         "within_hbm_budget": bool(peak <= budget),
                          "finite": bool(all(np.all(np.isfinite(a)) for a in g)) and bool(np.isfinite(L))}
     # gradient of a 20-step prefix: mixed against FP64 (the FP64 form is ~50x slower)
     Tp = 20
     _, _, gm20, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp, rebuild=1)
     ctx1m.set_mode(G.MODE_ACCURATE, G.PREC_FP64, THETA)
     _, _, g64, _, _ = _adjoint_run(G, ctx1m, b1m, Tp, dt, 5, Rp, rebuild=1)
+    fit = [int(k) for k, r in sweep.items() if r["within_hbm_budget"]]
     pl = {"workload": f"plummer N={len(b1m)}, p={P}, n_max={N_MAX}, {T} steps, dt={dt}, mixed, tree rebuilt every step",
-          "checkpoint_sweep": sweep, "grad_rel_err_mixed_vs_fp64_20_steps": _grad_rel(gm20, g64)}
+          "hbm_budget_bytes": budget, "checkpoint_sweep": sweep,
+          "fastest_within_budget": (min(fit, key=lambda k: sweep[str(k)]["adjoint_over_forward"]) if fit else None),
+          "grad_rel_err_mixed_vs_fp64_20_steps": _grad_rel(gm20, g64)}
     if args.fd_dirs_1m > 0:
         # central differences of the FP64 20-step prefix along seeded directions, trees
         # frozen along the unperturbed trajectory; compared with both adjoints
@@ -381,6 +389,35 @@ def run_adjoint(G, presets, ctx1m, b1m, args):
     out["plummer_1m"] = pl
     return out
 
+
+
+def run_disk_compact(G, presets, args):
+    """The disk workload (N = 4,000,000, n_max = 32) at p in {2,4,6,8}: ms per force
+    evaluation of the mixed and FP64 forms (L2 flushed) and their errors against the
+    FP64 N^2 sum on 1000 seeded samples.  ``--sweep disk`` adds n_max 16 and 64."""
+    n, n_max = args.sweep_n, 32
+    bounds = presets.BOUNDS["disk"]
+    b = presets.disk(n, seed=args.seed + 3)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=8, eps64=0.1))
+    ctx.build_tree(b, n_max, bounds)
+    eps = presets.cli_softening(b.x, b.y)
+    ctx.upload_bodies(b)
+    idx = np.sort(np.random.default_rng(4321).choice(n, min(1000, n), replace=False))
+    rows = []
+    for p in (2, 4, 6, 8):
+        ctx.set_params(p, eps)
+        ex, ey = ctx.n2_sampled(idx)
+        for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+            ctx.set_mode(G.MODE_ACCURATE, prec, THETA)
+            ctx.forces_resident()
+            ms, _ = ctx.bench_forces(3 if name == "mixed" else 1, True, 0)
+            r = G.Bodies.new(n)
+            ctx.download_bodies(r)
+            row = {"p": p, "form": name, "ms": float(np.mean(ms)), "bodies_per_s": n / (float(np.mean(ms)) * 1e-3)}
+            row.update(_err_stats(r.ax[idx], r.ay[idx], ex, ey))
+            rows.append(row)
+    ctx.close()
+    return {"workload": f"disk N={n}, n_max={n_max}, theta={THETA}, ACCURATE", "eps": eps, "rows": rows}
 
 
 def run_build_only(args):
@@ -551,6 +588,11 @@ def run_ours(args, rank, world, local, pg):
         res[name] = dict(ms=ms, kms=kms, plan_s=plan_s, far=far, near=near, inter=inter,
                          launches=ctx.last_launch_count(), passes=ctx.last_timings().tolist(),
                          ax=bb.ax.copy(), ay=bb.ay.copy(), steps=steps)
+        if name == "ref_fp64":
+            # the device tree and the reference's V/U lists of this workload, for the
+            # bit-for-bit comparison with the oracle in the CPU leg
+            dev_tree = ctx.export_tree()
+            dev_lists = (ctx.export_lists(G.LIST_V), ctx.export_lists(G.LIST_U))
 
     # force error of each form against the exact FP64 N^2 sum (GPU n2 kernel), 1000 seeded samples
     idx = np.sort(np.random.default_rng(1234).choice(n, min(1000, n), replace=False))
@@ -614,11 +656,35 @@ def run_ours(args, rank, world, local, pg):
         return 0
     uniform10k = run_uniform10k(G, presets, args, not args.no_cpu_baseline)
     cpu = None
+    ref_parity = None
+    ref_vs_cpu = None
     if not args.no_cpu_baseline:
-        _, _, _, _, times, cores = _cpu_baseline(gb, bounds, eps, n_evals=2)
+        ob, t_o, v_o, u_o, times, cores, f_o = _cpu_baseline(gb, bounds, eps, n_evals=2)
         cpu = {"value": n / float(np.median(times)), "unit": "bodies/s", "cores": cores, "kind": "port",
                "sample": f"2 full REF-mode force evaluations of the same N={n} Plummer workload (C restatement "
                          f"of galax-core compute_fmm_force, OpenMP in m2l/l2p like the reference's Rayon)"}
+        # parity at the benchmark size: the device tree, the reference's V/U lists and the
+        # REF-mode FP64 forces of this run against the oracle's (vector metric)
+        tree_eq = (dev_tree.n_nodes == t_o.n_nodes and np.array_equal(dev_tree.level_start, t_o.level_start)
+                   and all(np.array_equal(getattr(dev_tree, f), getattr(t_o, f))
+                           for f in ("cx", "cy", "hw", "mass", "comx", "comy", "body_start", "body_end",
+                                     "parent", "is_leaf", "child")))
+        (vd, vl), (ud, ul) = dev_lists
+        lists_eq = (np.array_equal(vl, v_o.lengths) and np.array_equal(vd, v_o.data)
+                    and np.array_equal(ul, u_o.lengths) and np.array_equal(ud, u_o.data))
+        dref = _rel_err(res["ref_fp64"]["ax"], res["ref_fp64"]["ay"], f_o.ax, f_o.ay)
+        ref_parity = {"workload": f"plummer N={n}, p={P}, n_max={N_MAX}, REF mode, FP64",
+                      "body_order_bit_exact": bool(np.array_equal(ob.x, gb.x) and np.array_equal(ob.y, gb.y)),
+                      "tree_bit_exact": bool(tree_eq), "lists_bit_exact": bool(lists_eq),
+                      "max_rel_force_diff": float(dref.max()), "median_rel_force_diff": float(np.median(dref)),
+                      "tolerance": 1e-10}
+        ref_gpu = n / (float(np.mean(res["ref_fp64"]["ms"])) * 1e-3)
+        ref_vs_cpu = {"what": "the reference's own algorithm (REF semantics, FP64) on the GPU against the same "
+                              "algorithm on the host cores (oracle port), same workload and run: like for like",
+                      "gpu_bodies_per_s": ref_gpu, "cpu_bodies_per_s": cpu["value"], "ratio": ref_gpu / cpu["value"]}
+    disk = None
+    if not args.no_disk:
+        disk = run_disk_compact(G, presets, args)
     line = {
         "metric": METRIC, "value": world * n / (ms_step * 1e-3), "unit": "bodies/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -651,7 +717,10 @@ def run_ours(args, rank, world, local, pg):
                           "median_rel_diff": float(np.median(d))},
         "tree": {"nodes": nn, "leaves": nl, "levels": nlev, "build_s_incl_host_copies": setup_tree_s},
         "cpu_baseline": cpu,
+        "ref_parity": ref_parity,
+        "ref_fp64_vs_cpu_reference": ref_vs_cpu,
         "kdk_steps": steps_cmp,
+        "disk_4m": disk,
         "uniform_10k": uniform10k,
         "adjoint": adjoint if adjoint is not None else "not run (--no-adjoint, or N>1 replicas: see the N=1 line)",
     }
@@ -677,11 +746,13 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adj-steps", type=int, default=500)
     ap.add_argument("--adj-k", type=lambda s: [int(v) for v in s.split(",")], default=[10, 22, 50, 1])
-    ap.add_argument("--fd-dirs", type=int, default=2)
-    ap.add_argument("--fd-dirs-1m", type=int, default=0)
+    ap.add_argument("--fd-dirs", type=int, default=16)
+    ap.add_argument("--fd-dirs-1m", type=int, default=8)
     ap.add_argument("--sweep", choices=["disk", "theta"], default=None)
     ap.add_argument("--build-only", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=4_000_000)
+    ap.add_argument("--no-disk", action="store_true")
+    ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

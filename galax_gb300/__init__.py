@@ -141,11 +141,13 @@ def _mag_rel_err(ax, ay, ex, ey):
 def n2_sampled_static(x_dev: int, y_dev: int, m_dev: int, n: int, eps: float, idx, stream: int = 0):
     """Exact FP64 softened forces on sampled targets from the caller's device arrays
     (addresses of n float64 values each), without a context and without allocating
-    device memory: for callers that cannot allocate when they want the check (device
-    memory owned by another runtime's caching allocator, or a stream being captured
-    into a CUDA graph).  At most N2_STATIC_MAX_SAMPLES targets per call; the first
-    call on a device should come before any stream capture; calls that overlap on
-    the GPU race on the shared staging array."""
+    device memory: for callers that cannot allocate when they want the check (their
+    device memory is owned by another runtime's caching allocator).  At most
+    N2_STATIC_MAX_SAMPLES targets per call.  `stream` must not be capturing: the call
+    copies through pageable host memory and waits for the stream.  The device address
+    of the staging array is looked up on the first call on a device and kept for the
+    life of the process.  Calls that overlap on the GPU race on the shared staging
+    array."""
     idx = np.ascontiguousarray(np.asarray(idx, np.int64))
     ax = np.zeros(idx.size)
     ay = np.zeros(idx.size)
@@ -425,6 +427,26 @@ class GpuContext:
         """n2_debug (galax-gpu/src/lib.rs:670-714): exact FP64 softened forces for every body."""
         self.upload_bodies(bodies)
         return self.n2_sampled(np.arange(len(bodies), dtype=np.int64))
+
+    def convergence(self, bodies: Bodies, n_max: int, bounds, eps: float, orders=(2, 4, 6, 8),
+                    sample_size: int = 1000, seed: int = 0):
+        """galax-cli --convergence (galax-cli/src/main.rs:355-377): copies of the bodies'
+        positions and masses (zero velocities and accelerations, like the CLI's ref_bodies),
+        build_constrained on them as they are ordered (it does not sort;
+        galax-core/src/lib.rs:541-588), the reference's V/U lists of that tree, then
+        validate_fmm in REF semantics, FP64, at every order p.  Returns rows
+        (p, samples, max, mean) of the magnitude error against the exact sum, the CLI's
+        table.  The sample draw is seeded (the reference's is not).  The context is left
+        with the balanced tree, REF mode, FP64 and the last order."""
+        rb = Bodies.from_arrays(bodies.x, bodies.y, bodies.mass)
+        self.build_tree(rb, n_max, bounds, balanced=True)
+        self.set_mode(MODE_REF, PREC_FP64, 0.5)
+        rows = []
+        for p in orders:
+            self.set_params(int(p), float(eps))
+            k, mx, mean, _ = self.validate_fmm(rb, sample_size, seed)
+            rows.append((int(p), k, mx, mean))
+        return rows
 
     # -- resident state
     def upload_bodies(self, b: Bodies) -> None:

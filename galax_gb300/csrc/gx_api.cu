@@ -609,14 +609,24 @@ int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64
 
 // The device address of a page-locked host array of n doubles (cudaHostAlloc or
 // cudaHostRegister), or null for any other memory.
+// The array counts as mapped only when its first and its last element resolve to the
+// same page-locked allocation (a registered range shorter than the array would let a
+// kernel run past it over the host link); otherwise it takes the staged copies.
 static double *mapped_host(const double *p, int64_t n) {
     if (!p || n <= 0) return nullptr;
-    cudaPointerAttributes at{};
+    cudaPointerAttributes at{}, at_last{};
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();  // pageable memory on older runtimes: not an error of the call
         return nullptr;
     }
     if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    if (cudaPointerGetAttributes(&at_last, p + (n - 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at_last.type != cudaMemoryTypeHost ||
+        static_cast<const double *>(at_last.devicePointer) != static_cast<const double *>(at.devicePointer) + (n - 1))
+        return nullptr;
     return static_cast<double *>(at.devicePointer);
 }
 

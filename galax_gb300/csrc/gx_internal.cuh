@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "../../include/galax_gb300.h"
+#include "../../include/galax_gb300_bench.h"
 
 #define GX_MAXP 16
 #define GX_LIST_CAP 64

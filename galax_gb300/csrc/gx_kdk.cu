@@ -184,10 +184,10 @@ int gx_n2_device(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, dou
 // device allocation.  Some callers cannot allocate device memory at the moment
 // they want a force check: a simulation whose device memory is owned by another
 // runtime's caching allocator (which may already hold nearly all of HBM, so a
-// cudaMalloc would fail or fragment it), or code running while a stream is being
-// captured into a CUDA graph, where cudaMalloc/cudaFree would break the capture.
-// Their device arrays are passed in; the per-sample indices and results are
-// staged through the file-scope array below instead of context scratch.
+// cudaMalloc would fail or fragment it).  Their device arrays are passed in; the
+// per-sample indices and results are staged through the file-scope array below
+// instead of context scratch.  The call copies through pageable host memory and
+// synchronises its stream, so that stream must not be capturing.
 //
 // The array is GX_N2_STATIC_MAX_SAMPLES * 24 bytes (96 KiB); every GPU that loads
 // this library holds it until the process exits.  All calls on a device share it
@@ -198,7 +198,9 @@ namespace {
 static __device__ __align__(256) unsigned char g_n2_static_scratch[GX_N2_STATIC_MAX_SAMPLES *
                                                                    (sizeof(int64_t) + 2 * sizeof(double))];
 // Device address of the array per device ordinal, found once per device with that
-// device current (the host-side symbol is a stand-in, not a device address).
+// device current (the host-side symbol is a stand-in, not a device address) and kept
+// for the life of the process: it belongs to the device's primary context, so a
+// caller's cudaDeviceReset ends the use of this entry point in that process.
 constexpr int kMaxDevices = 64;
 void *g_n2_static_addr[kMaxDevices] = {};
 std::mutex g_n2_static_mu;

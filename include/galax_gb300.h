@@ -161,19 +161,22 @@ int gx_diagnostics(gx_ctx *ctx, double out[5]);
 int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, double *ay);
 
 /* The same sampled exact sum without a context and without allocating: for
- * callers that cannot allocate device memory when they want the check (their
- * device memory belongs to another runtime's caching allocator, or a stream is
- * being captured into a CUDA graph).  No counterpart in the reference.
+ * callers that cannot allocate device memory when they want the check, because
+ * their device memory belongs to another runtime's caching allocator (which may
+ * hold nearly all of HBM, so a cudaMalloc would fail or fragment its pool).  No
+ * counterpart in the reference.
  * x, y, m are the caller's device arrays of n bodies; idx (host, n_idx entries,
  * each in [0, n)) and the host outputs ax, ay are staged through a file-scope
  * device array of GX_N2_STATIC_MAX_SAMPLES slots (96 KiB, held by every GPU that
  * loads the library until exit); more samples return GX_ERR_CAP_EXCEEDED.  The
  * first call on a device looks up that array's device address (once per device,
- * with the device current): make that first call before any stream capture.
- * Calls share the array and it keeps the last call's contents (each call
- * overwrites all it reads); calls that overlap on the GPU race.  stream is a
- * cudaStream_t (NULL = the legacy default stream); the call returns after the
- * stream has finished the work. */
+ * with the device current) and keeps it for the life of the process: the device's
+ * primary context is assumed, and after a cudaDeviceReset the library must not be
+ * called again in that process.  Calls share the array and it keeps the last
+ * call's contents (each call overwrites all it reads); calls that overlap on the
+ * GPU race.  stream is a cudaStream_t (NULL = the legacy default stream) that must
+ * not be capturing: the call copies through pageable host memory and returns
+ * after the stream has finished the work. */
 #define GX_N2_STATIC_MAX_SAMPLES 4096
 int gx_n2_sampled_static(const double *x, const double *y, const double *m, int64_t n, double eps,
                          const int64_t *idx, int64_t n_idx, double *ax, double *ay, void *stream);
@@ -211,14 +214,6 @@ int gx_rollout_backward(gx_ctx *ctx, const double *lx, const double *ly, const d
  * (P2P) runs on a second, lower-priority stream beside m2m..l2l, so those passes
  * include the slots it takes, and the last entry is the wait for it plus L2P. */
 int gx_last_timings(gx_ctx *ctx, double out[7]);
-/* Runs `reps` force evaluations on the resident bodies and returns the CUDA-event
- * time of each on the context stream (ms) and the time of one kernel of it
- * (`which`: 0 = the P2P kernel, timed on its own stream beside the far-field chain;
- * 1 = the M2L pass; 2 = the P2P kernel started after the far-field chain, so that it
- * runs alone).  With flush_l2 != 0 a 256 MB buffer (twice the L2) is written before
- * each evaluation, outside its timed interval. */
-int gx_bench_forces(gx_ctx *ctx, int32_t reps, int32_t flush_l2, double *ms_each, int32_t which,
-                    double *kernel_ms_each);
 /* Number of kernels the last force evaluation launched. */
 int gx_last_launch_count(gx_ctx *ctx, int64_t *count);
 /* Device status bits of the last force evaluation: GX_STATUS_SANITIZED when
@@ -227,10 +222,6 @@ int gx_last_launch_count(gx_ctx *ctx, int64_t *count);
  * the reference does it silently; the evaluation still returns GX_OK). */
 #define GX_STATUS_SANITIZED 1u
 int gx_last_status(gx_ctx *ctx, uint32_t *status);
-
-/* FP32 FMA throughput of this GPU in TFLOP/s (best of 5 timed launches of a
- * kernel of independent FMA chains): the ceiling used for the FP32 P2P pass. */
-int gx_probe_fp32_tflops(gx_ctx *ctx, double *tflops);
 
 /* Page-locked host memory for the host-buffer entry points (cudaMallocHost);
  * NULL on failure. */

@@ -1,6 +1,9 @@
 """The C ABI library builds for sm_103a, loads, and exports every entry point that
-include/galax_gb300.h declares; host-side argument checks work without a GPU."""
+the headers under include/ declare (the product header galax_gb300.h and the
+measurement header galax_gb300_bench.h); host-side argument checks work without a
+GPU."""
 import ctypes as C
+import glob
 import os
 import re
 
@@ -9,19 +12,26 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "galax_gb300.h")
+HEADERS = sorted(glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
-def declared_functions():
-    src = open(HEADER).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char)\s*\*?\s*(gx_\w+)\s*\(", src, flags=re.M)))
+def declared_functions(headers=None):
+    names = set()
+    for h in headers or HEADERS:
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"^\s*(?:int|void|const char)\s*\*?\s*(gx_\w+)\s*\(", src, flags=re.M))
+    return sorted(names)
 
 
 def test_header_declares_the_boundary():
-    names = declared_functions()
+    names = declared_functions([HEADER])
     for must in ["gx_create", "gx_destroy", "gx_upload_tree", "gx_build_tree", "gx_compute_forces", "gx_kdk_run",
                  "gx_n2_sampled", "gx_export_tree", "gx_export_lists", "gx_last_error"]:
         assert must in names
+    # measurement probes live in the bench header, not in the product boundary
+    assert "gx_probe_fp32_tflops" not in names and "gx_bench_forces" not in names
+    assert "gx_probe_fp32_tflops" in declared_functions() and "gx_bench_forces" in declared_functions()
 
 
 def test_library_exports_every_declared_symbol(G):

@@ -140,6 +140,40 @@ def test_validate_fmm_and_n2_regression_match_the_oracle(G, oracle):
     c2.close()
 
 
+def test_convergence_table_matches_the_oracle(G, oracle):
+    """galax-cli --convergence (galax-cli/src/main.rs:355-377) on a 5k uniform case after
+    5 leapfrog steps (the CLI runs it on the final, drifted state): build_constrained on
+    the bodies as ordered, the reference's V/U lists, validate_fmm at p in {2,4,6,8}.
+    The table equals the one formed from the oracle's constrained tree, REF FMM and
+    exact sum on the same samples."""
+    from galax_gb300 import presets
+    n, n_max, T = 5_000, 32, 5
+    bounds = presets.BOUNDS["uniform"]
+    b = presets.uniform(n, seed=23)
+    ob, t, v, u, eps = oracle_case(oracle, b, n_max, bounds, 4)
+    oracle.compute_fmm_force(ob, t, v, u, 4, eps, oracle.MODE_REF)
+    dt = oracle.cli_dt(ob.ax, ob.ay)
+    oracle.simulate(ob, t, v, u, 4, eps, dt, T, 0, oracle.MODE_REF)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 20, p=4, eps64=eps))
+    state = G.Bodies.from_arrays(ob.x, ob.y, ob.mass, ob.vx, ob.vy)
+    rows = ctx.convergence(state, n_max, bounds, eps, sample_size=400, seed=7)
+    # the oracle's table: ref_bodies = copies of x, y, mass (main.rs:358-361)
+    cb = oracle.Bodies.from_arrays(ob.x, ob.y, ob.mass)
+    tc = oracle.tree_build_constrained(cb, n_max, bounds, accel=True)
+    vc, uc = oracle.vlist_build(tc), oracle.ulist_build(tc)
+    idx = np.sort(np.random.default_rng(7).permutation(n)[:400])
+    rx, ry = oracle.n2_sampled(cb.x, cb.y, cb.mass, eps, idx)
+    assert [r[0] for r in rows] == [2, 4, 6, 8]
+    for p, k, mx, mean in rows:
+        f = cb.copy()
+        oracle.compute_fmm_force(f, tc, vc, uc, p, eps, oracle.MODE_REF)
+        rel = G._mag_rel_err(f.ax[idx], f.ay[idx], rx, ry)
+        assert k == 400
+        assert mx == pytest.approx(float(rel.max()), rel=1e-8), p
+        assert mean == pytest.approx(float(rel.mean()), rel=1e-8), p
+    ctx.close()
+
+
 def test_accurate_mixed_kdk_conserves_momentum(G):
     """The mixed ACCURATE form over 20 steps of the galaxy preset: total momentum stays
     at its initial value relative to sum m|v| (the reference has no device check of this)."""
