@@ -61,6 +61,9 @@ N_DEFAULT = 1_000_000
 # dram__bytes_write.sum) of this workload: the kernel works out of L2
 P2P_TRAFFIC_1M = 67.22e6
 P, N_MAX, THETA = 4, 32, 0.5
+# leaf-level near-list split (M2P / P2L) of the ACCURATE forms: near leaf pairs that are
+# far on one side at this opening angle leave P2P
+THETA_W = 0.35
 
 
 def _dist():
@@ -543,6 +546,49 @@ def run_sweep_theta(args):
     return 0
 
 
+def run_sweep_thetaw(args):
+    """Near-list split sweep on the Plummer workload (N = 1,000,000, p = 4, n_max = 32,
+    theta = 0.5): for each theta_w (0 = no split) the P2P, M2P and P2L pair counts, the
+    evaluation time of the mixed and FP64 forms, the P2P kernel alone, and the errors
+    against the FP64 N^2 sum on 1000 seeded samples.  Prints one JSON line."""
+    import galax_gb300 as G
+    from galax_gb300 import build as gbuild
+    from galax_gb300 import presets
+    gbuild.build()
+    n = args.n
+    b = presets.plummer(n, seed=args.seed)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=P, eps64=0.1))
+    ctx.build_tree(b, N_MAX, presets.BOUNDS["plummer"])
+    ctx.set_params(P, presets.cli_softening(b.x, b.y))
+    ctx.upload_bodies(b)
+    idx = np.sort(np.random.default_rng(1234).choice(n, min(1000, n), replace=False))
+    ex, ey = ctx.n2_sampled(idx)
+    rows = []
+    for tw in (0.0, 0.3, 0.35, 0.4, 0.45, 0.5):
+        ctx.set_near_split(tw)
+        for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+            ctx.set_mode(G.MODE_ACCURATE, prec, THETA)
+            ctx.forces_resident()
+            ms, kms = ctx.bench_forces(10 if name == "mixed" else 1, True, 0)
+            r = G.Bodies.new(n)
+            ctx.download_bodies(r)
+            far, near, inter = ctx.plan_info()
+            m2p, p2l = ctx.plan_split_info()
+            row = {"theta_w": tw, "form": name, "ms": float(np.mean(ms)), "p2p_kernel_ms": float(np.mean(kms)),
+                   "pass_ms": ctx.last_timings().tolist(), "bodies_per_s": n / (float(np.mean(ms)) * 1e-3),
+                   "far_pairs": far, "near_p2p_leaf_pairs": near, "m2p_leaf_pairs": m2p, "p2l_leaf_pairs": p2l,
+                   "p2p_interactions": inter}
+            if name == "mixed":
+                _, kal = ctx.bench_forces(5, True, 2)
+                row["p2p_kernel_ms_alone"] = float(np.mean(kal))
+            row.update(_err_stats(r.ax[idx], r.ay[idx], ex, ey))
+            rows.append(row)
+    ctx.close()
+    print(json.dumps({"sweep": "theta_w", "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "seed": args.seed,
+                      "rows": rows}), flush=True)
+    return 0
+
+
 def run_ours(args, rank, world, local, pg):
     import galax_gb300 as G
     from galax_gb300 import build as gbuild
@@ -748,10 +794,11 @@ def main():
     ap.add_argument("--adj-k", type=lambda s: [int(v) for v in s.split(",")], default=[10, 22, 50, 1])
     ap.add_argument("--fd-dirs", type=int, default=16)
     ap.add_argument("--fd-dirs-1m", type=int, default=8)
-    ap.add_argument("--sweep", choices=["disk", "theta"], default=None)
+    ap.add_argument("--sweep", choices=["disk", "theta", "thetaw"], default=None)
     ap.add_argument("--build-only", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=4_000_000)
     ap.add_argument("--no-disk", action="store_true")
+    ap.add_argument("--theta-w", type=float, default=THETA_W)
     ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -764,6 +811,8 @@ def main():
             return run_sweep_disk(args) if rank == 0 else 0
         if args.sweep == "theta":
             return run_sweep_theta(args) if rank == 0 else 0
+        if args.sweep == "thetaw":
+            return run_sweep_thetaw(args) if rank == 0 else 0
         if args.build_only:
             return run_build_only(args) if rank == 0 else 0
         return run_ours(args, rank, world, local, pg)

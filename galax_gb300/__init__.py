@@ -78,6 +78,8 @@ def lib():
         "gx_last_error": (C.c_char_p, [_VP]),
         "gx_set_mode": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double]),
         "gx_set_params": (C.c_int, [_VP, C.c_uint32, C.c_double]),
+        "gx_set_near_split": (C.c_int, [_VP, C.c_double]),
+        "gx_plan_split_info": (C.c_int, [_VP, _I64, _I64]),
         "gx_upload_tree": (C.c_int, [_VP, C.c_int64, C.c_int64, _D, _D, _D, _D, _D, _D, _I64, _I64, _I32, _I32, _U8,
                                      _U32, _U8, _U32, _U8]),
         "gx_build_tree": (C.c_int, [_VP, C.c_int64, _D, _D, _D, _D, _D, _D, _D, C.c_int64, _D, C.c_int]),
@@ -291,6 +293,17 @@ class GpuContext:
 
     def set_params(self, p: int, eps: float) -> None:
         self._check(lib().gx_set_params(self._h, int(p), float(eps)))
+
+    def set_near_split(self, theta_w: float) -> None:
+        """Leaf-level M2P / P2L for near leaf pairs that are far on one side (ACCURATE mode;
+        0 turns it off).  The adjoint entry points need it off."""
+        self._check(lib().gx_set_near_split(self._h, float(theta_w)))
+
+    def plan_split_info(self):
+        """(M2P leaf pairs, P2L leaf pairs) of the current ACCURATE plan."""
+        a, b = C.c_int64(), C.c_int64()
+        self._check(lib().gx_plan_split_info(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     # -- trees
     def upload_tree_data(self, tree, m2l_lists, p2p_lists) -> None:

@@ -107,6 +107,9 @@ int check_mode(gx_ctx *ctx) {
     if (!ctx->have_tree || !ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "adjoint needs a tree and bodies");
     if (ctx->mode != GX_MODE_ACCURATE)
         return gx_fail(ctx, GX_ERR_STATE, "the adjoint is defined for GX_MODE_ACCURATE (set it with gx_set_mode)");
+    if (ctx->theta_w > 0.0)
+        return gx_fail(ctx, GX_ERR_STATE,
+                       "the adjoint transposes P2P, not M2P/P2L: turn the near-list split off (gx_set_near_split 0)");
     return GX_OK;
 }
 

@@ -189,7 +189,9 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->Lff32, &ctx->pos32, &ctx->fl32, &ctx->part, &ctx->items_ref.leaf, &ctx->items_ref.qb, &ctx->items_ref.nq, &ctx->items_ref.off, &ctx->items_acc.leaf, &ctx->items_acc.qb, &ctx->items_acc.nq, &ctx->items_acc.off, &ctx->scratch_a, &ctx->scratch_b, &ctx->scratch_c, &ctx->scratch_d,
                       &ctx->scratch_e, &ctx->scratch_f, &ctx->scratch_g, &ctx->status, &ctx->red, &ctx->flush, &ctx->adj_lx, &ctx->adj_ly, &ctx->adj_lvx, &ctx->adj_lvy, &ctx->adj_lm, &ctx->adj_gx, &ctx->adj_gy, &ctx->adj_gm, &ctx->adj_lax, &ctx->adj_lay, &ctx->adj_lf, &ctx->adj_dL, &ctx->adj_dM, &ctx->adj_dMleaf, &ctx->adj_lam32, &ctx->ckpt, &ctx->seg, &ctx->ids, &ctx->perm, &ctx->roll_perms, &ctx->radius32,
                       &ctx->m2l_units.node, &ctx->m2l_units.start, &ctx->m2l_units.len, &ctx->m2l_units.node_u,
-                      &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state, &ctx->m2l_cnt};
+                      &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state, &ctx->m2l_cnt, &ctx->split_cnt,
+                      &ctx->split_tot, &ctx->p2l_units.leaf, &ctx->p2l_units.start, &ctx->p2l_units.len,
+                      &ctx->p2l_units.leaf_u, &ctx->p2l_part};
     for (DevBuf *b : bufs) free_buf(*b);
     for (gx_tree_plan &t : ctx->tp_cache) gx_tree_plan_free(t);
     for (auto &e : ctx->ev)
@@ -215,6 +217,14 @@ int gx_set_mode(gx_ctx *ctx, int mode, int precision, double theta) {
     ctx->prec = precision;
     if (mode == GX_MODE_ACCURATE && theta != ctx->theta) ctx->plan_acc_valid = false;
     if (mode == GX_MODE_ACCURATE) ctx->theta = theta;
+    return GX_OK;
+}
+
+int gx_set_near_split(gx_ctx *ctx, double theta_w) {
+    GX_TRY(check_ctx(ctx));
+    if (!(theta_w >= 0.0 && theta_w < 2.0)) return gx_fail(ctx, GX_ERR_INVALID_ARG, "theta_w must be in [0, 2)");
+    if (theta_w != ctx->theta_w) ctx->plan_acc_valid = false;
+    ctx->theta_w = theta_w;
     return GX_OK;
 }
 
@@ -536,9 +546,11 @@ static int ensure_plan(gx_ctx *ctx) {
     if (!ctx->have_bodies) return gx_fail(ctx, GX_ERR_STATE, "no bodies");
     if (!ctx->aux_valid) GX_TRY(gx_plan_tree_aux(ctx));
     if (ctx->mode == GX_MODE_ACCURATE) {
-        if (!ctx->plan_acc_valid || ctx->plan_theta != ctx->theta) {
+        if (!ctx->plan_acc_valid || ctx->plan_theta != ctx->theta || ctx->plan_theta_w != ctx->theta_w) {
             GX_TRY(gx_plan_accurate(ctx));
+            if (ctx->theta_w > 0.0) GX_TRY(gx_plan_near_split(ctx));
             GX_TRY(gx_plan_items(ctx, true));
+            ctx->plan_theta_w = ctx->theta_w;
         }
     } else {
         if (!ctx->ref_lists_valid) {
@@ -556,6 +568,15 @@ static int ensure_plan(gx_ctx *ctx) {
 }  // extern "C"
 int gx_ensure_plan_public(gx_ctx *ctx) { return ensure_plan(ctx); }
 extern "C" {
+
+int gx_plan_split_info(gx_ctx *ctx, int64_t *n_m2p_pairs, int64_t *n_p2l_pairs) {
+    GX_TRY(check_ctx(ctx));
+    GX_TRY(ensure_plan(ctx));
+    const bool on = ctx->mode == GX_MODE_ACCURATE && ctx->theta_w > 0.0;
+    if (n_m2p_pairs) *n_m2p_pairs = on ? ctx->n_m2p_pairs : 0;
+    if (n_p2l_pairs) *n_p2l_pairs = on ? ctx->n_p2l_pairs : 0;
+    return GX_OK;
+}
 
 int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64_t *n_p2p_interactions) {
     GX_TRY(check_ctx(ctx));
@@ -633,7 +654,8 @@ static double *mapped_host(const double *p, int64_t n) {
 // Whether ensure_plan has nothing to do (the plan of the current tree and mode exists).
 static bool plan_current(const gx_ctx *ctx) {
     if (!ctx->have_tree || !ctx->have_bodies || !ctx->aux_valid) return false;
-    if (ctx->mode == GX_MODE_ACCURATE) return ctx->plan_acc_valid && ctx->plan_theta == ctx->theta;
+    if (ctx->mode == GX_MODE_ACCURATE)
+        return ctx->plan_acc_valid && ctx->plan_theta == ctx->theta && ctx->plan_theta_w == ctx->theta_w;
     return ctx->ref_lists_valid && ctx->plan_ref_valid && ctx->plan_p == ctx->p && ctx->plan_eps == ctx->eps;
 }
 

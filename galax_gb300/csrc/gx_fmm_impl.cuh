@@ -825,6 +825,7 @@ __global__ void __launch_bounds__(128) k_p2p64_items(int64_t n_items, const int3
     int32_t leaf = item_leaf[it];
     int64_t qb = item_qb[it];
     int nq = item_nq[it];
+    if (nq < 0) return;  // an M2P item of the near-list split (k_m2p)
     int32_t t0 = bs[leaf], t1 = be[leaf];
     int sl = lane < nq ? src_idx[qb + lane] : -1;
     int sbeg = sl >= 0 ? bs[sl] : 0, send = sl >= 0 ? be[sl] : 0;
@@ -900,6 +901,7 @@ __global__ void __launch_bounds__(128, 7) k_p2p32_items(int64_t n_items, const i
         int32_t leaf = item_leaf[it];
         int64_t qb = item_qb[it];
         int nq = item_nq[it];
+        if (nq < 0) continue;  // an M2P item of the near-list split (k_m2p)
         int32_t t0 = bs[leaf], t1 = be[leaf];
         double tcx = comx[leaf], tcy = comy[leaf];
         int sl = lane < nq ? src_idx[qb + lane] : -1;
@@ -1019,6 +1021,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows1(int64_t n_items, const i
     for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
         const int32_t leaf = item_leaf[it];
         const int nq = item_nq[it];
+        if (nq < 0) continue;  // an M2P item of the near-list split (k_m2p)
         const int32_t t0 = bs[leaf], t1 = be[leaf];
         bool own_lane = false;
         __syncwarp();  // the previous item's reads of meta[w] are done
@@ -1128,6 +1131,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
     for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
         const int32_t leaf = item_leaf[it];
         const int nq = item_nq[it];
+        if (nq < 0) continue;  // an M2P item of the near-list split (k_m2p)
         const int32_t t0 = bs[leaf], t1 = be[leaf];
         bool own_lane = false;
         __syncwarp();  // the previous item's reads of meta[w] are done
@@ -1234,6 +1238,285 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
         else res = make_float2(oxB + xB, oyB + yB);             // target tl + 16 (half 0's part first)
         part[it * 32 + lane] = res;
     }
+}
+
+// ---------------------------------------------------------------- M2P / P2L
+// The leaf-level split of the ACCURATE near lists (theta_w > 0): a near leaf pair whose
+// target bodies are all far from the source leaf takes the source's multipole at each
+// target body (M2P, as extra work items of the target leaf, item_nq < 0); one whose
+// source bodies are all far from the target leaf adds them to its local expansion (P2L,
+// units of at most GX_P2L_UNIT source leaves).  Both use the unscaled Taylor
+// coefficients a_k of 1/R, R^2 = dx^2 + dy^2 + eps^2, from the three-term recurrence of
+// the fused M2L; a derivative of 1/R is k! a_k and the reference's G is its negative.
+
+// a_k for |k| <= N at (dx, dy): a[gx_mi(k, l)]; NR = N or, above the unrolled orders, a
+// run-time copy of it
+template <int N, class T>
+__device__ __forceinline__ void taylor_1r(T dx, T dy, T ir, T ir2, int NR, T *a) {
+    a[0] = ir;
+#pragma unroll
+    for (int n = 1; n <= N; n++) {
+        if (n > NR) break;
+        const T in_ = tab_inv<T>(n) * ir2;
+        const T c1 = -(T)(2 * n - 1) * in_, c2 = -(T)(n - 1) * in_;
+        const T c1x = c1 * dx, c1y = c1 * dy;
+#pragma unroll
+        for (int k = 0; k <= n; k++) {
+            const int l = n - k;
+            T v;
+            if (k >= 1 && l >= 1) v = c1x * a[gx_mi(k - 1, l)] + c1y * a[gx_mi(k, l - 1)];
+            else if (k >= 1) v = c1x * a[gx_mi(k - 1, l)];
+            else v = c1y * a[gx_mi(k, l - 1)];
+            if (k >= 2) v += c2 * a[gx_mi(k - 2, l)];
+            if (l >= 2) v += c2 * a[gx_mi(k, l - 2)];
+            a[gx_mi(k, l)] = v;
+        }
+    }
+}
+
+// M2P of one source multipole M (about com_s, raw coefficients) at offset
+// d = x - com_s:  a(x) = sum_S (-1)^|S| M[S] (S+e)! a_{S+e}(d), e = e_x, e_y.  FP32 at
+// p >= 6 forms the coefficients at unit distance (the 1/R kernel is homogeneous of
+// degree -1 in (d, eps)) and moves the powers of 1/R onto the moments, as the M2L does.
+template <int P, class T>
+__device__ __forceinline__ void m2p_eval(T dx, T dy, T eps2, const T *ms, T &fx, T &fy) {
+    constexpr int N = P + 1;
+    const int PP = gx_rt_order(P);
+    const T ir = rsqrt_t<T>(dx * dx + dy * dy + eps2);
+    T a[nc2(N)];
+    T scale = T(1);
+    T mw[nc2(P)];
+    if constexpr (sizeof(T) == 4 && P >= 6) {
+        T pw = T(1);
+        for (int q = 0; q <= PP; q++) {
+            for (int j = 0; j <= q; j++) mw[gx_mi(q - j, j)] = ms[gx_mi(q - j, j)] * pw;
+            pw *= ir;
+        }
+        // at unit distance R' = 1: a'_0 = 1 and 1/R'^2 = 1 (eps enters through R only);
+        // a_k(d) = a'_k(d / R) R^-(|k|+1)
+        taylor_1r<N, T>(dx * ir, dy * ir, T(1), T(1), PP + 1, a);
+        scale = ir * ir;
+    } else {
+#pragma unroll
+        for (int k = 0; k < nc2(P); k++) mw[k] = ms[k];
+        taylor_1r<N, T>(dx, dy, ir, ir * ir, PP + 1, a);
+    }
+    T sx = T(0), sy = T(0);
+#pragma unroll
+    for (int si = 0; si <= P; si++) {
+        if (si > PP) break;
+#pragma unroll
+        for (int sj = 0; sj <= P - si; sj++) {
+            if (si + sj > PP) break;
+            const T mv = ((si + sj) & 1) ? -mw[gx_mi(si, sj)] : mw[gx_mi(si, sj)];
+            sx += mv * (a[gx_mi(si + 1, sj)] * tab_ff<T>(si + 1, sj));
+            sy += mv * (a[gx_mi(si, sj + 1)] * tab_ff<T>(si, sj + 1));
+        }
+    }
+    fx += sx * scale;
+    fy += sy * scale;
+}
+
+// M2P items: one warp per item with item_nq < 0 (grid-stride; P2P items are skipped),
+// lane per target body (chunks of 32 above 32 bodies).  Per source leaf its lane forms
+// the offset com_a - com_s in FP64 once (rounded to T), shared through shared memory;
+// the source's moment row is a broadcast load.  Writes the item's partial slot like a
+// P2P item, so the ordered sum of the leaf's items includes it.
+template <int P, class T, class V>
+__global__ void __launch_bounds__(128) k_m2p(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                             const int64_t *__restrict__ item_qb, const int32_t *__restrict__ item_nq,
+                                             const float4 *__restrict__ pos, const double *__restrict__ X,
+                                             const double *__restrict__ Y, const double *__restrict__ comx,
+                                             const double *__restrict__ comy, const int32_t *__restrict__ bs,
+                                             const int32_t *__restrict__ be, const int32_t *__restrict__ src_idx,
+                                             T eps2, const T *__restrict__ M, int tchunks, V *__restrict__ part) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    __shared__ T shx[4][32], shy[4][32];
+    __shared__ int32_t shs[4][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
+        const int nq0 = item_nq[it];
+        if (nq0 >= 0) continue;
+        const int nq = -nq0;
+        const int32_t leaf = item_leaf[it];
+        const double tcx = comx[leaf], tcy = comy[leaf];
+        __syncwarp();  // the previous item's reads of the shared arrays are done
+        if (lane < nq) {
+            const int32_t sl = src_idx[item_qb[it] + lane];
+            shs[w][lane] = sl;
+            shx[w][lane] = (T)(tcx - comx[sl]);
+            shy[w][lane] = (T)(tcy - comy[sl]);
+        }
+        __syncwarp();
+        const int32_t t0 = bs[leaf], t1 = be[leaf];
+        for (int tc = 0; tc < tchunks; tc++) {
+            const int32_t i = t0 + tc * 32 + lane;
+            T px = T(0), py = T(0);
+            if (i < t1) {
+                if constexpr (sizeof(T) == 4) {
+                    const float4 v = pos[i];
+                    px = v.x;
+                    py = v.y;
+                } else {
+                    px = X[i] - tcx;
+                    py = Y[i] - tcy;
+                }
+            }
+            T fx = T(0), fy = T(0);
+            if (t0 + tc * 32 < t1) {
+                for (int k = 0; k < nq; k++) {
+                    T ms[NC];
+                    load_row<NC>(M + (int64_t)shs[w][k] * NS, ms);
+                    m2p_eval<P, T>(px + shx[w][k], py + shy[w][k], eps2, ms, fx, fy);
+                }
+            }
+            V r;
+            r.x = fx;
+            r.y = fy;
+            part[(it * tchunks + tc) * 32 + lane] = r;
+        }
+    }
+}
+
+// P2L units: one warp per unit (a target leaf and at most GX_P2L_UNIT of its P2L source
+// leaves), lane per source body.  L_a[T] += m_j G^(T)(com_a - x_j) / T! = -m_j a_T(com_a - x_j),
+// summed per lane in body order, then over the warp; a leaf with one unit subtracts the
+// sum from its local directly, otherwise the unit writes a partial and k_p2l_combine
+// adds the partials in unit order.  Runs after L2L (the leaf locals exist) and before L2P.
+// Lane q holds source q's body range and COM offset (one load round for the unit); the
+// bodies of the next source are requested before the current ones are used.
+template <int P, class T>
+__device__ __forceinline__ void p2l_body(T dx, T dy, T mj, T eps2, T *acc) {
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
+    const T ir = rsqrt_t<T>(dx * dx + dy * dy + eps2);
+    T c[nc2(P)];
+    if constexpr (sizeof(T) == 4 && P >= 6) {
+        taylor_1r<P, T>(dx * ir, dy * ir, T(1), T(1), PP, c);
+        T w = mj * ir;
+        for (int q = 0; q <= PP; q++) {
+            for (int i = 0; i <= q; i++) acc[gx_mi(q - i, i)] += w * c[gx_mi(q - i, i)];
+            w *= ir;
+        }
+    } else {
+        taylor_1r<P, T>(dx, dy, ir, ir * ir, PP, c);
+#pragma unroll
+        for (int k = 0; k < NCr; k++) acc[k] += mj * c[k];
+    }
+}
+
+template <int P, class T>
+__global__ void __launch_bounds__(128) k_p2l(int64_t n_units, const int32_t *__restrict__ uleaf,
+                                             const int64_t *__restrict__ ustart, const int32_t *__restrict__ ulen,
+                                             const int64_t *__restrict__ leaf_u, const int32_t *__restrict__ src_idx,
+                                             const float4 *__restrict__ pos, const double *__restrict__ X,
+                                             const double *__restrict__ Y, const double *__restrict__ Mb,
+                                             const double *__restrict__ comx, const double *__restrict__ comy,
+                                             const int32_t *__restrict__ bs, const int32_t *__restrict__ be, T eps2,
+                                             T *__restrict__ Lf, T *__restrict__ ppart) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    (void)NCr;
+    const int lane = threadIdx.x & 31;
+    const int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (u >= n_units) return;
+    const int32_t a = uleaf[u];
+    const int nq = ulen[u];
+    const double tcx = comx[a], tcy = comy[a];
+    int32_t sb = 0, se = 0;
+    T shx = T(0), shy = T(0);
+    double scx = 0.0, scy = 0.0;
+    if (lane < nq) {
+        const int32_t sl = src_idx[ustart[u] + lane];
+        sb = bs[sl];
+        se = be[sl];
+        scx = comx[sl];
+        scy = comy[sl];
+        shx = (T)(tcx - scx);
+        shy = (T)(tcy - scy);
+    }
+    T acc[NC];
+#pragma unroll
+    for (int k = 0; k < NCr; k++) acc[k] = T(0);
+    // one body of source k per lane (the first 32 of the leaf): relative position, mass
+    auto fetch = [&](int k, T &px, T &py, T &pm) {
+        const int32_t j = __shfl_sync(0xffffffffu, sb, k) + lane, j1 = __shfl_sync(0xffffffffu, se, k);
+        if constexpr (sizeof(T) == 4) {
+            const float4 v = j < j1 ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            px = v.x;
+            py = v.y;
+            pm = v.z;
+        } else {
+            const double cx = __shfl_sync(0xffffffffu, scx, k), cy = __shfl_sync(0xffffffffu, scy, k);
+            px = j < j1 ? X[j] - cx : 0.0;
+            py = j < j1 ? Y[j] - cy : 0.0;
+            pm = j < j1 ? Mb[j] : 0.0;
+        }
+    };
+    T cx_ = T(0), cy_ = T(0), cm = T(0);
+    if (nq > 0) fetch(0, cx_, cy_, cm);
+    for (int k = 0; k < nq; k++) {
+        T nx = T(0), ny = T(0), nm = T(0);
+        if (k + 1 < nq) fetch(k + 1, nx, ny, nm);
+        const T ox = __shfl_sync(0xffffffffu, shx, k), oy = __shfl_sync(0xffffffffu, shy, k);
+        const int32_t j0 = __shfl_sync(0xffffffffu, sb, k), j1 = __shfl_sync(0xffffffffu, se, k);
+        const double ckx = __shfl_sync(0xffffffffu, scx, k), cky = __shfl_sync(0xffffffffu, scy, k);
+        (void)ckx;
+        (void)cky;
+        // com_a - x_j = (com_a - com_s) - (x_j - com_s)
+        if (j0 + lane < j1) p2l_body<P, T>(ox - cx_, oy - cy_, cm, eps2, acc);
+        // leaves above 32 bodies (n_max > 32): the rest of the source's bodies
+        for (int32_t j = j0 + 32 + lane; j < j1; j += 32) {
+            T px, py, pm;
+            if constexpr (sizeof(T) == 4) {
+                const float4 v = pos[j];
+                px = v.x;
+                py = v.y;
+                pm = v.z;
+            } else {
+                px = X[j] - ckx;
+                py = Y[j] - cky;
+                pm = Mb[j];
+            }
+            p2l_body<P, T>(ox - px, oy - py, pm, eps2, acc);
+        }
+        cx_ = nx;
+        cy_ = ny;
+        cm = nm;
+    }
+    const bool single = leaf_u[a + 1] - leaf_u[a] == 1;
+#pragma unroll
+    for (int k = 0; k < NCr; k++) {
+        const T v = warp_sum_t<T>(acc[k]);
+        if (lane == (k & 31)) {
+            if (single) Lf[(int64_t)a * NS + k] -= v;
+            else ppart[u * NS + k] = v;
+        }
+    }
+}
+
+// Leaves with several P2L units: the partials in unit order, subtracted from the local.
+template <int P, class T>
+__global__ void k_p2l_combine(int64_t nl, const int64_t *__restrict__ leaf_u, const T *__restrict__ ppart,
+                              T *__restrict__ Lf) {
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<T>(NC);
+    const int PP = gx_rt_order(P);
+    const int NCr = (PP + 1) * (PP + 2) / 2;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t a = t / NC;
+    const int k = (int)(t - a * NC);
+    if (a >= nl || k >= NCr) return;
+    const int64_t u0 = leaf_u[a], u1 = leaf_u[a + 1];
+    if (u1 - u0 < 2) return;
+    T s = T(0);
+    for (int64_t q = u0; q < u1; q++) s += ppart[q * NS + k];
+    Lf[a * NS + k] -= s;
 }
 
 // Folding of long item ranges.  A wide halo leaf can have ~1000 P2P items (977 at 1M
@@ -1467,6 +1750,7 @@ int run_forces(gx_ctx *ctx, bool timed) {
     const int tchunks = (int)std::max<int64_t>(1, (ctx->max_leaf + 31) / 32);
     const int32_t *src_idx = mode == GX_MODE_ACCURATE ? dptr<int32_t>(ctx->near_idx) : dptr<int32_t>(ctx->p2p_idx);
     const unsigned gi = (unsigned)((I.n * 32 + 127) / 128);  // warp per item
+    const bool split = mode == GX_MODE_ACCURATE && ctx->theta_w > 0.0;  // near-list split: M2P items, P2L units
 
     auto passes = [&](auto tag) -> int {
         using T = decltype(tag);
@@ -1516,6 +1800,19 @@ int run_forces(gx_ctx *ctx, bool timed) {
                 k_p2p64_items<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
                                                             dptr<int32_t>(I.nq), X, Y, Mb, bs, be, src_idx, eps2,
                                                             tchunks, dptr<double2>(ctx->part));
+            ctx->launches++;
+        }
+        if (split && ctx->n_m2p_pairs > 0) {
+            // M2P items of the near-list split: their own slots of the same partial array
+            if (mixed)
+                k_m2p<P, float, float2><<<gi, 128, 0, ctx->stream2>>>(
+                    I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), pos, nullptr, nullptr, comx,
+                    comy, bs, be, src_idx, (float)eps2, reinterpret_cast<const float *>(M), tchunks,
+                    dptr<float2>(ctx->part));
+            else
+                k_m2p<P, double, double2><<<gi, 128, 0, ctx->stream2>>>(
+                    I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), nullptr, X, Y, comx, comy, bs,
+                    be, src_idx, eps2, reinterpret_cast<const double *>(M), tchunks, dptr<double2>(ctx->part));
             ctx->launches++;
         }
         if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[15], ctx->stream2));
@@ -1594,6 +1891,17 @@ int run_forces(gx_ctx *ctx, bool timed) {
                                                    comx, comy, L, Lf);
             ctx->launches++;
             Lleaf = Lf;
+        }
+        if (split && ctx->p2l_units.n > 0) {
+            // P2L of the near-list split into the leaf locals, before L2P reads them
+            const gx_ctx::P2LUnits &PU = ctx->p2l_units;
+            GX_TRY(gx_ensure(ctx, ctx->p2l_part, sizeof(T) * NS * (size_t)(PU.n + 1)));
+            const int64_t *leaf_u = dptr<int64_t>(PU.leaf_u);
+            k_p2l<P, T><<<(unsigned)((PU.n * 32 + 127) / 128), 128, 0, st>>>(
+                PU.n, dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start), dptr<int32_t>(PU.len), leaf_u, src_idx, pos, X, Y,
+                Mb, comx, comy, bs, be, (T)eps2, Lf, dptr<T>(ctx->p2l_part));
+            k_p2l_combine<P, T><<<gx_blocks(nl * NC, 256), 256, 0, st>>>(nl, leaf_u, dptr<T>(ctx->p2l_part), Lf);
+            ctx->launches += 2;
         }
         float2 *fl = nullptr;
         if (mixed) {  // L2P beside the near field

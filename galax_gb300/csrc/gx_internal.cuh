@@ -144,6 +144,19 @@ struct gx_ctx {
         int64_t n = 0;
     } m2l_units;
     DevBuf m2l_part;  // per-unit partial locals of nodes cut into several units
+    // ACCURATE near-list split (theta_w > 0): every leaf's near list is partitioned in
+    // place into [P2P | M2P | P2L] sources; the leaf's near count becomes its P2P count
+    // and split_cnt holds (M2P count, P2L count) per leaf.  M2P sources become extra work
+    // items of the leaf (item_nq < 0), P2L sources units of at most GX_P2L_UNIT leaves.
+    double theta_w = 0.0, plan_theta_w = 0.0;
+    DevBuf split_cnt;      // int32 [2 * n_leaves]
+    DevBuf split_tot;      // int64 [4]: P2P, M2P, P2L pairs (device totals of the split)
+    int64_t n_m2p_pairs = 0, n_p2l_pairs = 0, n_m2p_items = 0;
+    struct P2LUnits {
+        DevBuf leaf, start, len, leaf_u;  // int32, int64, int32, int64[n_leaves+1]
+        int64_t n = 0;
+    } p2l_units;
+    DevBuf p2l_part;  // per-unit partial locals of leaves with several P2L units
     DevBuf m2l_cnt;   // plan scratch: units per node
     DevBuf plan_ctr;       // ACCURATE plan: device running totals and overflow flags
     // sizes of the last tree and plan: the first capacities of the next build and plan
@@ -207,6 +220,7 @@ int gx_plan_ref(gx_ctx *ctx);
 int gx_plan_accurate(gx_ctx *ctx);
 int gx_plan_items(gx_ctx *ctx, bool accurate);
 int gx_plan_tree_aux(gx_ctx *ctx);
+int gx_plan_near_split(gx_ctx *ctx);
 // gx_fmm.cu
 int gx_forces_device(gx_ctx *ctx, bool timed);
 // gx_api.cu: device rebuild with the last build's parameters (permutes the resident
@@ -247,6 +261,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 __host__ __device__ constexpr int gx_nc(int p) { return (p + 1) * (p + 2) / 2; }
 constexpr int GX_M2L_UNIT = 256;  // far sources per M2L work unit (8 rounds of a warp)
+constexpr int GX_P2L_UNIT = 32;   // source leaves per P2L work unit (one per lane)
 __host__ __device__ constexpr int gx_mi(int i, int j) { return (i + j) * (i + j + 1) / 2 + j; }
 __host__ __device__ constexpr int gx_kdi(int k, int l, int p) { return (k + l) * (2 * p + 1) + l; }
 #endif

@@ -1271,6 +1271,102 @@ int gx_plan_accurate(gx_ctx *ctx) {
 }
 
 namespace {
+// Near-list split, one warp per leaf.  A near pair (a <- s), s != a, is M2P when every
+// target body sees the source leaf from at least d - R_a with (d - R_a) theta_w > R_s,
+// else P2L when every source body lies at least d - R_s from com_a with
+// (d - R_s) theta_w > R_a, else P2P; the leaf itself is P2P.  Tested in FP32 on the
+// MAC's operands with separately rounded operations (the oracle's gxo_near_split makes
+// the same decisions):  d2 tw^2 > (R_s + tw R_a)^2, then d2 tw^2 > (R_a + tw R_s)^2.
+__device__ __forceinline__ int near_kind(const float4 A, float Ra, const float4 B, float Rs, float tw, float tw2) {
+    const float ex = __fadd_rn(__fsub_rn(A.x, B.x), __fsub_rn(A.y, B.y));
+    const float ey = __fadd_rn(__fsub_rn(A.z, B.z), __fsub_rn(A.w, B.w));
+    const float lhs = __fmul_rn(__fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey)), tw2);
+    const float sm = __fadd_rn(Rs, __fmul_rn(tw, Ra));
+    if (lhs > __fmul_rn(sm, sm)) return 1;
+    const float sl = __fadd_rn(Ra, __fmul_rn(tw, Rs));
+    return lhs > __fmul_rn(sl, sl) ? 2 : 0;
+}
+
+// The leaf's list is copied to scratch (same offsets) and written back partitioned as
+// [P2P | M2P | P2L], each part in list order; the leaf's near count becomes its P2P
+// count, split_cnt[2a], [2a + 1] its M2P and P2L counts; tot gets the three totals.
+__global__ void __launch_bounds__(128) k_near_split(int64_t nl, const int64_t *__restrict__ nstart,
+                                                    int32_t *__restrict__ ncnt, int32_t *__restrict__ near_idx,
+                                                    int32_t *__restrict__ scratch, const float4 *__restrict__ hl,
+                                                    const float *__restrict__ R32, float tw, float tw2,
+                                                    int32_t *__restrict__ split_cnt,
+                                                    unsigned long long *__restrict__ tot) {
+    const int lane = threadIdx.x & 31;
+    const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (a >= nl) return;
+    const int64_t s0 = nstart[a];
+    const int c = ncnt[a];
+    const float4 A = hl[a];
+    const float Ra = R32[a];
+    const unsigned lt = (1u << lane) - 1u;
+    int n1 = 0, n2 = 0;
+    for (int b = 0; b < c; b += 32) {
+        const int q = b + lane;
+        const bool v = q < c;
+        const int32_t src = v ? near_idx[s0 + q] : 0;
+        const int k = (v && src != (int32_t)a) ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
+        if (v) scratch[s0 + q] = src;
+        n1 += __popc(__ballot_sync(0xffffffffu, v && k == 1));
+        n2 += __popc(__ballot_sync(0xffffffffu, v && k == 2));
+    }
+    __syncwarp();  // the copy is complete before it is read back
+    const int n0 = c - n1 - n2;
+    int o[3] = {0, n0, n0 + n1};
+    for (int b = 0; b < c; b += 32) {
+        const int q = b + lane;
+        const bool v = q < c;
+        const int32_t src = v ? scratch[s0 + q] : 0;
+        const int k = (v && src != (int32_t)a) ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++) {
+            const unsigned m = __ballot_sync(0xffffffffu, v && k == kk);
+            if (v && k == kk) near_idx[s0 + o[kk] + __popc(m & lt)] = src;
+            o[kk] += __popc(m);
+        }
+    }
+    if (lane == 0) {
+        ncnt[a] = n0;
+        split_cnt[2 * a] = n1;
+        split_cnt[2 * a + 1] = n2;
+        atomicAdd(tot + 0, (unsigned long long)n0);
+        atomicAdd(tot + 1, (unsigned long long)n1);
+        atomicAdd(tot + 2, (unsigned long long)n2);
+    }
+}
+}  // namespace
+
+// The leaf-level split of the ACCURATE near lists (theta_w > 0; no counterpart in the
+// reference, whose U-list pairs are all P2P, lib.rs:1395-1462): leaf pairs that fail the
+// MAC but whose bodies are far on one side take the source leaf's multipole at each
+// target body (M2P) or the source bodies into the target's local (P2L), both with
+// truncation bounded by theta_w^(p+1) like the far pairs' by theta^(p+1).  Runs after
+// gx_plan_accurate; the totals are read back by gx_plan_items.
+int gx_plan_near_split(gx_ctx *ctx) {
+    const int64_t nl = ctx->n_leaves, nn = ctx->n_nodes;
+    GX_TRY(gx_ensure(ctx, ctx->split_cnt, sizeof(int32_t) * 2 * (size_t)(nl > 0 ? nl : 1)));
+    GX_TRY(gx_ensure(ctx, ctx->split_tot, sizeof(unsigned long long) * 4));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_f, sizeof(int32_t) * (size_t)(ctx->hint_near + 1)));
+    GX_CUDA(ctx, cudaMemsetAsync(ctx->split_tot.p, 0, sizeof(unsigned long long) * 4, ctx->stream));
+    if (nl > 0) {
+        int64_t *nstart = dptr<int64_t>(ctx->near_off);
+        int32_t *ncnt = reinterpret_cast<int32_t *>(nstart + nn);
+        const float tw = (float)ctx->theta_w, tw2 = tw * tw;
+        k_near_split<<<(unsigned)((nl * 32 + 127) / 128), 128, 0, ctx->stream>>>(
+            nl, nstart, ncnt, dptr<int32_t>(ctx->near_idx), dptr<int32_t>(ctx->scratch_f), dptr<float4>(ctx->comhl),
+            dptr<float>(ctx->radius32), tw, tw2, dptr<int32_t>(ctx->split_cnt),
+            dptr<unsigned long long>(ctx->split_tot));
+        ctx->launches++;
+    }
+    GX_CUDA(ctx, cudaGetLastError());
+    return GX_OK;
+}
+
+namespace {
 constexpr int P2P_K = 32;  // source leaves per P2P work item
 
 // ancestor table: anc[level * nl + leaf] = the leaf's ancestor at that level
@@ -1293,26 +1389,58 @@ __global__ void k_comhl(int64_t nn, const double *comx, const double *comy, floa
 }
 
 
-// per leaf: number of items; start/count from either list layout
-__global__ void k_items_count(int64_t nl, const int64_t *start, const int32_t *cnt, int64_t *nitems) {
+// per leaf: number of items; start/count from either list layout.  With the near-list
+// split (split != null) the leaf's P2P items are followed by its M2P items, whose
+// source count is stored negated; split[2a] is the leaf's M2P count.
+__global__ void k_items_count(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split,
+                              int64_t *nitems) {
     int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a > nl) return;
     if (a == nl) { nitems[a] = 0; return; }
     int64_t c = cnt ? cnt[a] : start[a + 1] - start[a];
-    nitems[a] = (c + P2P_K - 1) / P2P_K;
+    int64_t cm = split ? split[2 * a] : 0;
+    nitems[a] = (c + P2P_K - 1) / P2P_K + (cm + P2P_K - 1) / P2P_K;
 }
 
-__global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int64_t *off, int32_t *leaf,
-                             int64_t *qb, int32_t *nq) {
+__global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split,
+                             const int64_t *off, int32_t *leaf, int64_t *qb, int32_t *nq) {
     int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nl) return;
     int64_t s0 = start[a];
     int64_t c = cnt ? cnt[a] : start[a + 1] - start[a];
-    for (int64_t k = 0; k * P2P_K < c; k++) {
-        int64_t it = off[a] + k;
+    int64_t it = off[a];
+    for (int64_t k = 0; k * P2P_K < c; k++, it++) {
         leaf[it] = (int32_t)a;
         qb[it] = s0 + k * P2P_K;
         nq[it] = (int32_t)min((int64_t)P2P_K, c - k * P2P_K);
+    }
+    const int64_t cm = split ? split[2 * a] : 0;
+    for (int64_t k = 0; k * P2P_K < cm; k++, it++) {
+        leaf[it] = (int32_t)a;
+        qb[it] = s0 + c + k * P2P_K;
+        nq[it] = -(int32_t)min((int64_t)P2P_K, cm - k * P2P_K);
+    }
+}
+
+// P2L units: per leaf the number of units of at most GX_P2L_UNIT source leaves (its P2L
+// sources follow its P2P and M2P sources); then unit -> (leaf, first, length)
+__global__ void k_p2l_units_count(int64_t nl, const int32_t *split, int64_t *nunits) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a > nl) return;
+    nunits[a] = a == nl ? 0 : (split[2 * a + 1] + GX_P2L_UNIT - 1) / GX_P2L_UNIT;
+}
+
+__global__ void k_p2l_units_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split,
+                                 const int64_t *leaf_u, int32_t *uleaf, int64_t *ustart, int32_t *ulen) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= nl) return;
+    const int64_t s0 = start[a] + cnt[a] + split[2 * a];
+    const int32_t c = split[2 * a + 1];
+    int64_t u = leaf_u[a];
+    for (int32_t k = 0; k * GX_P2L_UNIT < c; k++, u++) {
+        uleaf[u] = (int32_t)a;
+        ustart[u] = s0 + (int64_t)k * GX_P2L_UNIT;
+        ulen[u] = min(GX_P2L_UNIT, c - k * GX_P2L_UNIT);
     }
 }
 
@@ -1410,12 +1538,27 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     }
     // the P2P items and (ACCURATE) the M2L units: counts and scans of both, one wait for
     // their two totals, then both fills
+    const bool split = accurate && ctx->theta_w > 0.0;
+    const int32_t *scnt = split ? dptr<int32_t>(ctx->split_cnt) : nullptr;
     GX_TRY(gx_ensure(ctx, I.off, sizeof(int64_t) * (size_t)(nl + 1)));
     GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nl + 1)));
     int64_t *nit = dptr<int64_t>(ctx->scratch_c);
-    k_items_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, start, cnt, nit);
+    k_items_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, nit);
     GX_TRY(gx_exclusive_scan_i64(ctx, nit, dptr<int64_t>(I.off), nl + 1));
-    int64_t tot[2] = {0, 0};
+    int64_t tot[3] = {0, 0, 0};
+    unsigned long long stot[4] = {0, 0, 0, 0};
+    gx_ctx::P2LUnits &PU = ctx->p2l_units;
+    if (split) {
+        GX_TRY(gx_ensure(ctx, PU.leaf_u, sizeof(int64_t) * (size_t)(nl + 1)));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int64_t) * (size_t)(nl + 1)));
+        int64_t *npu = dptr<int64_t>(ctx->scratch_b);
+        k_p2l_units_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, scnt, npu);
+        GX_TRY(gx_exclusive_scan_i64(ctx, npu, dptr<int64_t>(PU.leaf_u), nl + 1));
+        GX_CUDA(ctx, cudaMemcpyAsync(&tot[2], dptr<int64_t>(PU.leaf_u) + nl, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(stot, ctx->split_tot.p, sizeof(stot), cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->launches++;
+    }
     GX_CUDA(ctx, cudaMemcpyAsync(&tot[0], dptr<int64_t>(I.off) + nl, sizeof(int64_t), cudaMemcpyDeviceToHost,
                                  ctx->stream));
     gx_ctx::M2LUnits &U = ctx->m2l_units;
@@ -1437,10 +1580,27 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     GX_TRY(gx_ensure(ctx, I.leaf, sizeof(int32_t) * (size_t)(tot[0] + 1)));
     GX_TRY(gx_ensure(ctx, I.qb, sizeof(int64_t) * (size_t)(tot[0] + 1)));
     GX_TRY(gx_ensure(ctx, I.nq, sizeof(int32_t) * (size_t)(tot[0] + 1)));
-    k_items_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, start, cnt, dptr<int64_t>(I.off), dptr<int32_t>(I.leaf),
-                                                              dptr<int64_t>(I.qb), dptr<int32_t>(I.nq));
+    k_items_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, dptr<int64_t>(I.off),
+                                                              dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                              dptr<int32_t>(I.nq));
     ctx->launches += 2;
     I.n = tot[0];
+    PU.n = 0;
+    ctx->n_m2p_pairs = ctx->n_p2l_pairs = 0;
+    if (split) {
+        ctx->n_near_pairs = (int64_t)stot[0];
+        ctx->n_m2p_pairs = (int64_t)stot[1];
+        ctx->n_p2l_pairs = (int64_t)stot[2];
+        const int64_t npu = tot[2];
+        GX_TRY(gx_ensure(ctx, PU.leaf, sizeof(int32_t) * (size_t)(npu + 1)));
+        GX_TRY(gx_ensure(ctx, PU.start, sizeof(int64_t) * (size_t)(npu + 1)));
+        GX_TRY(gx_ensure(ctx, PU.len, sizeof(int32_t) * (size_t)(npu + 1)));
+        k_p2l_units_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, dptr<int64_t>(PU.leaf_u),
+                                                                      dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
+                                                                      dptr<int32_t>(PU.len));
+        ctx->launches++;
+        PU.n = npu;
+    }
     if (accurate) {
         const int64_t nun = tot[1];
         GX_TRY(gx_ensure(ctx, U.node, sizeof(int32_t) * (size_t)(nun + 1)));

@@ -81,6 +81,17 @@ int gx_abi_version(void);
 
 /* Evaluation mode, precision and MAC opening angle (theta, ACCURATE only). */
 int gx_set_mode(gx_ctx *ctx, int mode, int precision, double theta);
+/* The leaf-level split of the ACCURATE near lists (no counterpart in the reference,
+ * whose U-list pairs are all P2P, galax-core/src/lib.rs:1395-1462).  With theta_w > 0 a
+ * near leaf pair (target a, source s, s != a) whose target bodies all see s from
+ * (d - R_a) with (d - R_a) theta_w > R_s evaluates s's multipole at each target body
+ * (M2P); else one whose source bodies all lie (d - R_s) from a's centre of mass with
+ * (d - R_s) theta_w > R_a adds them to a's local expansion (P2L); the rest stay P2P.
+ * Both bound the truncation by theta_w^(p+1).  theta_w = 0 (the default) turns it off.
+ * The adjoint entry points need it off. */
+int gx_set_near_split(gx_ctx *ctx, double theta_w);
+/* Leaf pairs of the current ACCURATE plan taken by M2P and by P2L (0 with the split off). */
+int gx_plan_split_info(gx_ctx *ctx, int64_t *n_m2p_pairs, int64_t *n_p2l_pairs);
 /* Changes p and the softening of an existing context. */
 int gx_set_params(gx_ctx *ctx, uint32_t p, double eps);
 

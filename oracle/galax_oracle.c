@@ -1459,8 +1459,78 @@ void gxo_mac_lists_build(const gxo_tree *t, const double *R, double theta, gxo_c
     free(R32);
 }
 
+/* The leaf-level split of the near lists (not in the reference).  A near pair
+ * (a <- s), s != a, whose target bodies all see the source leaf from at least
+ * d - R_a, with (d - R_a) theta_w > R_s, takes the source leaf's multipole evaluated at
+ * each target body (M2P); failing that, one whose source bodies all lie at least d - R_s
+ * from com_a, with (d - R_s) theta_w > R_a, adds them to the target leaf's local
+ * expansion (P2L); the rest, and the leaf itself, stay P2P.  Both tests bound the
+ * truncation by theta_w^(p+1), as the far test bounds M2L's.  Decided in float and
+ * squared like mac_far, with the same COM offsets and float radii:
+ *   M2P: d2 theta_w^2 > (R_s + theta_w R_a)^2,  P2L: d2 theta_w^2 > (R_a + theta_w R_s)^2.
+ * List order is kept within each output list. */
+void gxo_near_split(const gxo_tree *t, const double *R, double theta_w, const gxo_csr *near, gxo_csr **p2p_out,
+                    gxo_csr **m2p_out, gxo_csr **p2l_out) {
+    int64_t nn = t->n_nodes;
+    gxo_csr *o[3];
+    for (int k = 0; k < 3; k++) {
+        o[k] = (gxo_csr *)calloc(1, sizeof(gxo_csr));
+        o[k]->n = nn;
+        o[k]->off = (int64_t *)calloc((size_t)(nn + 1), sizeof(int64_t));
+        o[k]->idx = (int32_t *)malloc(sizeof(int32_t) * (size_t)(near->off[nn] + 1));
+    }
+    hl4 *hl = (hl4 *)malloc(sizeof(hl4) * (size_t)(nn > 0 ? nn : 1));
+    float *R32 = (float *)malloc(sizeof(float) * (size_t)(nn > 0 ? nn : 1));
+    for (int64_t i = 0; i < nn; i++) {
+        float xh = (float)t->comx[i], yh = (float)t->comy[i];
+        hl[i].xh = xh;
+        hl[i].xl = (float)(t->comx[i] - (double)xh);
+        hl[i].yh = yh;
+        hl[i].yl = (float)(t->comy[i] - (double)yh);
+        R32[i] = (float)R[i];
+    }
+    const float tw = (float)theta_w, tw2 = tw * tw;
+    int64_t cnt[3] = {0, 0, 0};
+    for (int64_t a = 0; a < nn; a++) {
+        for (int k = 0; k < 3; k++) o[k]->off[a] = cnt[k];
+        for (int64_t q = near->off[a]; q < near->off[a + 1]; q++) {
+            int32_t s = near->idx[q];
+            int kind = 0;
+            if (s != a && theta_w > 0.0) {
+                float ex = (hl[a].xh - hl[s].xh) + (hl[a].xl - hl[s].xl);
+                float ey = (hl[a].yh - hl[s].yh) + (hl[a].yl - hl[s].yl);
+                float d2 = ex * ex + ey * ey;
+                float lhs = d2 * tw2;
+                float sm = R32[s] + tw * R32[a];
+                float sl = R32[a] + tw * R32[s];
+                if (lhs > sm * sm) kind = 1;
+                else if (lhs > sl * sl) kind = 2;
+            }
+            o[kind]->idx[cnt[kind]++] = s;
+        }
+    }
+    for (int k = 0; k < 3; k++) o[k]->off[nn] = cnt[k];
+    *p2p_out = o[0];
+    *m2p_out = o[1];
+    *p2l_out = o[2];
+    free(hl);
+    free(R32);
+}
+
 void gxo_compute_fmm_force_mac(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
                                const gxo_csr *far, const gxo_csr *near, int64_t p, double eps) {
+    gxo_compute_fmm_force_wx(x, y, m, ax, ay, t, far, near, NULL, NULL, p, eps);
+}
+
+/* gxo_compute_fmm_force_mac with the split near lists: P2L into the leaf locals after
+ * the top-down L2L, L2P, M2P onto the bodies, then P2P over `near` (the remaining
+ * pairs).  m2p / p2l may be NULL.
+ *   M2P: a(x) = -sum_S (-1)^|S| M_s[S] G^(S+e)(x - com_s)   (e = e_x, e_y; G the
+ *        reference's derivatives of -1/R, lib.rs:1040-1151)
+ *   P2L: L_a[T] += m_j G^(T)(com_a - x_j) / T!   (M2L of a point mass, lib.rs:1199-1259) */
+void gxo_compute_fmm_force_wx(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
+                              const gxo_csr *far, const gxo_csr *near, const gxo_csr *m2p, const gxo_csr *p2l,
+                              int64_t p, double eps) {
     init_tables();
     int64_t n = t->n_nodes > 0 ? t->body_end[t->n_nodes - 1] : 0;
     for (int64_t i = 0; i < n; i++) {
@@ -1492,7 +1562,56 @@ void gxo_compute_fmm_force_mac(double *x, double *y, double *m, double *ax, doub
         free(G);
     }
     gxo_l2l(loc, t, p, 1);
+    if (p2l) {
+#pragma omp parallel num_threads(gxo_get_threads())
+        {
+            double *G = (double *)malloc(sizeof(double) * DS);
+#pragma omp for schedule(dynamic, 16)
+            for (int64_t id = 0; id < t->n_nodes; id++) {
+                double *L = loc + id * st;
+                for (int64_t q = p2l->off[id]; q < p2l->off[id + 1]; q++) {
+                    int64_t s = p2l->idx[q];
+                    for (int64_t j = t->body_start[s]; j < t->body_end[s]; j++) {
+                        gxo_kernel_derivs_recurrence(t->comx[id] - x[j], t->comy[id] - y[j], eps, p, G);
+                        for (int64_t oi = 0; oi <= p; oi++)
+                            for (int64_t oj = 0; oj <= p - oi; oj++)
+                                L[MI(oi, oj)] += m[j] * G[kdi(oi, oj, p)] / (g_fact[oi] * g_fact[oj]);
+                    }
+                }
+            }
+            free(G);
+        }
+    }
     gxo_l2p(x, y, ax, ay, loc, t, p);
+    if (m2p) {
+        const int64_t pp = (p + 2) / 2; /* derivative orders up to 2 pp >= p + 1 */
+        const int64_t DSp = (2 * pp + 1) * (2 * pp + 1);
+#pragma omp parallel num_threads(gxo_get_threads())
+        {
+            double *G = (double *)malloc(sizeof(double) * DSp);
+#pragma omp for schedule(dynamic, 16)
+            for (int64_t id = 0; id < t->n_nodes; id++) {
+                if (!t->is_leaf[id]) continue;
+                for (int64_t i = t->body_start[id]; i < t->body_end[id]; i++) {
+                    double fx = 0.0, fy = 0.0;
+                    for (int64_t q = m2p->off[id]; q < m2p->off[id + 1]; q++) {
+                        int64_t s = m2p->idx[q];
+                        const double *M = mult + s * st;
+                        gxo_kernel_derivs_recurrence(x[i] - t->comx[s], y[i] - t->comy[s], eps, pp, G);
+                        for (int64_t si = 0; si <= p; si++)
+                            for (int64_t sj = 0; sj <= p - si; sj++) {
+                                double mv = ((si + sj) & 1) ? -M[MI(si, sj)] : M[MI(si, sj)];
+                                fx += mv * G[kdi(si + 1, sj, pp)];
+                                fy += mv * G[kdi(si, sj + 1, pp)];
+                            }
+                    }
+                    ax[i] -= fx;
+                    ay[i] -= fy;
+                }
+            }
+            free(G);
+        }
+    }
     double s2 = eps * eps;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(gxo_get_threads())
     for (int64_t id = 0; id < t->n_nodes; id++) {

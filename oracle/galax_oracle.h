@@ -144,6 +144,14 @@ void gxo_csr_free(gxo_csr *c);
 void gxo_compute_fmm_force_mac(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
                                const gxo_csr *far, const gxo_csr *near, int64_t p, double eps);
 
+/* Leaf-level split of the near lists into P2P, M2P and P2L (criterion theta_w, see the
+ * source), and the evaluation with them; m2p / p2l may be NULL. */
+void gxo_near_split(const gxo_tree *t, const double *R, double theta_w, const gxo_csr *near, gxo_csr **p2p_out,
+                    gxo_csr **m2p_out, gxo_csr **p2l_out);
+void gxo_compute_fmm_force_wx(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
+                              const gxo_csr *far, const gxo_csr *near, const gxo_csr *m2p, const gxo_csr *p2l,
+                              int64_t p, double eps);
+
 /* ---- N^2 adjoint (not in the reference; the reference gradient of the GPU adjoint) ---- */
 void gxo_n2_vjp(const double *x, const double *y, const double *m, int64_t n, double eps, const double *lx,
                 const double *ly, double *gx, double *gy, double *gm);

@@ -450,6 +450,8 @@ def _mac_setup():
     L.gxo_mac_lists_build.argtypes = [_TP, _D, C.c_double, C.POINTER(CP), C.POINTER(CP)]
     L.gxo_csr_free.argtypes = [CP]
     L.gxo_compute_fmm_force_mac.argtypes = [_D] * 5 + [_TP, CP, CP, C.c_int64, C.c_double]
+    L.gxo_near_split.argtypes = [_TP, _D, C.c_double, CP, C.POINTER(CP), C.POINTER(CP), C.POINTER(CP)]
+    L.gxo_compute_fmm_force_wx.argtypes = [_D] * 5 + [_TP, CP, CP, CP, CP, C.c_int64, C.c_double]
     L._mac_ready = True
     return L
 
@@ -472,6 +474,22 @@ def mac_lists_build(t: Tree, radius: np.ndarray, theta: float):
 def compute_fmm_force_mac(b: Bodies, t: Tree, far: Csr, near: Csr, p: int, eps: float) -> None:
     _mac_setup().gxo_compute_fmm_force_mac(_d(b.x), _d(b.y), _d(b.mass), _d(b.ax), _d(b.ay), t.ptr, far.ptr, near.ptr,
                                            int(p), float(eps))
+
+
+def near_split(t: Tree, radius: np.ndarray, theta_w: float, near: Csr):
+    """The near lists split into (p2p, m2p, p2l) by the leaf-level tests of theta_w."""
+    L = _mac_setup()
+    CP = C.POINTER(_Csr)
+    a, b, c = CP(), CP(), CP()
+    r = _arr(radius)
+    L.gxo_near_split(t.ptr, _d(r), float(theta_w), near.ptr, C.byref(a), C.byref(b), C.byref(c))
+    return Csr(a), Csr(b), Csr(c)
+
+
+def compute_fmm_force_wx(b: Bodies, t: Tree, far: Csr, near: Csr, m2p: Csr, p2l: Csr, p: int, eps: float) -> None:
+    _mac_setup().gxo_compute_fmm_force_wx(_d(b.x), _d(b.y), _d(b.mass), _d(b.ax), _d(b.ay), t.ptr, far.ptr,
+                                          near.ptr, m2p.ptr if m2p is not None else None,
+                                          p2l.ptr if p2l is not None else None, int(p), float(eps))
 
 
 # ------------------------------------------------------------ N^2 adjoint

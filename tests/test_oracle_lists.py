@@ -79,3 +79,50 @@ def test_accurate_lists_cover_every_pair_once(oracle):
             for s in near.idx[near.off[a]:near.off[a + 1]]:
                 cover[t.body_start[a]:t.body_end[a], t.body_start[s]:t.body_end[s]] += 1
     assert np.all(cover == 1)
+
+
+def test_near_split_partitions_the_near_lists(oracle):
+    """The near-list split (M2P / P2L / P2P) is a partition of every leaf's near list that
+    keeps list order within each part; far pairs plus the three parts still count every
+    body pair once; and each classified pair satisfies its test, recomputed here in
+    float32 from the same operands (the COM (hi, lo) split and the radii rounded once)."""
+    b = presets.plummer(3000, seed=36)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, 16, presets.BOUNDS["plummer"])
+    R = oracle.node_radii(ob, t)
+    far, near = oracle.mac_lists_build(t, R, 0.5)
+    p2p, m2p, p2l = oracle.near_split(t, R, 0.4, near)
+    assert m2p.off[-1] > 0 and p2l.off[-1] > 0
+    f32 = np.float32
+    hx = t.comx.astype(f32)
+    lx = (t.comx - hx.astype(np.float64)).astype(f32)
+    hy = t.comy.astype(f32)
+    ly = (t.comy - hy.astype(np.float64)).astype(f32)
+    R32 = R.astype(f32)
+    tw = f32(0.4)
+    tw2 = f32(tw * tw)
+
+    def kind(a, s):
+        ex = f32(f32(hx[a] - hx[s]) + f32(lx[a] - lx[s]))
+        ey = f32(f32(hy[a] - hy[s]) + f32(ly[a] - ly[s]))
+        lhs = f32(f32(f32(ex * ex) + f32(ey * ey)) * tw2)
+        sm = f32(R32[s] + f32(tw * R32[a]))
+        if lhs > f32(sm * sm):
+            return 1
+        sl = f32(R32[a] + f32(tw * R32[s]))
+        return 2 if lhs > f32(sl * sl) else 0
+
+    cover = np.zeros((3000, 3000), np.int32)
+    for a in range(t.n_nodes):
+        for s in far.idx[far.off[a]:far.off[a + 1]]:
+            cover[t.body_start[a]:t.body_end[a], t.body_start[s]:t.body_end[s]] += 1
+        if not t.is_leaf[a]:
+            continue
+        whole = list(near.idx[near.off[a]:near.off[a + 1]])
+        parts = [list(c.idx[c.off[a]:c.off[a + 1]]) for c in (p2p, m2p, p2l)]
+        expect = [[s for s in whole if (0 if s == a else kind(a, s)) == k] for k in range(3)]
+        assert parts == expect, a
+        for part in parts:
+            for s in part:
+                cover[t.body_start[a]:t.body_end[a], t.body_start[s]:t.body_end[s]] += 1
+    assert np.all(cover == 1)
