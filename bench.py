@@ -63,7 +63,7 @@ P2P_TRAFFIC_1M = 67.22e6
 P, N_MAX, THETA = 4, 32, 0.5
 # leaf-level near-list split (M2P / P2L) of the ACCURATE forms: near leaf pairs that are
 # far on one side at this opening angle leave P2P
-THETA_W = 0.35
+THETA_W = 0.4
 
 
 def _dist():
@@ -238,6 +238,7 @@ def run_uniform10k(G, presets, args, with_cpu: bool):
     bounds = presets.BOUNDS["uniform"]
     gb = presets.uniform(n, seed=0)
     ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=P, eps64=0.1))
+    ctx.set_near_split(args.theta_w)
     ctx.build_tree(gb, N_MAX, bounds)  # permutes gb into Morton order, as Tree::build does
     eps = presets.cli_softening(gb.x, gb.y)
     ctx.set_params(P, eps)
@@ -402,6 +403,7 @@ def run_disk_compact(G, presets, args):
     bounds = presets.BOUNDS["disk"]
     b = presets.disk(n, seed=args.seed + 3)
     ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=8, eps64=0.1))
+    ctx.set_near_split(args.theta_w)
     ctx.build_tree(b, n_max, bounds)
     eps = presets.cli_softening(b.x, b.y)
     ctx.upload_bodies(b)
@@ -420,7 +422,8 @@ def run_disk_compact(G, presets, args):
             row.update(_err_stats(r.ax[idx], r.ay[idx], ex, ey))
             rows.append(row)
     ctx.close()
-    return {"workload": f"disk N={n}, n_max={n_max}, theta={THETA}, ACCURATE", "eps": eps, "rows": rows}
+    return {"workload": f"disk N={n}, n_max={n_max}, theta={THETA}, theta_w={args.theta_w}, ACCURATE", "eps": eps,
+            "rows": rows}
 
 
 def run_build_only(args):
@@ -607,6 +610,7 @@ def run_ours(args, rank, world, local, pg):
     ctx.upload_bodies(gb)
     nn, nl, nlev, _ = ctx.tree_info()
 
+    ctx.set_near_split(args.theta_w)  # ACCURATE forms only; REF keeps the reference's lists
     forms = [("mixed", G.MODE_ACCURATE, G.PREC_MIXED), ("fp64", G.MODE_ACCURATE, G.PREC_FP64),
              ("ref_fp64", G.MODE_REF, G.PREC_FP64)]
     res = {}
@@ -687,6 +691,7 @@ def run_ours(args, rank, world, local, pg):
 
     adjoint = None
     if not args.no_adjoint and world == 1:
+        ctx.set_near_split(0.0)  # the adjoint transposes P2P, M2L, L2L and L2P, not M2P / P2L
         adjoint = run_adjoint(G, presets, ctx, gb, args)
     mix = res["mixed"]
     ms_step = _max_over_ranks(pg, float(np.mean(mix["ms"])))
@@ -737,7 +742,8 @@ def run_ours(args, rank, world, local, pg):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed: FP32 P2M/M2L/L2L/L2P/P2P, FP64 state)",
         "data": "synthetic (seeded Plummer preset: a=1, r<=10a, equal masses 1/N)",
         "config": {"workload": f"plummer N={n}, p={P}, n_max={N_MAX}, one force evaluation per step, static tree",
-                   "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "mode": "ACCURATE", "eps": eps,
+                   "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "theta_w": args.theta_w, "mode": "ACCURATE",
+                   "eps": eps,
                    "l2": "flushed (256 MB write) before every step, outside its timed interval",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "bodies/s", "h2d_bytes_per_step": 3 * 8 * n,

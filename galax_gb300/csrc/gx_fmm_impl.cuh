@@ -1380,6 +1380,194 @@ __global__ void __launch_bounds__(128) k_m2p(int64_t n_items, const int32_t *__r
     }
 }
 
+// Packed FP32 pairs (two bodies per lane) for the mixed-form M2P and P2L at p <= 5.
+struct f2v {
+    uint64_t v;
+};
+__device__ __forceinline__ f2v f2splat(float c) { return {pk2(c, c)}; }
+__device__ __forceinline__ f2v f2pair(float a, float b) { return {pk2(a, b)}; }
+__device__ __forceinline__ f2v f2mul(f2v a, f2v b) { return {mul2(a.v, b.v)}; }
+__device__ __forceinline__ f2v f2add(f2v a, f2v b) { return {add2(a.v, b.v)}; }
+__device__ __forceinline__ f2v f2sub(f2v a, f2v b) { return {sub2(a.v, b.v)}; }
+__device__ __forceinline__ f2v f2fma(f2v a, f2v b, f2v c) { return {fma2(a.v, b.v, c.v)}; }
+
+// taylor_1r on pairs: a_k for |k| <= N at two offsets at once
+template <int N>
+__device__ __forceinline__ void taylor_1r_x2(f2v dx, f2v dy, f2v ir, f2v ir2, f2v *a) {
+    a[0] = ir;
+#pragma unroll
+    for (int n = 1; n <= N; n++) {
+        const f2v in_ = f2mul(f2splat((float)(1.0 / n)), ir2);
+        const f2v c1 = f2mul(f2splat(-(float)(2 * n - 1)), in_);
+        const f2v c2 = f2mul(f2splat(-(float)(n - 1)), in_);
+        const f2v c1x = f2mul(c1, dx), c1y = f2mul(c1, dy);
+#pragma unroll
+        for (int k = 0; k <= n; k++) {
+            const int l = n - k;
+            f2v v;
+            if (k >= 1 && l >= 1) v = f2fma(c1x, a[gx_mi(k - 1, l)], f2mul(c1y, a[gx_mi(k, l - 1)]));
+            else if (k >= 1) v = f2mul(c1x, a[gx_mi(k - 1, l)]);
+            else v = f2mul(c1y, a[gx_mi(k, l - 1)]);
+            if (k >= 2) v = f2fma(c2, a[gx_mi(k - 2, l)], v);
+            if (l >= 2) v = f2fma(c2, a[gx_mi(k, l - 2)], v);
+            a[gx_mi(k, l)] = v;
+        }
+    }
+}
+
+__device__ __forceinline__ f2v rsqrt_x2(f2v r2) {
+    float a, b;
+    upk2(r2.v, a, b);
+    return f2pair(rsqrt_fast(a), rsqrt_fast(b));
+}
+
+// M2P items, mixed form, leaves of at most 32 bodies, p <= 5: lane tl of each half-warp
+// holds target bodies tl and tl + 16 as a pair, half h takes the item's sources
+// h, h + 2, ...; per source its lane stores the moments signed and scaled by (S+e)!
+// (both components duplicated, ready as pair operands) and the COM offset in shared
+// memory.  The halves' sums are added in a fixed order (half 0's first), as in the
+// two-target P2P rows.
+template <int P>
+__global__ void __launch_bounds__(128) k_m2p_x2(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                const int64_t *__restrict__ item_qb,
+                                                const int32_t *__restrict__ item_nq, const float4 *__restrict__ pos,
+                                                const double *__restrict__ comx, const double *__restrict__ comy,
+                                                const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                                const int32_t *__restrict__ src_idx, float eps2,
+                                                const float *__restrict__ M, float2 *__restrict__ part) {
+    static_assert(P <= 5, "shared-memory moment rows are sized for p <= 5");
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<float>(NC);
+    __shared__ __align__(16) float4 smm[4][32][NC];  // (mx, mx, my, my) per moment
+    __shared__ __align__(8) float2 shf[4][32];        // com_a - com_s
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int half = lane >> 4, tl = lane & 15;
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const f2v E2 = f2splat(eps2);
+    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
+        const int nq0 = item_nq[it];
+        if (nq0 >= 0) continue;
+        const int nq = -nq0;
+        const int32_t leaf = item_leaf[it];
+        __syncwarp();  // the previous item's reads of the shared arrays are done
+        if (lane < nq) {
+            const int32_t sl = src_idx[item_qb[it] + lane];
+            shf[w][lane] = make_float2((float)(comx[leaf] - comx[sl]), (float)(comy[leaf] - comy[sl]));
+            float ms[NC];
+            load_row<NC>(M + (int64_t)sl * NS, ms);
+#pragma unroll
+            for (int si = 0; si <= P; si++)
+#pragma unroll
+                for (int sj = 0; sj <= P - si; sj++) {
+                    const float mv = ((si + sj) & 1) ? -ms[gx_mi(si, sj)] : ms[gx_mi(si, sj)];
+                    const float mx = mv * tab_ff<float>(si + 1, sj), my = mv * tab_ff<float>(si, sj + 1);
+                    smm[w][lane][gx_mi(si, sj)] = make_float4(mx, mx, my, my);
+                }
+        }
+        __syncwarp();
+        const int32_t t0 = bs[leaf], t1 = be[leaf];
+        const int32_t iA = t0 + tl, iB = t0 + tl + 16;
+        const float4 pA = iA < t1 ? pos[iA] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pB = iB < t1 ? pos[iB] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const f2v X = f2pair(pA.x, pB.x), Y = f2pair(pA.y, pB.y);
+        f2v FX = f2splat(0.f), FY = f2splat(0.f);
+        for (int k = half; k < nq; k += 2) {
+            const float2 o = shf[w][k];
+            const f2v dx = f2add(X, f2splat(o.x)), dy = f2add(Y, f2splat(o.y));
+            const f2v r2 = f2fma(dx, dx, f2fma(dy, dy, E2));
+            const f2v ir = rsqrt_x2(r2);
+            f2v a[nc2(P + 1)];
+            taylor_1r_x2<P + 1>(dx, dy, ir, f2mul(ir, ir), a);
+#pragma unroll
+            for (int si = 0; si <= P; si++)
+#pragma unroll
+                for (int sj = 0; sj <= P - si; sj++) {
+                    const float4 m4 = smm[w][k][gx_mi(si, sj)];
+                    FX = f2fma(f2pair(m4.x, m4.y), a[gx_mi(si + 1, sj)], FX);
+                    FY = f2fma(f2pair(m4.z, m4.w), a[gx_mi(si, sj + 1)], FY);
+                }
+        }
+        float xA, xB, yA, yB;
+        upk2(FX.v, xA, xB);
+        upk2(FY.v, yA, yB);
+        const float oxA = __shfl_xor_sync(0xffffffffu, xA, 16), oyA = __shfl_xor_sync(0xffffffffu, yA, 16);
+        const float oxB = __shfl_xor_sync(0xffffffffu, xB, 16), oyB = __shfl_xor_sync(0xffffffffu, yB, 16);
+        float2 res;
+        if (half == 0) res = make_float2(xA + oxA, yA + oyA);  // body tl
+        else res = make_float2(oxB + xB, oyB + yB);             // body tl + 16 (half 0's part first)
+        part[it * 32 + lane] = res;
+    }
+}
+
+// P2L units, mixed form, p <= 5: lane tl of each half-warp takes source bodies tl and
+// tl + 16 of a source leaf as a pair, half h the unit's sources h, h + 2, ...; the
+// coefficient sums stay pairs until the end (pair halves, then the warp, in a fixed
+// order).  Leaves above 32 bodies go through their further bodies 32 at a time.
+template <int P>
+__global__ void __launch_bounds__(128) k_p2l_x2(int64_t n_units, const int32_t *__restrict__ uleaf,
+                                                const int64_t *__restrict__ ustart, const int32_t *__restrict__ ulen,
+                                                const int64_t *__restrict__ leaf_u,
+                                                const int32_t *__restrict__ src_idx, const float4 *__restrict__ pos,
+                                                const double *__restrict__ comx, const double *__restrict__ comy,
+                                                const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                                float eps2, float *__restrict__ Lf, float *__restrict__ ppart) {
+    static_assert(P <= 5, "paired accumulators are sized for p <= 5");
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<float>(NC);
+    const int lane = threadIdx.x & 31;
+    const int half = lane >> 4, tl = lane & 15;
+    const int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (u >= n_units) return;
+    const int32_t a = uleaf[u];
+    const int nq = ulen[u];
+    int32_t sb = 0, se = 0;
+    float shx = 0.f, shy = 0.f;
+    if (lane < nq) {
+        const int32_t sl = src_idx[ustart[u] + lane];
+        sb = bs[sl];
+        se = be[sl];
+        shx = (float)(comx[a] - comx[sl]);
+        shy = (float)(comy[a] - comy[sl]);
+    }
+    const f2v E2 = f2splat(eps2);
+    f2v acc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; k++) acc[k] = f2splat(0.f);
+    const int rounds = (nq + 1) >> 1;  // both halves run the same number of rounds
+    for (int r = 0; r < rounds; r++) {
+        const int k = 2 * r + half;
+        const int kk = k < nq ? k : 0;
+        const int32_t j0 = __shfl_sync(0xffffffffu, sb, kk), e1 = __shfl_sync(0xffffffffu, se, kk);
+        const int32_t j1 = k < nq ? e1 : j0;  // the half without a source this round runs no body
+        const float ox = __shfl_sync(0xffffffffu, shx, kk), oy = __shfl_sync(0xffffffffu, shy, kk);
+        for (int32_t c0 = j0; c0 < j1; c0 += 32) {
+            const int32_t jA = c0 + tl, jB = c0 + tl + 16;
+            const float4 pA = jA < j1 ? pos[jA] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 pB = jB < j1 ? pos[jB] : make_float4(0.f, 0.f, 0.f, 0.f);
+            // com_a - x_j = (com_a - com_s) - (x_j - com_s); an empty slot has m = 0 and
+            // sits at com_s, at the leaf pair's nonzero distance
+            const f2v dx = f2sub(f2splat(ox), f2pair(pA.x, pB.x)), dy = f2sub(f2splat(oy), f2pair(pA.y, pB.y));
+            const f2v ir = rsqrt_x2(f2fma(dx, dx, f2fma(dy, dy, E2)));
+            f2v c[NC];
+            taylor_1r_x2<P>(dx, dy, ir, f2mul(ir, ir), c);
+            const f2v mm = f2pair(pA.z, pB.z);
+#pragma unroll
+            for (int q = 0; q < NC; q++) acc[q] = f2fma(mm, c[q], acc[q]);
+        }
+    }
+    const bool single = leaf_u[a + 1] - leaf_u[a] == 1;
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        float lo, hi;
+        upk2(acc[q].v, lo, hi);
+        const float v = warp_sum_t<float>(lo + hi);
+        if (lane == (q & 31)) {
+            if (single) Lf[(int64_t)a * NS + q] -= v;
+            else ppart[u * NS + q] = v;
+        }
+    }
+}
+
 // P2L units: one warp per unit (a target leaf and at most GX_P2L_UNIT of its P2L source
 // leaves), lane per source body.  L_a[T] += m_j G^(T)(com_a - x_j) / T! = -m_j a_T(com_a - x_j),
 // summed per lane in body order, then over the warp; a leaf with one unit subtracts the
@@ -1802,8 +1990,18 @@ int run_forces(gx_ctx *ctx, bool timed) {
                                                             tchunks, dptr<double2>(ctx->part));
             ctx->launches++;
         }
+        if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[15], ctx->stream2));  // the P2P kernel alone
         if (split && ctx->n_m2p_pairs > 0) {
             // M2P items of the near-list split: their own slots of the same partial array
+            if constexpr (P <= 5) {
+                if (mixed && tchunks == 1) {
+                    k_m2p_x2<P><<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                              dptr<int32_t>(I.nq), pos, comx, comy, bs, be, src_idx,
+                                                              (float)eps2, reinterpret_cast<const float *>(M),
+                                                              dptr<float2>(ctx->part));
+                    goto m2p_done;
+                }
+            }
             if (mixed)
                 k_m2p<P, float, float2><<<gi, 128, 0, ctx->stream2>>>(
                     I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), pos, nullptr, nullptr, comx,
@@ -1813,9 +2011,9 @@ int run_forces(gx_ctx *ctx, bool timed) {
                 k_m2p<P, double, double2><<<gi, 128, 0, ctx->stream2>>>(
                     I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), nullptr, X, Y, comx, comy, bs,
                     be, src_idx, eps2, reinterpret_cast<const double *>(M), tchunks, dptr<double2>(ctx->part));
+        m2p_done:
             ctx->launches++;
         }
-        if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[15], ctx->stream2));
         if (I.n > GX_FOLD_MIN) {
             const unsigned gf = (unsigned)(((I.n + GX_FOLD - 1) / GX_FOLD * 32 + 127) / 128);
             if (mixed)
@@ -1897,9 +2095,18 @@ int run_forces(gx_ctx *ctx, bool timed) {
             const gx_ctx::P2LUnits &PU = ctx->p2l_units;
             GX_TRY(gx_ensure(ctx, ctx->p2l_part, sizeof(T) * NS * (size_t)(PU.n + 1)));
             const int64_t *leaf_u = dptr<int64_t>(PU.leaf_u);
-            k_p2l<P, T><<<(unsigned)((PU.n * 32 + 127) / 128), 128, 0, st>>>(
-                PU.n, dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start), dptr<int32_t>(PU.len), leaf_u, src_idx, pos, X, Y,
-                Mb, comx, comy, bs, be, (T)eps2, Lf, dptr<T>(ctx->p2l_part));
+            const unsigned gu = (unsigned)((PU.n * 32 + 127) / 128);
+            bool packed = false;
+            if constexpr (P <= 5 && sizeof(T) == 4) {
+                k_p2l_x2<P><<<gu, 128, 0, st>>>(PU.n, dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
+                                                dptr<int32_t>(PU.len), leaf_u, src_idx, pos, comx, comy, bs, be,
+                                                (float)eps2, Lf, dptr<float>(ctx->p2l_part));
+                packed = true;
+            }
+            if (!packed)
+                k_p2l<P, T><<<gu, 128, 0, st>>>(PU.n, dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
+                                                dptr<int32_t>(PU.len), leaf_u, src_idx, pos, X, Y, Mb, comx, comy, bs,
+                                                be, (T)eps2, Lf, dptr<T>(ctx->p2l_part));
             k_p2l_combine<P, T><<<gx_blocks(nl * NC, 256), 256, 0, st>>>(nl, leaf_u, dptr<T>(ctx->p2l_part), Lf);
             ctx->launches += 2;
         }
