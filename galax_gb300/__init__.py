@@ -85,6 +85,7 @@ def lib():
         "gx_build_tree": (C.c_int, [_VP, C.c_int64, _D, _D, _D, _D, _D, _D, _D, C.c_int64, _D, C.c_int]),
         "gx_rebuild_resident": (C.c_int, [_VP, C.c_int64, _D, C.c_int, _I64]),
         "gx_tree_info": (C.c_int, [_VP, _I64, _I64, _I32, _I64]),
+        "gx_morton_encode": (C.c_int, [_VP, C.c_int64, _D, _D, _D, C.POINTER(C.c_uint64)]),
         "gx_export_tree": (C.c_int, [_VP, _D, _D, _D, _D, _D, _D, _I64, _I64, _I32, _I32, _U8, _I64]),
         "gx_export_lists": (C.c_int, [_VP, C.c_int, _U32, _U8]),
         "gx_plan_info": (C.c_int, [_VP, _I64, _I64, _I64]),
@@ -338,6 +339,16 @@ class GpuContext:
         self._check(lib().gx_rebuild_resident(self._h, int(n_max), _p(b), BUILD_BALANCED if balanced else 0,
                                               _p(perm, _I64) if perm is not None else None))
         return perm
+
+    def morton_encode(self, x, y, bounds) -> np.ndarray:
+        """morton_encode (galax-core/src/lib.rs:95-109) of many bodies on the device."""
+        x = np.ascontiguousarray(np.asarray(x, np.float64))
+        y = np.ascontiguousarray(np.asarray(y, np.float64))
+        b = np.ascontiguousarray(np.asarray(bounds, np.float64))
+        keys = np.zeros(x.size, np.uint64)
+        self._check(lib().gx_morton_encode(self._h, x.size, _p(x), _p(y), _p(b),
+                                           keys.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return keys
 
     def tree_info(self):
         nn, nl, nb = C.c_int64(), C.c_int64(), C.c_int64()

@@ -489,6 +489,23 @@ int gx_body_ids(gx_ctx *ctx, int64_t *ids) {
     return GX_OK;
 }
 
+int gx_morton_encode(gx_ctx *ctx, int64_t n, const double *x, const double *y, const double bounds[4],
+                     uint64_t *keys) {
+    GX_TRY(check_ctx(ctx));
+    if (n < 0 || (n > 0 && (!x || !y || !keys)) || !bounds) return gx_fail(ctx, GX_ERR_INVALID_ARG, "bad arguments");
+    if (n == 0) return GX_OK;
+    GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(double) * 2 * (size_t)n));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(uint64_t) * (size_t)n));
+    double *dx = dptr<double>(ctx->scratch_a), *dy = dx + n;
+    GX_CUDA(ctx, cudaMemcpyAsync(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    GX_CUDA(ctx, cudaMemcpyAsync(dy, y, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    gx_launch_morton(ctx, dx, dy, n, bounds, dptr<uint64_t>(ctx->scratch_b), nullptr);
+    GX_CUDA(ctx, cudaGetLastError());
+    GX_CUDA(ctx, cudaMemcpyAsync(keys, ctx->scratch_b.p, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GX_OK;
+}
+
 int gx_tree_info(gx_ctx *ctx, int64_t *n_nodes, int64_t *n_leaves, int32_t *n_levels, int64_t *n_bodies) {
     GX_TRY(check_ctx(ctx));
     if (!ctx->have_tree) return gx_fail(ctx, GX_ERR_STATE, "no tree");

@@ -214,6 +214,9 @@ struct gx_ctx {
 // ---------------------------------------------------------------- sub-modules
 // gx_tree.cu
 int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bounds[4], int flags);
+// Morton keys of n bodies (device arrays) on the context stream; idx (optional) gets 0..n-1
+void gx_launch_morton(gx_ctx *ctx, const double *x, const double *y, int64_t n, const double bounds[4], uint64_t *keys,
+                      uint32_t *idx);
 // gx_lists.cu
 int gx_lists_build_ref(gx_ctx *ctx);
 int gx_plan_ref(gx_ctx *ctx);

@@ -15,12 +15,34 @@ namespace {
 constexpr double kOneMinus = 1.0 - 1e-15;  // clamp bound of normalize (lib.rs:76)
 
 // normalize (lib.rs:75-78): NaN clamps to NaN and casts to 0, like Rust `as u64`.
-__device__ __forceinline__ uint64_t normalize_dev(double x, double lo, double hi) {
+__device__ __forceinline__ uint64_t normalize_ref(double x, double lo, double hi) {
     double t = __ddiv_rn(__dsub_rn(x, lo), __dsub_rn(hi, lo));
     if (t < 0.0) t = 0.0;
     if (t > kOneMinus) t = kOneMinus;
     if (!(t > 0.0)) return 0ull;
     return __double2ull_rz(__dmul_rn(t, 2097152.0));
+}
+
+// The same cell index without the division.  The key uses t = RN(a / w), a = x - lo,
+// w = hi - lo, only through floor(t * 2^21) clamped to [0, 2^21 - 1] (the clamp at
+// 1 - 1e-15 and the clamp at 0 land in the end cells; NaN gives 0).  With
+// iw = RN(1/w) (w > 0 finite, iw normal, formed once on the host) and |a/w| < 2,
+// q = RN(a * iw) is within 1.5 * 2^-52 of a/w and RN(a/w) within 0.5 * 2^-52, so the two
+// differ by at most 2^-51; times 2^21 (exact) that is 2^-30.  Hence when s = q * 2^21 lies
+// farther than 2^-29 from an integer, floor(s) = floor(RN(a/w) * 2^21) exactly; values
+// that near a cell boundary, and non-finite ones, take the correctly rounded division.
+// One multiply instead of a correctly rounded FP64 division per coordinate.
+__device__ __forceinline__ uint64_t normalize_dev(double x, double lo, double hi, double iw) {
+    if (iw > 0.0) {
+        const double s = __dmul_rn(__dmul_rn(__dsub_rn(x, lo), iw), 2097152.0);
+        if (s < 2097152.0 * 2.0 && s > -1.0) {      // finite and |t| < 2: the window of the bound
+            if (s <= 0.0) return 0ull;               // a <= 0 or RN(a/w) < 2^-21: the low cell
+            if (s >= 2097151.5) return 2097151ull;   // RN(a/w) 2^21 >= 2097151.49: the top cell
+            const double f = floor(s), fr = __dsub_rn(s, f);
+            if (fr > 0x1p-29 && fr < 1.0 - 0x1p-29) return (uint64_t)f;
+        }
+    }
+    return normalize_ref(x, lo, hi);
 }
 
 // spread_bits (lib.rs:85-93)
@@ -35,12 +57,34 @@ __device__ __forceinline__ uint64_t spread_dev(uint64_t v) {
 }
 
 __global__ void k_morton(const double *__restrict__ x, const double *__restrict__ y, int64_t n, double x0, double x1,
-                         double y0, double y1, uint64_t *__restrict__ keys, uint32_t *__restrict__ idx) {
+                         double y0, double y1, double ixw, double iyw, uint64_t *__restrict__ keys,
+                         uint32_t *__restrict__ idx) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    keys[i] = spread_dev(normalize_dev(x[i], x0, x1)) | (spread_dev(normalize_dev(y[i], y0, y1)) << 1);
-    idx[i] = (uint32_t)i;
+    keys[i] = spread_dev(normalize_dev(x[i], x0, x1, ixw)) | (spread_dev(normalize_dev(y[i], y0, y1, iyw)) << 1);
+    if (idx) idx[i] = (uint32_t)i;
 }
+
+}  // namespace
+
+// RN(1 / (hi - lo)) for the division-free normalisation, or 0 (the division path) when the
+// width is not a positive finite number whose reciprocal is a normal number
+double gx_inv_width(double lo, double hi) {
+    const double w = hi - lo;
+    if (!(w > 0.0) || !std::isfinite(w)) return 0.0;
+    const double iw = 1.0 / w;
+    return (std::isfinite(iw) && std::fpclassify(iw) == FP_NORMAL) ? iw : 0.0;
+}
+
+void gx_launch_morton(gx_ctx *ctx, const double *x, const double *y, int64_t n, const double bounds[4], uint64_t *keys,
+                      uint32_t *idx) {
+    k_morton<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(x, y, n, bounds[0], bounds[1], bounds[2], bounds[3],
+                                                         gx_inv_width(bounds[0], bounds[1]),
+                                                         gx_inv_width(bounds[2], bounds[3]), keys, idx);
+    ctx->launches++;
+}
+
+namespace {
 
 // gather of the seven body arrays (Tree::permute, lib.rs:146-161)
 __global__ void k_permute(const uint32_t *__restrict__ idx, int64_t n, const double *__restrict__ in,
@@ -484,9 +528,7 @@ int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bou
     GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(uint32_t) * n * 2));           // idx, idx alt
     uint64_t *keys = dptr<uint64_t>(ctx->keys), *keys_alt = dptr<uint64_t>(ctx->scratch_b);
     uint32_t *idx = dptr<uint32_t>(ctx->scratch_c), *idx_alt = idx + n;
-    k_morton<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(dptr<double>(ctx->x), dptr<double>(ctx->y), n, bounds[0],
-                                                         bounds[1], bounds[2], bounds[3], keys, idx);
-    ctx->launches++;
+    gx_launch_morton(ctx, dptr<double>(ctx->x), dptr<double>(ctx->y), n, bounds, keys, idx);
     GX_CUDA(ctx, cudaGetLastError());
     if (!(flags & GX_BUILD_BALANCED)) {
         bool alt = false;
@@ -527,10 +569,8 @@ int gx_tree_rebuild_with_splits(gx_ctx *ctx, int64_t n_max, const double bounds[
     int64_t n = ctx->n_bodies;
     GX_TRY(gx_ensure(ctx, ctx->keys, sizeof(uint64_t) * n));
     GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(uint32_t) * n * 2));
-    k_morton<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(dptr<double>(ctx->x), dptr<double>(ctx->y), n, bounds[0],
-                                                         bounds[1], bounds[2], bounds[3], dptr<uint64_t>(ctx->keys),
-                                                         dptr<uint32_t>(ctx->scratch_c));
-    ctx->launches++;
+    gx_launch_morton(ctx, dptr<double>(ctx->x), dptr<double>(ctx->y), n, bounds, dptr<uint64_t>(ctx->keys),
+                     dptr<uint32_t>(ctx->scratch_c));
     std::vector<int32_t> hrs, hre;
     int64_t s = 0;
     size_t k = 0;

@@ -124,6 +124,10 @@ int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, doub
  * GX_BUILD_BALANCED runs build_constrained (lib.rs:541-694), which does not reorder. */
 int gx_rebuild_resident(gx_ctx *ctx, int64_t n_max, const double bounds[4], int flags, int64_t *perm);
 int gx_tree_info(gx_ctx *ctx, int64_t *n_nodes, int64_t *n_leaves, int32_t *n_levels, int64_t *n_bodies);
+/* morton_encode (galax-core/src/lib.rs:95-109) of n bodies at once on the device, bit-exact:
+ * host x, y in, host keys out; bounds = {x_min, x_max, y_min, y_max}. */
+int gx_morton_encode(gx_ctx *ctx, int64_t n, const double *x, const double *y, const double bounds[4],
+                     uint64_t *keys);
 /* Copies the current tree to host arrays (any pointer may be NULL); the Tree the
  * CLI keeps on the host.  level_start has n_levels+1 entries. */
 int gx_export_tree(gx_ctx *ctx, double *cx, double *cy, double *hw, double *mass, double *comx,

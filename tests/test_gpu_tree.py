@@ -178,3 +178,34 @@ def test_rebuild_after_steps_sorts_the_moved_bodies(G, oracle):
     c2.close()
     ctx.close()
     assert np.array_equal(out.ax, ref.ax) and np.array_equal(out.ay, ref.ay)
+
+
+def test_morton_keys_bit_exact_at_cell_boundaries(G, oracle):
+    """morton_encode (lib.rs:95-109) on the device without a division per coordinate: keys
+    equal the oracle's (IEEE division) for positions on, and one or two ulps either side
+    of, cell boundaries, the box edges, out-of-box values, signed zeros, huge and denormal
+    values, NaN and infinities, over three boxes, plus a million random bodies."""
+    rng = np.random.default_rng(77)
+    ctx = G.GpuContext(G.GpuConfig(max_n=1 << 21, max_nodes=1 << 20, p=4, eps64=0.1))
+    boxes = [(-50.0, 50.0, -50.0, 50.0), (0.0, 100.0, 0.0, 100.0), (-0.3, 7.1, 1e-3, 1e-3 + 3.7)]
+    for lo_x, hi_x, lo_y, hi_y in boxes:
+        w = hi_x - lo_x
+        k = rng.integers(0, 1 << 21, 20000)
+        base = lo_x + (k / 2.0 ** 21) * w  # on (or one rounding from) a cell boundary
+        xs = [base, np.nextafter(base, np.inf), np.nextafter(base, -np.inf),
+              np.nextafter(np.nextafter(base, np.inf), np.inf), np.nextafter(np.nextafter(base, -np.inf), -np.inf)]
+        special = np.array([lo_x, hi_x, np.nextafter(lo_x, -np.inf), np.nextafter(hi_x, np.inf),
+                            np.nextafter(hi_x, -np.inf), lo_x - 1e-300, 0.0, -0.0, 1e308, -1e308, np.nan, np.inf,
+                            -np.inf, lo_x + w * (1 - 1e-15), lo_x + w * (1 - 2.0 ** -21), lo_x + w * 2.0 ** -21,
+                            5e-324, -5e-324])
+        x = np.concatenate(xs + [special, rng.uniform(lo_x - 0.1 * w, hi_x + 0.1 * w, 100000)])
+        y = np.concatenate([rng.uniform(lo_y, hi_y, x.size - special.size), special])
+        y = y[rng.permutation(y.size)]
+        got = ctx.morton_encode(x, y, (lo_x, hi_x, lo_y, hi_y))
+        want = oracle.morton_encode_many(x, y, (lo_x, hi_x, lo_y, hi_y))
+        bad = np.nonzero(got != want)[0]
+        assert bad.size == 0, (lo_x, hi_x, bad[:5], x[bad[:5]], y[bad[:5]])
+    x = rng.uniform(-60, 60, 1_000_000)
+    y = rng.standard_normal(1_000_000) * 20
+    assert np.array_equal(ctx.morton_encode(x, y, boxes[0]), oracle.morton_encode_many(x, y, boxes[0]))
+    ctx.close()
