@@ -441,6 +441,7 @@ def run_build_only(args):
     ctx.build_tree(b.copy(), N_MAX, presets.BOUNDS["plummer"])
     ctx.set_params(P, presets.cli_softening(b.x, b.y))
     ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
+    ctx.set_near_split(args.theta_w)
     times, plan = [], []
     for _ in range(max(1, args.steps)):
         ctx.upload_bodies(b)  # unsorted order again: the sort does full work
@@ -463,7 +464,7 @@ def run_build_only(args):
     ref_plan = (t1 - t0) - (t2 - t1)
     nn, nl, lv, _ = ctx.tree_info()
     ctx.close()
-    print(json.dumps({"build_only": True, "n": n, "nodes": nn, "leaves": nl, "levels": lv,
+    print(json.dumps({"build_only": True, "n": n, "theta_w": args.theta_w, "nodes": nn, "leaves": nl, "levels": lv,
                       "build_ms": [t * 1e3 for t in times], "plan_ms": [t * 1e3 for t in plan],
                       "ref_plan_ms": ref_plan * 1e3, "ref_eval_ms": (t2 - t1) * 1e3}), flush=True)
     return 0

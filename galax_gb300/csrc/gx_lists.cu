@@ -583,27 +583,31 @@ __global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const
 // Leaves below single-child chain levels 1 .. L: by the only-child rule every level
 // under L keeps all of its parent's near entries (each mapped to its only child) and has
 // no far entries, so a leaf's near list is its level-L ancestor's (node x + up) shifted
-// down by up.  The level-L lists are the last block written; the leaf lists go after it.
-// One warp per leaf.
-__global__ void k_chain_leaf_lists(int64_t nl, int64_t up, int64_t *nstart, int32_t *ncnt, int32_t *near_idx,
-                                   int64_t near_cap, int64_t *ctr) {
+// down by up.  The level-L lists are the last block written, [NEAR - NEAR_LAST, NEAR);
+// the leaf lists are that block copied after it, entry for entry (a flat copy: a warp per
+// leaf left the ~6000-entry list of the widest halo leaf to one warp's dependent rounds),
+// then each leaf takes its ancestor's offset within the block.
+__global__ void k_chain_copy(int64_t up, int32_t *near_idx, int64_t near_cap, int64_t *ctr) {
     if (ctr[PC_OVF]) return;
-    const int lane = threadIdx.x & 31;
-    const int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (x >= nl) return;
-    const int64_t a = x + up;
-    const int64_t block = ctr[PC_NEAR] - ctr[PC_NEAR_LAST];  // first entry of level L's lists
-    const int64_t src = nstart[a], cnt = ncnt[a];
-    const int64_t dst = ctr[PC_NEAR] + (src - block);
-    if (dst + cnt > near_cap) {
-        if (lane == 0) atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF), (unsigned long long)OVF_NEAR);
+    const int64_t n = ctr[PC_NEAR_LAST], dst = ctr[PC_NEAR], src = dst - n;
+    if (dst + n > near_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF), (unsigned long long)OVF_NEAR);
         return;
     }
-    for (int64_t q = lane; q < cnt; q += 32) near_idx[dst + q] = (int32_t)(near_idx[src + q] - up);
-    if (lane == 0) {
-        nstart[x] = dst;
-        ncnt[x] = (int32_t)cnt;
-    }
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        near_idx[dst + i] = (int32_t)(near_idx[src + i] - up);
+}
+
+__global__ void k_chain_leaf_offsets(int64_t nl, int64_t up, int64_t near_cap, int64_t *nstart, int32_t *ncnt,
+                                     const int64_t *ctr) {
+    const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nl) return;
+    const int64_t n = ctr[PC_NEAR_LAST], dst = ctr[PC_NEAR];
+    if (ctr[PC_OVF] || dst + n > near_cap) return;
+    nstart[x] = dst + (nstart[x + up] - (dst - n));
+    ncnt[x] = ncnt[x + up];
 }
 
 // The chain shortcut needs node x + l nl (levels 1 .. L) to have the single child
@@ -1240,10 +1244,11 @@ int gx_plan_accurate(gx_ctx *ctx) {
         }
         if (lv_low >= 2) {
             const int64_t up = ctx->level_start[lv_low];
-            k_chain_leaf_lists<<<(unsigned)((nl0 * 32 + 127) / 128), 128, 0, ctx->stream>>>(
-                nl0, up, nstart, ncnt, dptr<int32_t>(ctx->near_idx), near_cap, ctr);
+            const unsigned gcopy = (unsigned)(ctx->sm_count > 0 ? ctx->sm_count * 8 : 1216);
+            k_chain_copy<<<gcopy, 256, 0, ctx->stream>>>(up, dptr<int32_t>(ctx->near_idx), near_cap, ctr);
+            k_chain_leaf_offsets<<<gx_blocks(nl0, 256), 256, 0, ctx->stream>>>(nl0, up, near_cap, nstart, ncnt, ctr);
             k_chain_leaf_close<<<1, 1, 0, ctx->stream>>>(ctr);
-            ctx->launches += 2;
+            ctx->launches += 3;
             GX_CUDA(ctx, cudaGetLastError());
         }
         GX_CUDA(ctx, cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1290,52 +1295,71 @@ __device__ __forceinline__ int near_kind(const float4 A, float Ra, const float4 
 // The leaf's list is copied to scratch (same offsets) and written back partitioned as
 // [P2P | M2P | P2L], each part in list order; the leaf's near count becomes its P2P
 // count, split_cnt[2a], [2a + 1] its M2P and P2L counts; tot gets the three totals.
-__global__ void __launch_bounds__(128) k_near_split(int64_t nl, const int64_t *__restrict__ nstart,
-                                                    int32_t *__restrict__ ncnt, int32_t *__restrict__ near_idx,
-                                                    int32_t *__restrict__ scratch, const float4 *__restrict__ hl,
-                                                    const float *__restrict__ R32, float tw, float tw2,
-                                                    int32_t *__restrict__ split_cnt,
-                                                    unsigned long long *__restrict__ tot) {
-    const int lane = threadIdx.x & 31;
-    const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// One block of NS_THREADS per leaf, each thread a contiguous chunk of the list, the
+// chunks' counts scanned across the block: the widest halo leaf's list (~6000 entries at
+// 1M Plummer) is spread over the block instead of one warp's sequential rounds.
+constexpr int NS_THREADS = 128;
+__global__ void __launch_bounds__(NS_THREADS) k_near_split(int64_t nl, const int64_t *__restrict__ nstart,
+                                                           int32_t *__restrict__ ncnt, int32_t *__restrict__ near_idx,
+                                                           int32_t *__restrict__ scratch,
+                                                           const float4 *__restrict__ hl,
+                                                           const float *__restrict__ R32, float tw, float tw2,
+                                                           int32_t *__restrict__ split_cnt,
+                                                           unsigned long long *__restrict__ tot) {
+    __shared__ int wsum[3][NS_THREADS / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int64_t a = blockIdx.x;
     if (a >= nl) return;
     const int64_t s0 = nstart[a];
     const int c = ncnt[a];
     const float4 A = hl[a];
     const float Ra = R32[a];
-    const unsigned lt = (1u << lane) - 1u;
-    int n1 = 0, n2 = 0;
-    for (int b = 0; b < c; b += 32) {
-        const int q = b + lane;
-        const bool v = q < c;
-        const int32_t src = v ? near_idx[s0 + q] : 0;
-        const int k = (v && src != (int32_t)a) ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
-        if (v) scratch[s0 + q] = src;
-        n1 += __popc(__ballot_sync(0xffffffffu, v && k == 1));
-        n2 += __popc(__ballot_sync(0xffffffffu, v && k == 2));
+    const int per = (c + NS_THREADS - 1) / NS_THREADS;
+    const int q0 = min(c, t * per), q1 = min(c, q0 + per);
+    int cnt[3] = {0, 0, 0};
+    for (int q = q0; q < q1; q++) {
+        const int32_t src = near_idx[s0 + q];
+        scratch[s0 + q] = src;
+        cnt[src != (int32_t)a ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0]++;
     }
-    __syncwarp();  // the copy is complete before it is read back
-    const int n0 = c - n1 - n2;
-    int o[3] = {0, n0, n0 + n1};
-    for (int b = 0; b < c; b += 32) {
-        const int q = b + lane;
-        const bool v = q < c;
-        const int32_t src = v ? scratch[s0 + q] : 0;
-        const int k = (v && src != (int32_t)a) ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
+    // exclusive scan of the three counts over the block, in thread (= list) order
+    int ex[3];
 #pragma unroll
-        for (int kk = 0; kk < 3; kk++) {
-            const unsigned m = __ballot_sync(0xffffffffu, v && k == kk);
-            if (v && k == kk) near_idx[s0 + o[kk] + __popc(m & lt)] = src;
-            o[kk] += __popc(m);
+    for (int k = 0; k < 3; k++) {
+        int v = cnt[k];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
         }
+        ex[k] = v - cnt[k];
+        if (lane == 31) wsum[k][w] = v;
     }
-    if (lane == 0) {
-        ncnt[a] = n0;
-        split_cnt[2 * a] = n1;
-        split_cnt[2 * a + 1] = n2;
-        atomicAdd(tot + 0, (unsigned long long)n0);
-        atomicAdd(tot + 1, (unsigned long long)n1);
-        atomicAdd(tot + 2, (unsigned long long)n2);
+    __syncthreads();  // also orders the scratch copy before its read-back below
+    int total[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        int before = 0, all = 0;
+        for (int ww = 0; ww < NS_THREADS / 32; ww++) {
+            if (ww < w) before += wsum[k][ww];
+            all += wsum[k][ww];
+        }
+        ex[k] += before;
+        total[k] = all;
+    }
+    int o[3] = {ex[0], total[0] + ex[1], total[0] + total[1] + ex[2]};
+    for (int q = q0; q < q1; q++) {
+        const int32_t src = scratch[s0 + q];
+        const int k = src != (int32_t)a ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
+        near_idx[s0 + o[k]++] = src;
+    }
+    if (t == 0) {
+        ncnt[a] = total[0];
+        split_cnt[2 * a] = total[1];
+        split_cnt[2 * a + 1] = total[2];
+        atomicAdd(tot + 0, (unsigned long long)total[0]);
+        atomicAdd(tot + 1, (unsigned long long)total[1]);
+        atomicAdd(tot + 2, (unsigned long long)total[2]);
     }
 }
 }  // namespace
@@ -1356,7 +1380,7 @@ int gx_plan_near_split(gx_ctx *ctx) {
         int64_t *nstart = dptr<int64_t>(ctx->near_off);
         int32_t *ncnt = reinterpret_cast<int32_t *>(nstart + nn);
         const float tw = (float)ctx->theta_w, tw2 = tw * tw;
-        k_near_split<<<(unsigned)((nl * 32 + 127) / 128), 128, 0, ctx->stream>>>(
+        k_near_split<<<(unsigned)nl, NS_THREADS, 0, ctx->stream>>>(
             nl, nstart, ncnt, dptr<int32_t>(ctx->near_idx), dptr<int32_t>(ctx->scratch_f), dptr<float4>(ctx->comhl),
             dptr<float>(ctx->radius32), tw, tw2, dptr<int32_t>(ctx->split_cnt),
             dptr<unsigned long long>(ctx->split_tot));
