@@ -191,7 +191,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->m2l_units.node, &ctx->m2l_units.start, &ctx->m2l_units.len, &ctx->m2l_units.node_u,
                       &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state, &ctx->m2l_cnt, &ctx->split_cnt,
                       &ctx->split_tot, &ctx->p2l_units.leaf, &ctx->p2l_units.start, &ctx->p2l_units.len,
-                      &ctx->p2l_units.leaf_u, &ctx->p2l_part};
+                      &ctx->p2l_units.leaf_u, &ctx->p2l_part, &ctx->m2p_list, &ctx->m2p_off};
     for (DevBuf *b : bufs) free_buf(*b);
     for (gx_tree_plan &t : ctx->tp_cache) gx_tree_plan_free(t);
     for (auto &e : ctx->ev)

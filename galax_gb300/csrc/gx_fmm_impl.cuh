@@ -1323,7 +1323,8 @@ __device__ __forceinline__ void m2p_eval(T dx, T dy, T eps2, const T *ms, T &fx,
 // the source's moment row is a broadcast load.  Writes the item's partial slot like a
 // P2P item, so the ordered sum of the leaf's items includes it.
 template <int P, class T, class V>
-__global__ void __launch_bounds__(128) k_m2p(int64_t n_items, const int32_t *__restrict__ item_leaf,
+__global__ void __launch_bounds__(128) k_m2p(int64_t n_list, const int32_t *__restrict__ list,
+                                             const int32_t *__restrict__ item_leaf,
                                              const int64_t *__restrict__ item_qb, const int32_t *__restrict__ item_nq,
                                              const float4 *__restrict__ pos, const double *__restrict__ X,
                                              const double *__restrict__ Y, const double *__restrict__ comx,
@@ -1336,7 +1337,8 @@ __global__ void __launch_bounds__(128) k_m2p(int64_t n_items, const int32_t *__r
     __shared__ int32_t shs[4][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
+    for (int64_t li = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < n_list; li += nwarps) {
+        const int64_t it = list[li];
         const int nq0 = item_nq[it];
         if (nq0 >= 0) continue;
         const int nq = -nq0;
@@ -1428,7 +1430,8 @@ __device__ __forceinline__ f2v rsqrt_x2(f2v r2) {
 // memory.  The halves' sums are added in a fixed order (half 0's first), as in the
 // two-target P2P rows.
 template <int P>
-__global__ void __launch_bounds__(128) k_m2p_x2(int64_t n_items, const int32_t *__restrict__ item_leaf,
+__global__ void __launch_bounds__(128, 8) k_m2p_x2(int64_t n_list, const int32_t *__restrict__ list,
+                                                const int32_t *__restrict__ item_leaf,
                                                 const int64_t *__restrict__ item_qb,
                                                 const int32_t *__restrict__ item_nq, const float4 *__restrict__ pos,
                                                 const double *__restrict__ comx, const double *__restrict__ comy,
@@ -1444,7 +1447,8 @@ __global__ void __launch_bounds__(128) k_m2p_x2(int64_t n_items, const int32_t *
     const int half = lane >> 4, tl = lane & 15;
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const f2v E2 = f2splat(eps2);
-    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
+    for (int64_t li = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < n_list; li += nwarps) {
+        const int64_t it = list[li];
         const int nq0 = item_nq[it];
         if (nq0 >= 0) continue;
         const int nq = -nq0;
@@ -1504,7 +1508,7 @@ __global__ void __launch_bounds__(128) k_m2p_x2(int64_t n_items, const int32_t *
 // coefficient sums stay pairs until the end (pair halves, then the warp, in a fixed
 // order).  Leaves above 32 bodies go through their further bodies 32 at a time.
 template <int P>
-__global__ void __launch_bounds__(128) k_p2l_x2(int64_t n_units, const int32_t *__restrict__ uleaf,
+__global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_t *__restrict__ uleaf,
                                                 const int64_t *__restrict__ ustart, const int32_t *__restrict__ ulen,
                                                 const int64_t *__restrict__ leaf_u,
                                                 const int32_t *__restrict__ src_idx, const float4 *__restrict__ pos,
@@ -1534,26 +1538,53 @@ __global__ void __launch_bounds__(128) k_p2l_x2(int64_t n_units, const int32_t *
 #pragma unroll
     for (int k = 0; k < NC; k++) acc[k] = f2splat(0.f);
     const int rounds = (nq + 1) >> 1;  // both halves run the same number of rounds
-    for (int r = 0; r < rounds; r++) {
+    // round r: this half's source k = 2r + half; its first 32 bodies are requested one
+    // round ahead (leaves above 32 bodies load the rest in place)
+    auto fetch = [&](int r, float4 &pA, float4 &pB, int32_t &j0, int32_t &j1, float &ox, float &oy) {
         const int k = 2 * r + half;
         const int kk = k < nq ? k : 0;
-        const int32_t j0 = __shfl_sync(0xffffffffu, sb, kk), e1 = __shfl_sync(0xffffffffu, se, kk);
-        const int32_t j1 = k < nq ? e1 : j0;  // the half without a source this round runs no body
-        const float ox = __shfl_sync(0xffffffffu, shx, kk), oy = __shfl_sync(0xffffffffu, shy, kk);
-        for (int32_t c0 = j0; c0 < j1; c0 += 32) {
-            const int32_t jA = c0 + tl, jB = c0 + tl + 16;
-            const float4 pA = jA < j1 ? pos[jA] : make_float4(0.f, 0.f, 0.f, 0.f);
-            const float4 pB = jB < j1 ? pos[jB] : make_float4(0.f, 0.f, 0.f, 0.f);
-            // com_a - x_j = (com_a - com_s) - (x_j - com_s); an empty slot has m = 0 and
-            // sits at com_s, at the leaf pair's nonzero distance
-            const f2v dx = f2sub(f2splat(ox), f2pair(pA.x, pB.x)), dy = f2sub(f2splat(oy), f2pair(pA.y, pB.y));
-            const f2v ir = rsqrt_x2(f2fma(dx, dx, f2fma(dy, dy, E2)));
-            f2v c[NC];
-            taylor_1r_x2<P>(dx, dy, ir, f2mul(ir, ir), c);
-            const f2v mm = f2pair(pA.z, pB.z);
+        j0 = __shfl_sync(0xffffffffu, sb, kk);
+        const int32_t e1 = __shfl_sync(0xffffffffu, se, kk);
+        j1 = k < nq ? e1 : j0;  // the half without a source this round runs no body
+        ox = __shfl_sync(0xffffffffu, shx, kk);
+        oy = __shfl_sync(0xffffffffu, shy, kk);
+        const int32_t jA = j0 + tl, jB = j0 + tl + 16;
+        pA = jA < j1 ? pos[jA] : make_float4(0.f, 0.f, 0.f, 0.f);
+        pB = jB < j1 ? pos[jB] : make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+    auto body_pair = [&](const float4 &pA, const float4 &pB, float ox, float oy) {
+        // com_a - x_j = (com_a - com_s) - (x_j - com_s); an empty slot has m = 0 and
+        // sits at com_s, at the leaf pair's nonzero distance
+        const f2v dx = f2sub(f2splat(ox), f2pair(pA.x, pB.x)), dy = f2sub(f2splat(oy), f2pair(pA.y, pB.y));
+        const f2v ir = rsqrt_x2(f2fma(dx, dx, f2fma(dy, dy, E2)));
+        f2v c[NC];
+        taylor_1r_x2<P>(dx, dy, ir, f2mul(ir, ir), c);
+        const f2v mm = f2pair(pA.z, pB.z);
 #pragma unroll
-            for (int q = 0; q < NC; q++) acc[q] = f2fma(mm, c[q], acc[q]);
+        for (int q = 0; q < NC; q++) acc[q] = f2fma(mm, c[q], acc[q]);
+    };
+    float4 cA = make_float4(0.f, 0.f, 0.f, 0.f), cB = cA;
+    int32_t c0 = 0, c1 = 0;
+    float cox = 0.f, coy = 0.f;
+    if (rounds > 0) fetch(0, cA, cB, c0, c1, cox, coy);
+    for (int r = 0; r < rounds; r++) {
+        float4 nA = make_float4(0.f, 0.f, 0.f, 0.f), nB = nA;
+        int32_t n0 = 0, n1 = 0;
+        float nox = 0.f, noy = 0.f;
+        if (r + 1 < rounds) fetch(r + 1, nA, nB, n0, n1, nox, noy);
+        if (c0 < c1) body_pair(cA, cB, cox, coy);
+        for (int32_t b0 = c0 + 32; b0 < c1; b0 += 32) {
+            const int32_t jA = b0 + tl, jB = b0 + tl + 16;
+            const float4 pA = jA < c1 ? pos[jA] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float4 pB = jB < c1 ? pos[jB] : make_float4(0.f, 0.f, 0.f, 0.f);
+            body_pair(pA, pB, cox, coy);
         }
+        cA = nA;
+        cB = nB;
+        c0 = n0;
+        c1 = n1;
+        cox = nox;
+        coy = noy;
     }
     const bool single = leaf_u[a + 1] - leaf_u[a] == 1;
 #pragma unroll
@@ -1991,11 +2022,13 @@ int run_forces(gx_ctx *ctx, bool timed) {
             ctx->launches++;
         }
         if (timed) GX_CUDA(ctx, cudaEventRecord(ctx->ev[15], ctx->stream2));  // the P2P kernel alone
-        if (split && ctx->n_m2p_pairs > 0) {
+        if (split && ctx->n_m2p_items > 0) {
+            const unsigned gm = (unsigned)((ctx->n_m2p_items * 32 + 127) / 128);  // warp per M2P item
             // M2P items of the near-list split: their own slots of the same partial array
             if constexpr (P <= 5) {
                 if (mixed && tchunks == 1) {
-                    k_m2p_x2<P><<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                    k_m2p_x2<P><<<gm, 128, 0, ctx->stream2>>>(ctx->n_m2p_items, dptr<int32_t>(ctx->m2p_list),
+                                                              dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
                                                               dptr<int32_t>(I.nq), pos, comx, comy, bs, be, src_idx,
                                                               (float)eps2, reinterpret_cast<const float *>(M),
                                                               dptr<float2>(ctx->part));
@@ -2003,13 +2036,13 @@ int run_forces(gx_ctx *ctx, bool timed) {
                 }
             }
             if (mixed)
-                k_m2p<P, float, float2><<<gi, 128, 0, ctx->stream2>>>(
-                    I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), pos, nullptr, nullptr, comx,
+                k_m2p<P, float, float2><<<gm, 128, 0, ctx->stream2>>>(
+                    ctx->n_m2p_items, dptr<int32_t>(ctx->m2p_list), dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), pos, nullptr, nullptr, comx,
                     comy, bs, be, src_idx, (float)eps2, reinterpret_cast<const float *>(M), tchunks,
                     dptr<float2>(ctx->part));
             else
-                k_m2p<P, double, double2><<<gi, 128, 0, ctx->stream2>>>(
-                    I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), nullptr, X, Y, comx, comy, bs,
+                k_m2p<P, double, double2><<<gm, 128, 0, ctx->stream2>>>(
+                    ctx->n_m2p_items, dptr<int32_t>(ctx->m2p_list), dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), nullptr, X, Y, comx, comy, bs,
                     be, src_idx, eps2, reinterpret_cast<const double *>(M), tchunks, dptr<double2>(ctx->part));
         m2p_done:
             ctx->launches++;

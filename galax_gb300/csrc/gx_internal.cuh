@@ -152,6 +152,8 @@ struct gx_ctx {
     DevBuf split_cnt;      // int32 [2 * n_leaves]
     DevBuf split_tot;      // int64 [4]: P2P, M2P, P2L pairs (device totals of the split)
     int64_t n_m2p_pairs = 0, n_p2l_pairs = 0, n_m2p_items = 0;
+    DevBuf m2p_list;  // int32: the item indices of the M2P items, leaf by leaf
+    DevBuf m2p_off;   // int64 [n_leaves + 1]: each leaf's first entry in m2p_list
     struct P2LUnits {
         DevBuf leaf, start, len, leaf_u;  // int32, int64, int32, int64[n_leaves+1]
         int64_t n = 0;

@@ -1426,8 +1426,16 @@ __global__ void k_items_count(int64_t nl, const int64_t *start, const int32_t *c
     nitems[a] = (c + P2P_K - 1) / P2P_K + (cm + P2P_K - 1) / P2P_K;
 }
 
+// per leaf: number of M2P items (the compact list the M2P kernel runs over)
+__global__ void k_m2p_items_count(int64_t nl, const int32_t *split, int64_t *n) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a > nl) return;
+    n[a] = a == nl ? 0 : (split[2 * a] + P2P_K - 1) / P2P_K;
+}
+
 __global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split,
-                             const int64_t *off, int32_t *leaf, int64_t *qb, int32_t *nq) {
+                             const int64_t *off, int32_t *leaf, int64_t *qb, int32_t *nq, const int64_t *m2p_off,
+                             int32_t *m2p_list) {
     int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nl) return;
     int64_t s0 = start[a];
@@ -1443,6 +1451,7 @@ __global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cn
         leaf[it] = (int32_t)a;
         qb[it] = s0 + c + k * P2P_K;
         nq[it] = -(int32_t)min((int64_t)P2P_K, cm - k * P2P_K);
+        m2p_list[m2p_off[a] + k] = (int32_t)it;
     }
 }
 
@@ -1569,10 +1578,18 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     int64_t *nit = dptr<int64_t>(ctx->scratch_c);
     k_items_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, nit);
     GX_TRY(gx_exclusive_scan_i64(ctx, nit, dptr<int64_t>(I.off), nl + 1));
-    int64_t tot[3] = {0, 0, 0};
+    int64_t tot[4] = {0, 0, 0, 0};
     unsigned long long stot[4] = {0, 0, 0, 0};
     gx_ctx::P2LUnits &PU = ctx->p2l_units;
     if (split) {
+        GX_TRY(gx_ensure(ctx, ctx->m2p_off, sizeof(int64_t) * (size_t)(nl + 1)));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_e, sizeof(int64_t) * (size_t)(nl + 1)));  // free after the plan
+        int64_t *nm = dptr<int64_t>(ctx->scratch_e);
+        k_m2p_items_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, scnt, nm);
+        GX_TRY(gx_exclusive_scan_i64(ctx, nm, dptr<int64_t>(ctx->m2p_off), nl + 1));
+        GX_CUDA(ctx, cudaMemcpyAsync(&tot[3], dptr<int64_t>(ctx->m2p_off) + nl, sizeof(int64_t),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->launches++;
         GX_TRY(gx_ensure(ctx, PU.leaf_u, sizeof(int64_t) * (size_t)(nl + 1)));
         GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int64_t) * (size_t)(nl + 1)));
         int64_t *npu = dptr<int64_t>(ctx->scratch_b);
@@ -1604,11 +1621,13 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     GX_TRY(gx_ensure(ctx, I.leaf, sizeof(int32_t) * (size_t)(tot[0] + 1)));
     GX_TRY(gx_ensure(ctx, I.qb, sizeof(int64_t) * (size_t)(tot[0] + 1)));
     GX_TRY(gx_ensure(ctx, I.nq, sizeof(int32_t) * (size_t)(tot[0] + 1)));
-    k_items_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, dptr<int64_t>(I.off),
-                                                              dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
-                                                              dptr<int32_t>(I.nq));
+    if (split) GX_TRY(gx_ensure(ctx, ctx->m2p_list, sizeof(int32_t) * (size_t)(tot[3] + 1)));
+    k_items_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(
+        nl, start, cnt, scnt, dptr<int64_t>(I.off), dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
+        split ? dptr<int64_t>(ctx->m2p_off) : nullptr, split ? dptr<int32_t>(ctx->m2p_list) : nullptr);
     ctx->launches += 2;
     I.n = tot[0];
+    ctx->n_m2p_items = split ? tot[3] : 0;
     PU.n = 0;
     ctx->n_m2p_pairs = ctx->n_p2l_pairs = 0;
     if (split) {
