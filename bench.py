@@ -551,8 +551,9 @@ def run_sweep_theta(args):
 
 
 def run_sweep_thetaw(args):
-    """Near-list split sweep on the Plummer workload (N = 1,000,000, p = 4, n_max = 32,
-    theta = 0.5): for each theta_w (0 = no split) the P2P, M2P and P2L pair counts, the
+    """Near-list split sweep on the Plummer workload (N = 1,000,000, p = 4, n_max = 32):
+    at theta = 0.5 for each theta_w (0 = no split), and at the --sweep-thetas opening angles
+    for theta_w in {0.3, 0.35, 0.4}, the P2P, M2P and P2L pair counts, the
     evaluation time of the mixed and FP64 forms, the P2P kernel alone, and the errors
     against the FP64 N^2 sum on 1000 seeded samples.  Prints one JSON line."""
     import galax_gb300 as G
@@ -568,17 +569,23 @@ def run_sweep_thetaw(args):
     idx = np.sort(np.random.default_rng(1234).choice(n, min(1000, n), replace=False))
     ex, ey = ctx.n2_sampled(idx)
     rows = []
-    for tw in (0.0, 0.3, 0.35, 0.4, 0.45, 0.5):
+    grid = [(THETA, tw) for tw in (0.0, 0.3, 0.35, 0.4, 0.45, 0.5)]
+    grid += [(th, tw) for th in args.sweep_thetas for tw in (0.3, 0.35, 0.4) if th != THETA]
+    for theta, tw in grid:
         ctx.set_near_split(tw)
-        for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
-            ctx.set_mode(G.MODE_ACCURATE, prec, THETA)
+        # the FP64 form has the mixed form's error (to the third digit); it is timed at the
+        # headline opening angle only
+        forms = (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)) if theta == THETA else (("mixed", G.PREC_MIXED),)
+        for name, prec in forms:
+            ctx.set_mode(G.MODE_ACCURATE, prec, theta)
             ctx.forces_resident()
             ms, kms = ctx.bench_forces(10 if name == "mixed" else 1, True, 0)
             r = G.Bodies.new(n)
             ctx.download_bodies(r)
             far, near, inter = ctx.plan_info()
             m2p, p2l = ctx.plan_split_info()
-            row = {"theta_w": tw, "form": name, "ms": float(np.mean(ms)), "p2p_kernel_ms": float(np.mean(kms)),
+            row = {"theta": theta, "theta_w": tw, "form": name, "ms": float(np.mean(ms)),
+                   "p2p_kernel_ms": float(np.mean(kms)),
                    "pass_ms": ctx.last_timings().tolist(), "bodies_per_s": n / (float(np.mean(ms)) * 1e-3),
                    "far_pairs": far, "near_p2p_leaf_pairs": near, "m2p_leaf_pairs": m2p, "p2l_leaf_pairs": p2l,
                    "p2p_interactions": inter}
@@ -806,6 +813,7 @@ def main():
     ap.add_argument("--sweep-n", type=int, default=4_000_000)
     ap.add_argument("--no-disk", action="store_true")
     ap.add_argument("--theta-w", type=float, default=THETA_W)
+    ap.add_argument("--sweep-thetas", type=lambda v: [float(x) for x in v.split(",")], default=[0.55, 0.6])
     ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
     args = ap.parse_args()
     if args.warmup < 3:
