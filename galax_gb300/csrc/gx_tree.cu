@@ -141,7 +141,12 @@ __global__ void k_chunk_ranges(int64_t n, int64_t n_max, int64_t nl, int32_t *rs
 // them there, and the host only waits once per batch of rounds.  A round whose new
 // level would not fit the node storage sets the overflow flag; the build is then redone
 // with more storage.
-enum { TS_S = 0, TS_E = 1, TS_C = 2, TS_SHIFT = 3, TS_NSEG = 4, TS_NG = 5, TS_FLAGS = 6, TS_ROUNDS = 7, TS_N = 8 };
+enum {
+    TS_S = 0, TS_E = 1, TS_C = 2, TS_SHIFT = 3, TS_NSEG = 4, TS_NG = 5, TS_FLAGS = 6, TS_ROUNDS = 7,
+    TS_CHAIN_M = 8,  // min over adjacent leaves of the highest bit in which their first keys differ
+    TS_CHAIN_L = 9,  // single-child rounds built by k_chain_rounds
+    TS_N = 10
+};
 enum { TS_DONE = 1, TS_OVERFLOW = 2, TS_STUCK = 4 };
 constexpr int TS_MAX_ROUNDS = 400;  // level starts kept: TS_MAX_ROUNDS + 2
 
@@ -264,6 +269,64 @@ __global__ void k_parent_fields(const int64_t *st, double *cx, double *cy, doubl
     int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ng) return;
     parent_fields_one(e + g, cx, cy, hw, mass, comx, comy, bs, be, child, parent, is_leaf);
+}
+
+// Single-child rounds.  Round r groups consecutive nodes whose first bodies' keys agree
+// after >> 2r; while every node of the level is its own group, the round makes one parent
+// per node.  Starting from the leaves, that holds for rounds r = 1 .. m/2 exactly, m the
+// smallest, over adjacent leaves, highest bit in which their first keys differ (below
+// it the prefixes differ for every pair; at 2r > m one pair agrees).  k_chain_depth finds
+// m; k_chain_rounds builds those rounds at once, a thread per leaf walking its chain
+// (level l node x + l nl is the one parent of x + (l-1) nl, its fields by the same
+// parent_fields_one as a round), and moves the round state past them, so the multi-block
+// rounds start at the first round that groups.  At 1M Plummer that is the first eight
+// rounds: 8 x 13 launches become 2.
+__global__ void k_chain_depth(int64_t nl, const uint64_t *__restrict__ keys, const int32_t *__restrict__ bs,
+                              int64_t *st) {
+    __shared__ int wmin[8];
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int m = 64;
+    if (i >= 1 && i < nl) {
+        const uint64_t d = keys[bs[i]] ^ keys[bs[i - 1]];
+        m = d ? 63 - __clzll((long long)d) : -1;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) wmin[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int b = wmin[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = min(b, wmin[w]);
+        if (b < 64) atomicMin(reinterpret_cast<long long *>(st + TS_CHAIN_M), (long long)b);
+    }
+}
+
+__global__ void k_chain_rounds(int64_t *st, int64_t *level_start, int64_t nl, int64_t cap_nodes, double *cx,
+                               double *cy, double *hw, double *mass, double *comx, double *comy, int32_t *bs,
+                               int32_t *be, int4 *child, int32_t *parent, uint8_t *is_leaf) {
+    if (st[TS_FLAGS] != 0 || nl <= TS_SMALL) return;
+    int64_t L = st[TS_CHAIN_M] >= 2 ? st[TS_CHAIN_M] / 2 : 0;
+    L = min(L, cap_nodes / nl - 1);
+    L = min(L, (int64_t)TS_MAX_ROUNDS - 2);
+    if (L <= 0) return;
+    const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x < nl) {
+        for (int64_t l = 1; l <= L; l++) {
+            const int64_t q = x + l * nl, c = x + (l - 1) * nl;
+            child[q] = make_int4((int)c, -1, -1, -1);
+            parent[c] = (int32_t)q;
+            parent_fields_one(q, cx, cy, hw, mass, comx, comy, bs, be, child, parent, is_leaf);
+        }
+    }
+    if (x == 0) {
+        for (int64_t r = 1; r <= L; r++) level_start[r + 1] = (r + 1) * nl;
+        st[TS_S] = L * nl;
+        st[TS_E] = (L + 1) * nl;
+        st[TS_C] = nl;
+        st[TS_SHIFT] = 2 + 2 * L;
+        st[TS_ROUNDS] = L;
+        st[TS_CHAIN_L] = L;
+    }
 }
 
 // The rounds of levels of at most TS_SMALL nodes, all in one block: each phase of a
@@ -450,10 +513,20 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
             dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), dptr<int4>(ctx->child),
             dptr<int32_t>(ctx->parent), dptr<uint8_t>(ctx->is_leaf));
         ctx->launches++;
-        const int64_t init[TS_N] = {0, nl, nl, 2, 0, 0, nl > 1 ? 0 : TS_DONE, 0};
+        const int64_t init[TS_N] = {0, nl, nl, 2, 0, 0, nl > 1 ? 0 : TS_DONE, 0, 64, 0};
         const int64_t ls01[2] = {0, nl};
         GX_CUDA(ctx, cudaMemcpyAsync(st, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
         GX_CUDA(ctx, cudaMemcpyAsync(lstart, ls01, sizeof(ls01), cudaMemcpyHostToDevice, ctx->stream));
+        if (nl > TS_SMALL) {
+            k_chain_depth<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, dptr<uint64_t>(ctx->keys),
+                                                                      dptr<int32_t>(ctx->bs), st);
+            k_chain_rounds<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(
+                st, lstart, nl, cap, dptr<double>(ctx->cx), dptr<double>(ctx->cy), dptr<double>(ctx->hw),
+                dptr<double>(ctx->mass), dptr<double>(ctx->comx), dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs),
+                dptr<int32_t>(ctx->be), dptr<int4>(ctx->child), dptr<int32_t>(ctx->parent),
+                dptr<uint8_t>(ctx->is_leaf));
+            ctx->launches += 2;
+        }
         // rounds in batches: the last build's round count first, then 8 at a time
         // multi-block rounds in batches (the last build's count first), each batch followed
         // by the single-block kernel for the small levels
@@ -498,9 +571,10 @@ static int build_from_ranges(gx_ctx *ctx, const int32_t *rs, const int32_t *re, 
     GX_CUDA(ctx, cudaMemcpyAsync(ls.data(), lstart, sizeof(int64_t) * ls.size(), cudaMemcpyDeviceToHost, ctx->stream));
     GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     ctx->level_start.assign(ls.begin(), ls.end());
-    ctx->hint_big_rounds = 0;
+    ctx->hint_big_rounds = 0;  // multi-block rounds after the single-child ones
     for (size_t l = 0; l + 2 < ls.size(); l++)
         if (ls[l + 1] - ls[l] > TS_SMALL) ctx->hint_big_rounds++;
+    ctx->hint_big_rounds = std::max<int64_t>(0, ctx->hint_big_rounds - hs[TS_CHAIN_L]);
     const int64_t nn = ls.back();
     ctx->n_nodes = nn;
     ctx->hint_nodes = nn;

@@ -54,6 +54,9 @@ def _compare_tree(G, O, b, n_max, bounds, balanced=False):
     ("galaxy", 5_001, 32),
     ("disk", 20_000, 16),
     ("uniform", 3_000, 64),
+    # more than 2048 leaves: the single-child rounds are built by one fused kernel
+    ("plummer", 200_000, 32),
+    ("uniform", 100_000, 16),
 ])
 def test_tree_and_lists_bit_exact(G, oracle, preset, n, n_max):
     from galax_gb300 import presets
