@@ -56,10 +56,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FMM bodies/s (1M, p=4) mixed vs FP64 at equal force error; adjoint/fwd time"
 N_DEFAULT = 1_000_000
-# DRAM bytes (read 46.78 MB + written 20.44 MB) of one k_p2p32_rows launch at the
-# default workload, from a one-pass ncu capture (dram__bytes_read.sum +
-# dram__bytes_write.sum) of this workload: the kernel works out of L2
-P2P_TRAFFIC_1M = 67.22e6
+# DRAM bytes of one k_p2p32_rows launch at the default workload (theta_w = 0.4), the mean
+# of two launches of a one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum:
+# 34.92 + 1.14 MB and 34.88 + 0.49 MB): the kernel works out of L2
+P2P_TRAFFIC_1M = 35.72e6
 P, N_MAX, THETA = 4, 32, 0.5
 # leaf-level near-list split (M2P / P2L) of the ACCURATE forms: near leaf pairs that are
 # far on one side at this opening angle leave P2P
