@@ -1319,8 +1319,9 @@ __global__ void __launch_bounds__(NS_THREADS) k_near_split(int64_t nl, const int
     int cnt[3] = {0, 0, 0};
     for (int q = q0; q < q1; q++) {
         const int32_t src = near_idx[s0 + q];
-        scratch[s0 + q] = src;
-        cnt[src != (int32_t)a ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0]++;
+        const int k = src != (int32_t)a ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
+        scratch[s0 + q] = src | (k << 30);  // node ids stay below 2^30 (checked by the host)
+        cnt[k]++;
     }
     // exclusive scan of the three counts over the block, in thread (= list) order
     int ex[3];
@@ -1349,9 +1350,9 @@ __global__ void __launch_bounds__(NS_THREADS) k_near_split(int64_t nl, const int
     }
     int o[3] = {ex[0], total[0] + ex[1], total[0] + total[1] + ex[2]};
     for (int q = q0; q < q1; q++) {
-        const int32_t src = scratch[s0 + q];
-        const int k = src != (int32_t)a ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
-        near_idx[s0 + o[k]++] = src;
+        const int32_t v = scratch[s0 + q];
+        const int k = (v >> 30) & 3;
+        near_idx[s0 + o[k]++] = v & 0x3fffffff;
     }
     if (t == 0) {
         ncnt[a] = total[0];
@@ -1372,6 +1373,7 @@ __global__ void __launch_bounds__(NS_THREADS) k_near_split(int64_t nl, const int
 // gx_plan_accurate; the totals are read back by gx_plan_items.
 int gx_plan_near_split(gx_ctx *ctx) {
     const int64_t nl = ctx->n_leaves, nn = ctx->n_nodes;
+    if (nn >= ((int64_t)1 << 30)) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "near-list split: 2^30 or more nodes");
     GX_TRY(gx_ensure(ctx, ctx->split_cnt, sizeof(int32_t) * 2 * (size_t)(nl > 0 ? nl : 1)));
     GX_TRY(gx_ensure(ctx, ctx->split_tot, sizeof(unsigned long long) * 4));
     GX_TRY(gx_ensure(ctx, ctx->scratch_f, sizeof(int32_t) * (size_t)(ctx->hint_near + 1)));
