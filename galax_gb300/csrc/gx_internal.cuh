@@ -241,6 +241,10 @@ int gx_exclusive_scan_i32(gx_ctx *ctx, const int32_t *in, int32_t *out, int64_t 
 // the grand total goes to *total_dev when given
 int gx_exclusive_scan_i64_devn(gx_ctx *ctx, const int64_t *in, int64_t *out, const int64_t *n_dev, int64_t n_add,
                                int64_t n_cap, int64_t *total_dev = nullptr);
+// m arrays at a common stride (in + k * stride -> out + k * stride), one set of launches;
+// total_dev (if given) receives m totals
+int gx_exclusive_scan_i64_devn_multi(gx_ctx *ctx, const int64_t *in, int64_t *out, int m, int64_t stride,
+                                     const int64_t *n_dev, int64_t n_add, int64_t n_cap, int64_t *total_dev = nullptr);
 int gx_radix_sort_u64(gx_ctx *ctx, uint64_t *keys, uint32_t *vals, int64_t n, int begin_bit, int end_bit,
                       uint64_t *keys_alt, uint32_t *vals_alt, bool *result_in_alt);
 // gx_kdk.cu

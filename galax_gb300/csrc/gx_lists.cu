@@ -400,28 +400,74 @@ __device__ __forceinline__ double dist_rn(double dx, double dy) {
     return __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
 }
 
+// a warp per leaf, a lane per body: the maximum is exact in any order, and as the
+// correctly rounded square root is monotone, the largest distance is the root of the
+// largest squared distance (one FP64 square root per leaf instead of one per body)
 __global__ void k_radius_leaves(int64_t nl, const double *x, const double *y, const double *comx, const double *comy,
                                 const int32_t *bs, const int32_t *be, double *R) {
-    int64_t L = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t L = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (L >= nl) return;
+    const double cx = comx[L], cy = comy[L];
+    double r2 = 0.0;
+    for (int32_t i = bs[L] + lane; i < be[L]; i += 32) {
+        const double dx = x[i] - cx, dy = y[i] - cy;
+        r2 = fmax(r2, __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+    if (lane == 0) R[L] = __dsqrt_rn(r2);
+}
+
+__device__ __forceinline__ double radius_node(int64_t q, const int4 *child, const double *comx, const double *comy,
+                                              const double *R) {
+    const int4 c4 = child[q];
+    const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
     double r = 0.0;
-    for (int32_t i = bs[L]; i < be[L]; i++) r = fmax(r, dist_rn(x[i] - comx[L], y[i] - comy[L]));
-    R[L] = r;
+    for (int k = 0; k < 4; k++) {
+        const int c = cc[k];
+        if (c < 0) continue;
+        r = fmax(r, __dadd_rn(dist_rn(comx[c] - comx[q], comy[c] - comy[q]), R[c]));
+    }
+    return r;
 }
 
 __global__ void k_radius_parents(int64_t s, int64_t e, const int4 *child, const double *comx, const double *comy,
                                  double *R) {
     int64_t q = s + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= e) return;
-    int4 c4 = child[q];
-    int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-    double r = 0.0;
-    for (int k = 0; k < 4; k++) {
-        int c = cc[k];
-        if (c < 0) continue;
-        r = fmax(r, __dadd_rn(dist_rn(comx[c] - comx[q], comy[c] - comy[q]), R[c]));
+    R[q] = radius_node(q, child, comx, comy, R);
+}
+
+// levels 1 .. L of single-child chains over the leaves (node x + l nl, child x + (l-1) nl):
+// one thread walks each leaf's chain, the arithmetic of radius_node with one child.  The
+// chain form is checked in the same plan attempt (k_chain_check), which is redone with
+// per-level radii when it fails.
+__global__ void k_radius_chain(int64_t nl, int L, const double *comx, const double *comy, double *R) {
+    const int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= nl) return;
+    double r = R[x];
+    for (int l = 1; l <= L; l++) {
+        const int64_t q = x + l * nl, c = q - nl;
+        r = fmax(0.0, __dadd_rn(dist_rn(comx[c] - comx[q], comy[c] - comy[q]), r));
+        R[q] = r;
     }
-    R[q] = r;
+}
+
+// the top levels (at most RADIUS_TOP nodes each) in one block, a barrier between levels
+constexpr int RADIUS_TOP = 256;  // one SM's FP64 pipe: only the small levels
+constexpr int RADIUS_TOP_THREADS = 256;
+struct RadiusLevels {
+    int64_t start[66];  // level_start of levels lo .. hi + 1
+    int lo, hi;
+};
+__global__ void __launch_bounds__(RADIUS_TOP_THREADS) k_radius_top(RadiusLevels RL, const int4 *child,
+                                                                   const double *comx, const double *comy, double *R) {
+    for (int lv = RL.lo; lv <= RL.hi; lv++) {
+        const int64_t s = RL.start[lv - RL.lo], e = RL.start[lv - RL.lo + 1];
+        for (int64_t q = s + threadIdx.x; q < e; q += RADIUS_TOP_THREADS) R[q] = radius_node(q, child, comx, comy, R);
+        __syncthreads();
+    }
 }
 
 // Far when |com_a - com_b| theta > R_a + R_b, decided in FP32 and compared squared:
@@ -494,15 +540,29 @@ __global__ void k_mac_units(int64_t s, int64_t e, const int64_t *uoff, int64_t u
     }
 }
 
-// pass 0: per-unit counts (ufar, unear), and each candidate's decisions (far mask in
-// the low nibble, near mask in the high one, one bit per child slot) in dec; pass 1:
-// the children written at the running totals plus the per-unit offsets, from dec
-// without testing again.  A grid-stride loop over the level's units, one warp per unit.
-__global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const int32_t *uchunk, const int32_t *parent,
-                      const int4 *child, const float4 *hl, const float *R32, float theta2,
-                      const int64_t *near_start, const int32_t *near_cnt, const int32_t *near_idx_in, int64_t *ufar,
-                      int64_t *unear, int32_t *far_idx, int32_t *near_idx, int64_t far_cap, int64_t near_cap,
-                      uint8_t *dec, int64_t *ctr) {
+__device__ __forceinline__ bool mac_far_v(const float4 A, float Ra, const float4 B, float Rb, float theta2) {
+    const float ex = __fadd_rn(__fsub_rn(A.x, B.x), __fsub_rn(A.y, B.y));
+    const float ey = __fadd_rn(__fsub_rn(A.z, B.z), __fsub_rn(A.w, B.w));
+    const float d2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+    const float s = __fadd_rn(Ra, Rb);
+    return __fmul_rn(d2, theta2) > __fmul_rn(s, s);
+}
+
+// pass 0: per-unit counts (ufar, unear), and each candidate's decisions in dec (one word
+// per lane and unit: byte k holds candidate k * 32 + lane's far mask in the low nibble and
+// its near mask in the high one, one bit per child slot); pass 1: the children written at
+// the running totals plus the per-unit offsets, from dec without testing again.  A
+// grid-stride loop over the level's units, one warp per unit; each lane loads its
+// MAC_ROUNDS candidates, then their children, then tests them, so that the gathers of a
+// unit are in flight together.
+constexpr int MAC_ROUNDS = MAC_CHUNK / 32;
+__global__ void __launch_bounds__(128) k_mac(const int64_t *Uptr, int pass, const int32_t *unode,
+                                             const int32_t *uchunk, const int32_t *parent, const int4 *child,
+                                             const float4 *hl, const float *R32, float theta2,
+                                             const int64_t *near_start, const int32_t *near_cnt,
+                                             const int32_t *near_idx_in, int64_t *ufar, int64_t *unear,
+                                             int32_t *far_idx, int32_t *near_idx, int64_t far_cap, int64_t near_cap,
+                                             uint32_t *dec, int64_t *ctr) {
     const unsigned full = 0xffffffffu;
     if (ctr[PC_OVF]) return;
     const int64_t n_units = *Uptr;
@@ -510,72 +570,82 @@ __global__ void k_mac(const int64_t *Uptr, int pass, const int32_t *unode, const
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t far0 = pass ? ctr[PC_FAR] : 0, near0 = pass ? ctr[PC_NEAR] : 0;
     for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n_units; u += nwarps) {
-        int32_t x = unode[u];
-        int32_t P = parent[x];
+        const int32_t x = unode[u];
+        const int32_t P = parent[x];
         // x is its parent's only child: against the only child of a near entry of P the
         // pair holds the parents' bodies and stays near without a test
         const bool only_child = child[P].y < 0;
-        int64_t qa = near_start[P] + (int64_t)uchunk[u] * MAC_CHUNK;
-        int64_t qe = min(near_start[P] + (int64_t)near_cnt[P], qa + MAC_CHUNK);
-        int64_t nf = 0, nn = 0;
-        int64_t fb = pass ? far0 + ufar[u] : 0, nb = pass ? near0 + unear[u] : 0;
+        const int64_t qa = near_start[P] + (int64_t)uchunk[u] * MAC_CHUNK;
+        const int qn = (int)min((int64_t)MAC_CHUNK, near_start[P] + (int64_t)near_cnt[P] - qa);
+        int64_t fb = 0, nb = 0;
         if (pass) {
             // this unit's whole range must fit; otherwise flag and write nothing
-            int64_t fe = far0 + ufar[u + 1], ne = near0 + unear[u + 1];
-            unsigned long long bad = (fe > far_cap ? OVF_FAR : 0) | (ne > near_cap ? OVF_NEAR : 0);
+            fb = far0 + ufar[u];
+            nb = near0 + unear[u];
+            const int64_t fe = far0 + ufar[u + 1], ne = near0 + unear[u + 1];
+            const unsigned long long bad = (fe > far_cap ? OVF_FAR : 0) | (ne > near_cap ? OVF_NEAR : 0);
             if (bad) {
                 if (lane == 0) atomicOr(reinterpret_cast<unsigned long long *>(ctr + PC_OVF), bad);
                 continue;
             }
         }
-        for (int64_t qb = qa; qb < qe; qb += 32) {
-            int64_t q = qb + lane;
-            int cc[4] = {-1, -1, -1, -1};
-            unsigned fm = 0, nm = 0;
-            if (q < qe) {
-                int4 c4 = child[near_idx_in[q]];
-                cc[0] = c4.x;
-                cc[1] = c4.y;
-                cc[2] = c4.z;
-                cc[3] = c4.w;
-                uint8_t *dq = dec + u * MAC_CHUNK + (q - qa);
-                if (pass) {
-                    const unsigned d = *dq;
-                    fm = d & 15u;
-                    nm = d >> 4;
-                } else {
-                    const bool inherit = only_child && cc[1] < 0;
-                    for (int k = 0; k < 4; k++) {
-                        if (cc[k] < 0) continue;
-                        if (!inherit && mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
-                        else nm |= 1u << k;
-                    }
-                    *dq = (uint8_t)(fm | (nm << 4));
+        int32_t cand[MAC_ROUNDS];
+#pragma unroll
+        for (int k = 0; k < MAC_ROUNDS; k++) cand[k] = k * 32 + lane < qn ? near_idx_in[qa + k * 32 + lane] : -1;
+        int4 c4[MAC_ROUNDS];
+#pragma unroll
+        for (int k = 0; k < MAC_ROUNDS; k++) c4[k] = cand[k] >= 0 ? child[cand[k]] : make_int4(-1, -1, -1, -1);
+        uint32_t d = 0;
+        if (pass) {
+            d = dec[u * 32 + lane];
+        } else {
+            const float4 A = hl[x];
+            const float Ra = R32[x];
+#pragma unroll
+            for (int k = 0; k < MAC_ROUNDS; k++) {
+                const int cc[4] = {c4[k].x, c4[k].y, c4[k].z, c4[k].w};
+                const bool inherit = only_child && cc[1] < 0;
+                unsigned fm = 0, nm = 0;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if (cc[j] < 0) continue;
+                    if (!inherit && mac_far_v(A, Ra, hl[cc[j]], R32[cc[j]], theta2)) fm |= 1u << j;
+                    else nm |= 1u << j;
                 }
+                d |= (fm | (nm << 4)) << (8 * k);
             }
-            int myf = __popc(fm), myn = __popc(nm);
+            dec[u * 32 + lane] = d;
+            const int nf = __reduce_add_sync(full, __popc(d & 0x0f0f0f0fu));
+            const int nn = __reduce_add_sync(full, __popc(d & 0xf0f0f0f0u));
+            if (lane == 0) {
+                ufar[u] = nf;
+                unear[u] = nn;
+            }
+            continue;
+        }
+        int64_t nf = 0, nn = 0;
+#pragma unroll
+        for (int k = 0; k < MAC_ROUNDS; k++) {
+            const unsigned fm = (d >> (8 * k)) & 15u, nm = (d >> (8 * k + 4)) & 15u;
+            const int myf = __popc(fm), myn = __popc(nm);
             int pf = myf, pn = myn;  // inclusive warp scans
+#pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
+                const int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
                 if (lane >= o) {
                     pf += tf;
                     pn += tn;
                 }
             }
-            int tf = __shfl_sync(full, pf, 31), tn = __shfl_sync(full, pn, 31);
-            if (pass) {
-                int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
-                for (int k = 0; k < 4; k++) {
-                    if ((fm >> k) & 1u) far_idx[a++] = cc[k];
-                    if ((nm >> k) & 1u) near_idx[b++] = cc[k];
-                }
+            const int cc[4] = {c4[k].x, c4[k].y, c4[k].z, c4[k].w};
+            int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if ((fm >> j) & 1u) far_idx[a++] = cc[j];
+                if ((nm >> j) & 1u) near_idx[b++] = cc[j];
             }
-            nf += tf;
-            nn += tn;
-        }
-        if (!pass && lane == 0) {
-            ufar[u] = nf;
-            unear[u] = nn;
+            nf += __shfl_sync(full, pf, 31);
+            nn += __shfl_sync(full, pn, 31);
         }
     }
 }
@@ -636,7 +706,7 @@ __global__ void k_chain_leaf_close(int64_t *ctr) {
 // the multi-block pass (parent's near entry, child slot), with block barriers between
 // the steps instead of a dozen launches per level.
 constexpr int PLAN_SMALL = 256;
-constexpr int PLAN_SMALL_THREADS = 256;
+constexpr int PLAN_SMALL_THREADS = 1024;
 struct PlanLevels {
     int64_t start[66];  // level_start of levels lo .. hi + 1 (relative index lv - lo)
     int lo, hi;
@@ -671,7 +741,7 @@ __global__ void __launch_bounds__(PLAN_SMALL_THREADS) k_mac_small_levels(
     PlanLevels L, const int32_t *__restrict__ parent, const int4 *__restrict__ child, const float4 *__restrict__ hl,
     const float *__restrict__ R32, float theta2, int64_t *fstart, int32_t *fcnt, int64_t *nstart, int32_t *ncnt,
     int32_t *far_idx, int32_t *near_idx, int64_t far_cap, int64_t near_cap, int64_t *ctr) {
-    constexpr int PER = PLAN_SMALL / PLAN_SMALL_THREADS;
+    constexpr int PER = (PLAN_SMALL + PLAN_SMALL_THREADS - 1) / PLAN_SMALL_THREADS;
     constexpr int NW = PLAN_SMALL_THREADS / 32;
     const unsigned full = 0xffffffffu;
     __shared__ int cnt_f[PLAN_SMALL], cnt_n[PLAN_SMALL];
@@ -683,42 +753,48 @@ __global__ void __launch_bounds__(PLAN_SMALL_THREADS) k_mac_small_levels(
         const int32_t P = parent[x];
         const bool only_child = child[P].y < 0;
         const int64_t qa = nstart[P], qe = qa + ncnt[P];
+        const float4 A = hl[x];
+        const float Ra = R32[x];
         int nf = 0, nn = 0;
-        for (int64_t qb = qa; qb < qe; qb += 32) {
-            const int64_t q = qb + lane;
-            int cc[4] = {-1, -1, -1, -1};
-            unsigned fm = 0, nm = 0;
-            if (q < qe) {
-                const int4 c4 = child[near_idx[q]];
-                cc[0] = c4.x;
-                cc[1] = c4.y;
-                cc[2] = c4.z;
-                cc[3] = c4.w;
+        for (int64_t qb = qa; qb < qe; qb += 32 * MAC_ROUNDS) {
+            int32_t cand[MAC_ROUNDS];
+#pragma unroll
+            for (int k = 0; k < MAC_ROUNDS; k++) cand[k] = qb + k * 32 + lane < qe ? near_idx[qb + k * 32 + lane] : -1;
+            int4 c4[MAC_ROUNDS];
+#pragma unroll
+            for (int k = 0; k < MAC_ROUNDS; k++) c4[k] = cand[k] >= 0 ? child[cand[k]] : make_int4(-1, -1, -1, -1);
+#pragma unroll
+            for (int k = 0; k < MAC_ROUNDS; k++) {
+                const int cc[4] = {c4[k].x, c4[k].y, c4[k].z, c4[k].w};
                 const bool inherit = only_child && cc[1] < 0;
-                for (int k = 0; k < 4; k++) {
-                    if (cc[k] < 0) continue;
-                    if (!inherit && mac_far(hl, R32, x, cc[k], theta2)) fm |= 1u << k;
-                    else nm |= 1u << k;
+                unsigned fm = 0, nm = 0;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if (cc[j] < 0) continue;
+                    if (!inherit && mac_far_v(A, Ra, hl[cc[j]], R32[cc[j]], theta2)) fm |= 1u << j;
+                    else nm |= 1u << j;
                 }
-            }
-            const int myf = __popc(fm), myn = __popc(nm);
-            int pf = myf, pn = myn;
-            for (int o = 1; o < 32; o <<= 1) {
-                const int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
-                if (lane >= o) {
-                    pf += tf;
-                    pn += tn;
+                const int myf = __popc(fm), myn = __popc(nm);
+                int pf = myf, pn = myn;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int tf = __shfl_up_sync(full, pf, o), tn = __shfl_up_sync(full, pn, o);
+                    if (lane >= o) {
+                        pf += tf;
+                        pn += tn;
+                    }
                 }
-            }
-            if (pass) {
-                int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
-                for (int k = 0; k < 4; k++) {
-                    if ((fm >> k) & 1u) far_idx[a++] = cc[k];
-                    if ((nm >> k) & 1u) near_idx[b++] = cc[k];
+                if (pass) {
+                    int64_t a = fb + nf + (pf - myf), b = nb + nn + (pn - myn);
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        if ((fm >> j) & 1u) far_idx[a++] = cc[j];
+                        if ((nm >> j) & 1u) near_idx[b++] = cc[j];
+                    }
                 }
+                nf += __shfl_sync(full, pf, 31);
+                nn += __shfl_sync(full, pn, 31);
             }
-            nf += __shfl_sync(full, pf, 31);
-            nn += __shfl_sync(full, pn, 31);
         }
         nf_out = nf;
         nn_out = nn;
@@ -1125,16 +1201,6 @@ int gx_plan_accurate(gx_ctx *ctx) {
     GX_TRY(gx_ensure(ctx, ctx->radius, sizeof(double) * (size_t)nn));
     double *R = dptr<double>(ctx->radius);
     int64_t nl = ctx->level_start[1];
-    k_radius_leaves<<<gx_blocks(nl, 128), 128, 0, ctx->stream>>>(nl, dptr<double>(ctx->x), dptr<double>(ctx->y),
-                                                                dptr<double>(ctx->comx), dptr<double>(ctx->comy),
-                                                                dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), R);
-    ctx->launches++;
-    for (int lv = 1; lv < ctx->n_levels; lv++) {
-        int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
-        k_radius_parents<<<gx_blocks(e - s, 128), 128, 0, ctx->stream>>>(s, e, dptr<int4>(ctx->child),
-                                                                        dptr<double>(ctx->comx), dptr<double>(ctx->comy), R);
-        ctx->launches++;
-    }
     // per-node start/count for far and near lists
     GX_TRY(gx_ensure(ctx, ctx->far_off, sizeof(int64_t) * (size_t)nn + sizeof(int32_t) * (size_t)nn + 64));
     GX_TRY(gx_ensure(ctx, ctx->near_off, sizeof(int64_t) * (size_t)nn + sizeof(int32_t) * (size_t)nn + 64));
@@ -1148,7 +1214,6 @@ int gx_plan_accurate(gx_ctx *ctx) {
     const float theta2 = thf * thf;
     GX_TRY(gx_ensure(ctx, ctx->radius32, sizeof(float) * (size_t)nn));
     float *R32 = dptr<float>(ctx->radius32);
-    k_to_f32<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, R, R32);
     const float4 *hl = dptr<float4>(ctx->comhl);
     int64_t cmax = 1;
     for (int lv = 0; lv < ctx->n_levels; lv++)
@@ -1160,6 +1225,45 @@ int gx_plan_accurate(gx_ctx *ctx) {
     while (L + 1 < ctx->n_levels && ctx->level_start[L + 2] - ctx->level_start[L + 1] == nl0) L++;
     ctx->chain_levels = L >= 2 ? L : 0;
     int lv_low = ctx->chain_levels;  // the lowest level the loop below processes
+    // node radii, FP64 and rounded once to FP32: per level, or with the chain levels walked
+    // by one thread per leaf and the top levels in one block
+    auto radii = [&](int chain) -> int {
+        k_radius_leaves<<<gx_blocks(nl * 32, 256), 256, 0, ctx->stream>>>(
+            nl, dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->comx), dptr<double>(ctx->comy),
+            dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), R);
+        ctx->launches++;
+        int lv = 1;
+        if (chain >= 2) {
+            k_radius_chain<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, chain, dptr<double>(ctx->comx),
+                                                                       dptr<double>(ctx->comy), R);
+            ctx->launches++;
+            lv = chain + 1;
+        }
+        int top = ctx->n_levels;  // levels top .. n_levels - 1 go to one block
+        while (top - 1 >= lv && ctx->level_start[top] - ctx->level_start[top - 1] <= RADIUS_TOP && top - 1 > ctx->n_levels - 65)
+            top--;
+        for (; lv < top; lv++) {
+            const int64_t s = ctx->level_start[lv], e = ctx->level_start[lv + 1];
+            k_radius_parents<<<gx_blocks(e - s, 128), 128, 0, ctx->stream>>>(s, e, dptr<int4>(ctx->child),
+                                                                            dptr<double>(ctx->comx),
+                                                                            dptr<double>(ctx->comy), R);
+            ctx->launches++;
+        }
+        if (top < ctx->n_levels) {
+            RadiusLevels RL;
+            RL.lo = top;
+            RL.hi = ctx->n_levels - 1;
+            for (int l = RL.lo; l <= RL.hi + 1; l++) RL.start[l - RL.lo] = ctx->level_start[l];
+            k_radius_top<<<1, RADIUS_TOP_THREADS, 0, ctx->stream>>>(RL, dptr<int4>(ctx->child),
+                                                                   dptr<double>(ctx->comx), dptr<double>(ctx->comy), R);
+            ctx->launches++;
+        }
+        k_to_f32<<<gx_blocks(nn, 256), 256, 0, ctx->stream>>>(nn, R, R32);
+        ctx->launches++;
+        GX_CUDA(ctx, cudaGetLastError());
+        return GX_OK;
+    };
+    GX_TRY(radii(lv_low));
     // capacities: unit arrays and the far / near index arrays, kept from the last plan
     if (ctx->mac_ucap < 1024) ctx->mac_ucap = std::max<int64_t>(1024, nn);
     int64_t far_cap = std::max<int64_t>({(int64_t)(ctx->far_idx.bytes / sizeof(int32_t)), int64_t(1) << 20, 64 * nn,
@@ -1178,8 +1282,8 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * (size_t)(cmax + 1) * 2));
         GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int32_t) * (size_t)(ucap + 1) * 2));
         GX_TRY(gx_ensure(ctx, ctx->scratch_e, sizeof(int64_t) * (size_t)(ucap + 1) * 4));
-        GX_TRY(gx_ensure(ctx, ctx->scratch_d, (size_t)(ucap + 1) * MAC_CHUNK));
-        uint8_t *dec = dptr<uint8_t>(ctx->scratch_d);
+        GX_TRY(gx_ensure(ctx, ctx->scratch_d, sizeof(uint32_t) * 32 * (size_t)(ucap + 1)));
+        uint32_t *dec = dptr<uint32_t>(ctx->scratch_d);
         int64_t *nch = dptr<int64_t>(ctx->scratch_a), *uoff = nch + (cmax + 1);
         int32_t *unode = dptr<int32_t>(ctx->scratch_b), *uchunk = unode + (ucap + 1);
         int64_t *ufar = dptr<int64_t>(ctx->scratch_e), *unear = ufar + (ucap + 1), *ufo = unear + (ucap + 1),
@@ -1230,8 +1334,8 @@ int gx_plan_accurate(gx_ctx *ctx) {
                                                  dptr<int4>(ctx->child), hl, R32, theta2, nstart, ncnt,
                                                  dptr<int32_t>(ctx->near_idx), ufar, unear, nullptr, nullptr, far_cap,
                                                  near_cap, dec, ctr);
-            GX_TRY(gx_exclusive_scan_i64_devn(ctx, ufar, ufo, Ud, 1, ucap + 1));
-            GX_TRY(gx_exclusive_scan_i64_devn(ctx, unear, uno, Ud, 1, ucap + 1));
+            // ufar, unear -> ufo, uno (arrays ucap + 1 apart) in one scan
+            GX_TRY(gx_exclusive_scan_i64_devn_multi(ctx, ufar, ufo, 2, ucap + 1, Ud, 1, ucap + 1));
             k_mac<<<gmac, 128, 0, ctx->stream>>>(Ud, 1, unode, uchunk, dptr<int32_t>(ctx->parent),
                                                  dptr<int4>(ctx->child), hl, R32, theta2, nstart, ncnt,
                                                  dptr<int32_t>(ctx->near_idx), ufo, uno, dptr<int32_t>(ctx->far_idx),
@@ -1239,7 +1343,7 @@ int gx_plan_accurate(gx_ctx *ctx) {
             k_mac_node_lists<<<gx_blocks(c, 256), 256, 0, ctx->stream>>>(s, e, uoff, ufo, uno, ctr, fstart, fcnt,
                                                                         nstart, ncnt);
             k_mac_advance<<<1, 1, 0, ctx->stream>>>(Ud, ufo, uno, ctr);
-            ctx->launches += 7;
+            ctx->launches += 6;
             GX_CUDA(ctx, cudaGetLastError());
         }
         if (lv_low >= 2) {
@@ -1254,7 +1358,10 @@ int gx_plan_accurate(gx_ctx *ctx) {
         GX_CUDA(ctx, cudaMemcpyAsync(hc, ctr, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
         GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         if (!hc[PC_OVF]) break;
-        if (hc[PC_OVF] & OVF_CHAIN) ctx->chain_levels = lv_low = 0;  // no shortcut for this tree
+        if (hc[PC_OVF] & OVF_CHAIN) {  // no shortcut for this tree; its radii per level
+            ctx->chain_levels = lv_low = 0;
+            GX_TRY(radii(0));
+        }
         if (hc[PC_OVF] & OVF_UNITS) ctx->mac_ucap *= 4;
         if (hc[PC_OVF] & OVF_FAR) far_cap *= 4;
         if (hc[PC_OVF] & OVF_NEAR) near_cap *= 4;
@@ -1276,12 +1383,12 @@ int gx_plan_accurate(gx_ctx *ctx) {
 }
 
 namespace {
-// Near-list split, one warp per leaf.  A near pair (a <- s), s != a, is M2P when every
-// target body sees the source leaf from at least d - R_a with (d - R_a) theta_w > R_s,
-// else P2L when every source body lies at least d - R_s from com_a with
-// (d - R_s) theta_w > R_a, else P2P; the leaf itself is P2P.  Tested in FP32 on the
-// MAC's operands with separately rounded operations (the oracle's gxo_near_split makes
-// the same decisions):  d2 tw^2 > (R_s + tw R_a)^2, then d2 tw^2 > (R_a + tw R_s)^2.
+// Near-list split.  A near pair (a <- s), s != a, is M2P when every target body sees the
+// source leaf from at least d - R_a with (d - R_a) theta_w > R_s, else P2L when every
+// source body lies at least d - R_s from com_a with (d - R_s) theta_w > R_a, else P2P; the
+// leaf itself is P2P.  Tested in FP32 on the MAC's operands with separately rounded
+// operations (the oracle's gxo_near_split makes the same decisions):
+// d2 tw^2 > (R_s + tw R_a)^2, then d2 tw^2 > (R_a + tw R_s)^2.
 __device__ __forceinline__ int near_kind(const float4 A, float Ra, const float4 B, float Rs, float tw, float tw2) {
     const float ex = __fadd_rn(__fsub_rn(A.x, B.x), __fsub_rn(A.y, B.y));
     const float ey = __fadd_rn(__fsub_rn(A.z, B.z), __fsub_rn(A.w, B.w));
@@ -1292,76 +1399,137 @@ __device__ __forceinline__ int near_kind(const float4 A, float Ra, const float4 
     return lhs > __fmul_rn(sl, sl) ? 2 : 0;
 }
 
-// The leaf's list is copied to scratch (same offsets) and written back partitioned as
-// [P2P | M2P | P2L], each part in list order; the leaf's near count becomes its P2P
-// count, split_cnt[2a], [2a + 1] its M2P and P2L counts; tot gets the three totals.
-// One block of NS_THREADS per leaf, each thread a contiguous chunk of the list, the
-// chunks' counts scanned across the block: the widest halo leaf's list (~6000 entries at
-// 1M Plummer) is spread over the block instead of one warp's sequential rounds.
-constexpr int NS_THREADS = 128;
-__global__ void __launch_bounds__(NS_THREADS) k_near_split(int64_t nl, const int64_t *__restrict__ nstart,
-                                                           int32_t *__restrict__ ncnt, int32_t *__restrict__ near_idx,
-                                                           int32_t *__restrict__ scratch,
-                                                           const float4 *__restrict__ hl,
-                                                           const float *__restrict__ R32, float tw, float tw2,
-                                                           int32_t *__restrict__ split_cnt,
-                                                           unsigned long long *__restrict__ tot) {
-    __shared__ int wsum[3][NS_THREADS / 32];
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
-    const int64_t a = blockIdx.x;
+// Each leaf's list is cut into units of NS_CHUNK entries (unit = (leaf, chunk j, length)),
+// one warp per unit, so that the widest halo leaves (lists of every leaf of the tree at
+// 1M Plummer) spread over many warps like the short ones.  k_ns_kinds tags each entry
+// with its kind (copied to scratch at the same offset, kind in bits 30-31) and counts the
+// unit's kinds; k_ns_write sums the counts of the leaf's earlier units and of all of them
+// and writes the unit's entries back, partitioned as [P2P | M2P | P2L] in list order.
+constexpr int NS_CHUNK = 256;
+constexpr int NS_ROUNDS = NS_CHUNK / 32;
+
+__global__ void k_ns_nchunks(int64_t nl, const int32_t *ncnt, int64_t *nch) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a > nl) return;
+    nch[a] = a == nl ? 0 : (ncnt[a] + NS_CHUNK - 1) / NS_CHUNK;
+}
+
+__global__ void k_ns_units(int64_t nl, const int32_t *ncnt, const int64_t *uoff, int4 *unit, int32_t *split_cnt) {
+    const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= nl) return;
-    const int64_t s0 = nstart[a];
-    const int c = ncnt[a];
-    const float4 A = hl[a];
-    const float Ra = R32[a];
-    const int per = (c + NS_THREADS - 1) / NS_THREADS;
-    const int q0 = min(c, t * per), q1 = min(c, q0 + per);
-    int cnt[3] = {0, 0, 0};
-    for (int q = q0; q < q1; q++) {
-        const int32_t src = near_idx[s0 + q];
-        const int k = src != (int32_t)a ? near_kind(A, Ra, hl[src], R32[src], tw, tw2) : 0;
-        scratch[s0 + q] = src | (k << 30);  // node ids stay below 2^30 (checked by the host)
-        cnt[k]++;
-    }
-    // exclusive scan of the three counts over the block, in thread (= list) order
-    int ex[3];
+    const int32_t c = ncnt[a];
+    const int64_t u0 = uoff[a];
+    for (int32_t j = 0; j * NS_CHUNK < c; j++) unit[u0 + j] = make_int4((int32_t)a, j, min(NS_CHUNK, c - j * NS_CHUNK), 0);
+    if (c == 0) split_cnt[2 * a] = split_cnt[2 * a + 1] = 0;  // no unit writes them
+}
+
+__global__ void __launch_bounds__(128) k_ns_kinds(const int64_t *__restrict__ Ud, const int4 *__restrict__ unit,
+                                                   const int64_t *__restrict__ nstart,
+                                                   const int32_t *__restrict__ near_idx, int32_t *__restrict__ scratch,
+                                                   const float4 *__restrict__ hl, const float *__restrict__ R32,
+                                                   float tw, float tw2, int4 *__restrict__ ucnt) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t nu = *Ud, nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nu; u += nwarps) {
+        const int4 r = unit[u];
+        const int32_t a = r.x;
+        const int64_t s = nstart[a] + (int64_t)r.y * NS_CHUNK;
+        int32_t v[NS_ROUNDS];
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        int v = cnt[k];
+        for (int k = 0; k < NS_ROUNDS; k++) v[k] = k * 32 + lane < r.z ? near_idx[s + k * 32 + lane] : -1;
+        const float4 A = hl[a];
+        const float Ra = R32[a];
+        int n1 = 0, n2 = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, v, o);
-            if (lane >= o) v += u;
+        for (int k = 0; k < NS_ROUNDS; k++) {
+            int kind = 0;
+            if (v[k] >= 0) {
+                if (v[k] != a) kind = near_kind(A, Ra, hl[v[k]], R32[v[k]], tw, tw2);
+                scratch[s + k * 32 + lane] = v[k] | (kind << 30);  // node ids stay below 2^30 (checked by the host)
+            }
+            n1 += __popc(__ballot_sync(full, kind == 1));
+            n2 += __popc(__ballot_sync(full, kind == 2));
         }
-        ex[k] = v - cnt[k];
-        if (lane == 31) wsum[k][w] = v;
+        if (lane == 0) ucnt[u] = make_int4(r.z - n1 - n2, n1, n2, 0);
     }
-    __syncthreads();  // also orders the scratch copy before its read-back below
-    int total[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        int before = 0, all = 0;
-        for (int ww = 0; ww < NS_THREADS / 32; ww++) {
-            if (ww < w) before += wsum[k][ww];
-            all += wsum[k][ww];
+}
+
+// tot[0..2] gets the three totals: per block, the leaf totals its warps met at chunk 0
+__global__ void __launch_bounds__(128) k_ns_write(const int64_t *__restrict__ Ud, const int4 *__restrict__ unit,
+                                                   const int64_t *__restrict__ uoff,
+                                                   const int64_t *__restrict__ nstart,
+                                                   const int32_t *__restrict__ scratch,
+                                                   const int4 *__restrict__ ucnt, int32_t *__restrict__ near_idx,
+                                                   int32_t *__restrict__ ncnt, int32_t *__restrict__ split_cnt,
+                                                   unsigned long long *__restrict__ tot) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    __shared__ unsigned long long btot[3];
+    if (threadIdx.x < 3) btot[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned long long my[3] = {0, 0, 0};
+    const int64_t nu = *Ud, nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < nu; u += nwarps) {
+        const int4 r = unit[u];
+        const int32_t a = r.x, j = r.y;
+        const int64_t u0 = uoff[a], nua = uoff[a + 1] - u0;
+        // counts of the leaf's units before this one (p) and of all of them (t)
+        int p0 = 0, p1 = 0, p2 = 0, t0 = 0, t1 = 0, t2 = 0;
+        for (int64_t i = lane; i < nua; i += 32) {
+            const int4 c = ucnt[u0 + i];
+            t0 += c.x;
+            t1 += c.y;
+            t2 += c.z;
+            if (i < j) {
+                p0 += c.x;
+                p1 += c.y;
+                p2 += c.z;
+            }
         }
-        ex[k] += before;
-        total[k] = all;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            p0 += __shfl_xor_sync(full, p0, o);
+            p1 += __shfl_xor_sync(full, p1, o);
+            p2 += __shfl_xor_sync(full, p2, o);
+            t0 += __shfl_xor_sync(full, t0, o);
+            t1 += __shfl_xor_sync(full, t1, o);
+            t2 += __shfl_xor_sync(full, t2, o);
+        }
+        const int64_t s0 = nstart[a], s = s0 + (int64_t)j * NS_CHUNK;
+        int o0 = p0, o1 = t0 + p1, o2 = t0 + t1 + p2;
+#pragma unroll
+        for (int k = 0; k < NS_ROUNDS; k++) {
+            const bool ok = k * 32 + lane < r.z;
+            const int32_t v = ok ? scratch[s + k * 32 + lane] : 0;
+            const int kind = ok ? (v >> 30) & 3 : 3;
+            const unsigned m0 = __ballot_sync(full, kind == 0), m1 = __ballot_sync(full, kind == 1),
+                           m2 = __ballot_sync(full, kind == 2);
+            if (ok) {
+                const int pos = kind == 0 ? o0 + __popc(m0 & lt) : kind == 1 ? o1 + __popc(m1 & lt) : o2 + __popc(m2 & lt);
+                near_idx[s0 + pos] = v & 0x3fffffff;
+            }
+            o0 += __popc(m0);
+            o1 += __popc(m1);
+            o2 += __popc(m2);
+        }
+        if (j == 0 && lane == 0) {
+            ncnt[a] = t0;
+            split_cnt[2 * a] = t1;
+            split_cnt[2 * a + 1] = t2;
+            my[0] += (unsigned long long)t0;
+            my[1] += (unsigned long long)t1;
+            my[2] += (unsigned long long)t2;
+        }
     }
-    int o[3] = {ex[0], total[0] + ex[1], total[0] + total[1] + ex[2]};
-    for (int q = q0; q < q1; q++) {
-        const int32_t v = scratch[s0 + q];
-        const int k = (v >> 30) & 3;
-        near_idx[s0 + o[k]++] = v & 0x3fffffff;
+    if (lane == 0) {
+        atomicAdd(&btot[0], my[0]);
+        atomicAdd(&btot[1], my[1]);
+        atomicAdd(&btot[2], my[2]);
     }
-    if (t == 0) {
-        ncnt[a] = total[0];
-        split_cnt[2 * a] = total[1];
-        split_cnt[2 * a + 1] = total[2];
-        atomicAdd(tot + 0, (unsigned long long)total[0]);
-        atomicAdd(tot + 1, (unsigned long long)total[1]);
-        atomicAdd(tot + 2, (unsigned long long)total[2]);
-    }
+    __syncthreads();
+    if (threadIdx.x < 3 && btot[threadIdx.x]) atomicAdd(tot + threadIdx.x, btot[threadIdx.x]);
 }
 }  // namespace
 
@@ -1376,17 +1544,31 @@ int gx_plan_near_split(gx_ctx *ctx) {
     if (nn >= ((int64_t)1 << 30)) return gx_fail(ctx, GX_ERR_CAP_EXCEEDED, "near-list split: 2^30 or more nodes");
     GX_TRY(gx_ensure(ctx, ctx->split_cnt, sizeof(int32_t) * 2 * (size_t)(nl > 0 ? nl : 1)));
     GX_TRY(gx_ensure(ctx, ctx->split_tot, sizeof(unsigned long long) * 4));
-    GX_TRY(gx_ensure(ctx, ctx->scratch_f, sizeof(int32_t) * (size_t)(ctx->hint_near + 1)));
     GX_CUDA(ctx, cudaMemsetAsync(ctx->split_tot.p, 0, sizeof(unsigned long long) * 4, ctx->stream));
     if (nl > 0) {
         int64_t *nstart = dptr<int64_t>(ctx->near_off);
         int32_t *ncnt = reinterpret_cast<int32_t *>(nstart + nn);
         const float tw = (float)ctx->theta_w, tw2 = tw * tw;
-        k_near_split<<<(unsigned)nl, NS_THREADS, 0, ctx->stream>>>(
-            nl, nstart, ncnt, dptr<int32_t>(ctx->near_idx), dptr<int32_t>(ctx->scratch_f), dptr<float4>(ctx->comhl),
-            dptr<float>(ctx->radius32), tw, tw2, dptr<int32_t>(ctx->split_cnt),
-            dptr<unsigned long long>(ctx->split_tot));
-        ctx->launches++;
+        // units: at most one per leaf plus one per NS_CHUNK entries of the near-list storage
+        const int64_t ncap = (int64_t)(ctx->near_idx.bytes / sizeof(int32_t));
+        const int64_t ucap = nl + ncap / NS_CHUNK + 1;
+        GX_TRY(gx_ensure(ctx, ctx->scratch_f, sizeof(int32_t) * (size_t)(ncap + 1)));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_a, sizeof(int64_t) * 2 * (size_t)(nl + 1)));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_b, sizeof(int4) * (size_t)ucap));
+        GX_TRY(gx_ensure(ctx, ctx->scratch_d, sizeof(int4) * (size_t)ucap));
+        int64_t *nch = dptr<int64_t>(ctx->scratch_a), *uoff = nch + (nl + 1);
+        int4 *unit = dptr<int4>(ctx->scratch_b), *ucnt = dptr<int4>(ctx->scratch_d);
+        k_ns_nchunks<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, ncnt, nch);
+        GX_TRY(gx_exclusive_scan_i64(ctx, nch, uoff, nl + 1));
+        k_ns_units<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, ncnt, uoff, unit, dptr<int32_t>(ctx->split_cnt));
+        const unsigned g = (unsigned)(ctx->sm_count > 0 ? ctx->sm_count * 16 : 2432);  // grid-stride, 4 warps a block
+        k_ns_kinds<<<g, 128, 0, ctx->stream>>>(uoff + nl, unit, nstart, dptr<int32_t>(ctx->near_idx),
+                                               dptr<int32_t>(ctx->scratch_f), dptr<float4>(ctx->comhl),
+                                               dptr<float>(ctx->radius32), tw, tw2, ucnt);
+        k_ns_write<<<g, 128, 0, ctx->stream>>>(uoff + nl, unit, uoff, nstart, dptr<int32_t>(ctx->scratch_f), ucnt,
+                                               dptr<int32_t>(ctx->near_idx), ncnt, dptr<int32_t>(ctx->split_cnt),
+                                               dptr<unsigned long long>(ctx->split_tot));
+        ctx->launches += 4;
     }
     GX_CUDA(ctx, cudaGetLastError());
     return GX_OK;
@@ -1435,21 +1617,24 @@ __global__ void k_m2p_items_count(int64_t nl, const int32_t *split, int64_t *n) 
     n[a] = a == nl ? 0 : (split[2 * a] + P2P_K - 1) / P2P_K;
 }
 
+// one warp per leaf, lanes over its items: the widest halo leaves have ~1000 items
 __global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split,
                              const int64_t *off, int32_t *leaf, int64_t *qb, int32_t *nq, const int64_t *m2p_off,
                              int32_t *m2p_list) {
-    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (a >= nl) return;
-    int64_t s0 = start[a];
-    int64_t c = cnt ? cnt[a] : start[a + 1] - start[a];
-    int64_t it = off[a];
-    for (int64_t k = 0; k * P2P_K < c; k++, it++) {
-        leaf[it] = (int32_t)a;
-        qb[it] = s0 + k * P2P_K;
-        nq[it] = (int32_t)min((int64_t)P2P_K, c - k * P2P_K);
+    const int64_t s0 = start[a];
+    const int64_t c = cnt ? cnt[a] : start[a + 1] - start[a];
+    const int64_t it0 = off[a], np = (c + P2P_K - 1) / P2P_K;
+    for (int64_t k = lane; k < np; k += 32) {
+        leaf[it0 + k] = (int32_t)a;
+        qb[it0 + k] = s0 + k * P2P_K;
+        nq[it0 + k] = (int32_t)min((int64_t)P2P_K, c - k * P2P_K);
     }
-    const int64_t cm = split ? split[2 * a] : 0;
-    for (int64_t k = 0; k * P2P_K < cm; k++, it++) {
+    const int64_t cm = split ? split[2 * a] : 0, nm = (cm + P2P_K - 1) / P2P_K;
+    for (int64_t k = lane; k < nm; k += 32) {
+        const int64_t it = it0 + np + k;
         leaf[it] = (int32_t)a;
         qb[it] = s0 + c + k * P2P_K;
         nq[it] = -(int32_t)min((int64_t)P2P_K, cm - k * P2P_K);
@@ -1467,15 +1652,16 @@ __global__ void k_p2l_units_count(int64_t nl, const int32_t *split, int64_t *nun
 
 __global__ void k_p2l_units_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split,
                                  const int64_t *leaf_u, int32_t *uleaf, int64_t *ustart, int32_t *ulen) {
-    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // a warp per leaf
+    const int lane = threadIdx.x & 31;
     if (a >= nl) return;
     const int64_t s0 = start[a] + cnt[a] + split[2 * a];
     const int32_t c = split[2 * a + 1];
-    int64_t u = leaf_u[a];
-    for (int32_t k = 0; k * GX_P2L_UNIT < c; k++, u++) {
-        uleaf[u] = (int32_t)a;
-        ustart[u] = s0 + (int64_t)k * GX_P2L_UNIT;
-        ulen[u] = min(GX_P2L_UNIT, c - k * GX_P2L_UNIT);
+    const int64_t u0 = leaf_u[a];
+    for (int32_t k = lane; k * GX_P2L_UNIT < c; k += 32) {
+        uleaf[u0 + k] = (int32_t)a;
+        ustart[u0 + k] = s0 + (int64_t)k * GX_P2L_UNIT;
+        ulen[u0 + k] = min(GX_P2L_UNIT, c - k * GX_P2L_UNIT);
     }
 }
 
@@ -1624,7 +1810,7 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     GX_TRY(gx_ensure(ctx, I.qb, sizeof(int64_t) * (size_t)(tot[0] + 1)));
     GX_TRY(gx_ensure(ctx, I.nq, sizeof(int32_t) * (size_t)(tot[0] + 1)));
     if (split) GX_TRY(gx_ensure(ctx, ctx->m2p_list, sizeof(int32_t) * (size_t)(tot[3] + 1)));
-    k_items_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(
+    k_items_fill<<<gx_blocks(nl * 32, 256), 256, 0, ctx->stream>>>(
         nl, start, cnt, scnt, dptr<int64_t>(I.off), dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq),
         split ? dptr<int64_t>(ctx->m2p_off) : nullptr, split ? dptr<int32_t>(ctx->m2p_list) : nullptr);
     ctx->launches += 2;
@@ -1640,7 +1826,7 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
         GX_TRY(gx_ensure(ctx, PU.leaf, sizeof(int32_t) * (size_t)(npu + 1)));
         GX_TRY(gx_ensure(ctx, PU.start, sizeof(int64_t) * (size_t)(npu + 1)));
         GX_TRY(gx_ensure(ctx, PU.len, sizeof(int32_t) * (size_t)(npu + 1)));
-        k_p2l_units_fill<<<gx_blocks(nl, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, dptr<int64_t>(PU.leaf_u),
+        k_p2l_units_fill<<<gx_blocks(nl * 32, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, dptr<int64_t>(PU.leaf_u),
                                                                       dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
                                                                       dptr<int32_t>(PU.len));
         ctx->launches++;

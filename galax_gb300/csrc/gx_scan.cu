@@ -58,7 +58,7 @@ __global__ void k_scan_sums(const T *in, int64_t n, T *sums) {
 
 // In-place exclusive scan of `sums` (nb entries) by one block; writes the grand total.
 template <class T>
-__global__ void k_scan_single(T *sums, int64_t nb, T *total) {
+__device__ void scan_single_block(T *sums, int64_t nb, T *total) {
     __shared__ T tot;
     T carry = 0;
     for (int64_t base = 0; base < nb; base += SCAN_TILE) {
@@ -80,6 +80,11 @@ __global__ void k_scan_single(T *sums, int64_t nb, T *total) {
         __syncthreads();
     }
     if (threadIdx.x == 0 && total) *total = carry;
+}
+
+template <class T>
+__global__ void k_scan_single(T *sums, int64_t nb, T *total) {
+    scan_single_block<T>(sums, nb, total);
 }
 
 template <class T>
@@ -109,9 +114,14 @@ __device__ __forceinline__ int64_t dev_len(const int64_t *n_dev, int64_t n_add, 
     return n < n_cap ? n : n_cap;
 }
 
-__global__ void k_scan_sums_dn(const int64_t *in, const int64_t *n_dev, int64_t n_add, int64_t n_cap, int64_t *sums) {
+// blockIdx.y selects one of gridDim.y arrays: in + y * stride, out + y * stride, and
+// the block sums of array y at sums + y * (gridDim.x + 1)
+__global__ void k_scan_sums_dn(const int64_t *in, const int64_t *n_dev, int64_t n_add, int64_t n_cap, int64_t *sums,
+                               int64_t stride) {
     __shared__ int64_t tot;
     const int64_t n = dev_len(n_dev, n_add, n_cap);
+    in += blockIdx.y * stride;
+    sums += blockIdx.y * (int64_t)(gridDim.x + 1);
     int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
     int64_t s = 0;
     if (base < n)
@@ -123,12 +133,20 @@ __global__ void k_scan_sums_dn(const int64_t *in, const int64_t *n_dev, int64_t 
     if (threadIdx.x == 0) sums[blockIdx.x] = tot;
 }
 
+__global__ void k_scan_single_dn(int64_t *sums, int64_t nb, int64_t *total) {
+    const int64_t y = blockIdx.x;
+    scan_single_block<int64_t>(sums + y * (nb + 1), nb, total ? total + y : sums + y * (nb + 1) + nb);
+}
+
 __global__ void k_scan_apply_dn(const int64_t *in, int64_t *out, const int64_t *n_dev, int64_t n_add, int64_t n_cap,
-                                const int64_t *sums) {
+                                const int64_t *sums, int64_t stride) {
     __shared__ int64_t tot;
     const int64_t n = dev_len(n_dev, n_add, n_cap);
     int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
     if (base >= n) return;  // uniform per block
+    in += blockIdx.y * stride;
+    out += blockIdx.y * stride;
+    sums += blockIdx.y * (int64_t)(gridDim.x + 1);
     int64_t v[SCAN_ITEMS];
     int64_t s = 0;
     for (int k = 0; k < SCAN_ITEMS; k++) {
@@ -257,13 +275,19 @@ int gx_exclusive_scan_i64(gx_ctx *ctx, const int64_t *in, int64_t *out, int64_t 
 
 int gx_exclusive_scan_i64_devn(gx_ctx *ctx, const int64_t *in, int64_t *out, const int64_t *n_dev, int64_t n_add,
                                int64_t n_cap, int64_t *total_dev) {
-    if (n_cap <= 0) return GX_OK;
+    return gx_exclusive_scan_i64_devn_multi(ctx, in, out, 1, 0, n_dev, n_add, n_cap, total_dev);
+}
+
+int gx_exclusive_scan_i64_devn_multi(gx_ctx *ctx, const int64_t *in, int64_t *out, int m, int64_t stride,
+                                     const int64_t *n_dev, int64_t n_add, int64_t n_cap, int64_t *total_dev) {
+    if (n_cap <= 0 || m <= 0) return GX_OK;
     int64_t nb = (n_cap + SCAN_TILE - 1) / SCAN_TILE;
-    GX_TRY(gx_ensure(ctx, ctx->scratch_g, sizeof(int64_t) * (nb + 1)));
+    GX_TRY(gx_ensure(ctx, ctx->scratch_g, sizeof(int64_t) * (size_t)m * (nb + 1)));
     int64_t *sums = dptr<int64_t>(ctx->scratch_g);
-    k_scan_sums_dn<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(in, n_dev, n_add, n_cap, sums);
-    k_scan_single<int64_t><<<1, SCAN_THREADS, 0, ctx->stream>>>(sums, nb, total_dev ? total_dev : sums + nb);
-    k_scan_apply_dn<<<(unsigned)nb, SCAN_THREADS, 0, ctx->stream>>>(in, out, n_dev, n_add, n_cap, sums);
+    const dim3 grid((unsigned)nb, (unsigned)m);
+    k_scan_sums_dn<<<grid, SCAN_THREADS, 0, ctx->stream>>>(in, n_dev, n_add, n_cap, sums, stride);
+    k_scan_single_dn<<<(unsigned)m, SCAN_THREADS, 0, ctx->stream>>>(sums, nb, total_dev);
+    k_scan_apply_dn<<<grid, SCAN_THREADS, 0, ctx->stream>>>(in, out, n_dev, n_add, n_cap, sums, stride);
     ctx->launches += 3;
     GX_CUDA(ctx, cudaGetLastError());
     return GX_OK;
