@@ -193,6 +193,7 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->split_tot, &ctx->p2l_units.leaf, &ctx->p2l_units.start, &ctx->p2l_units.len,
                       &ctx->p2l_units.leaf_u, &ctx->p2l_part, &ctx->m2p_list, &ctx->m2p_off};
     for (DevBuf *b : bufs) free_buf(*b);
+    for (DevBuf &b : ctx->body_alt) free_buf(b);
     for (gx_tree_plan &t : ctx->tp_cache) gx_tree_plan_free(t);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);

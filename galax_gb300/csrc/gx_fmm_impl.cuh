@@ -1503,6 +1503,20 @@ __global__ void __launch_bounds__(128, 8) k_m2p_x2(int64_t n_list, const int32_t
     }
 }
 
+// cp.async of 16 bytes global -> shared through L1 (a P2L source leaf is read by the
+// units of many nearby target leaves), zero-filled when ok is false (no bytes are read
+// then; src must still be a valid address)
+__device__ __forceinline__ void cp_async16_zfill(void *dst_smem, const void *src, bool ok) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst_smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(ok ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+constexpr int P2L_RING = 4;  // rounds of P2L source bodies in flight per warp (three ahead)
+
 // P2L units, mixed form, p <= 5: lane tl of each half-warp takes source bodies tl and
 // tl + 16 of a source leaf as a pair, half h the unit's sources h, h + 2, ...; the
 // coefficient sums stay pairs until the end (pair halves, then the warp, in a fixed
@@ -1518,6 +1532,7 @@ __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_
     static_assert(P <= 5, "paired accumulators are sized for p <= 5");
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<float>(NC);
+    __shared__ __align__(16) float4 p2l_ring[4][P2L_RING][64];  // per warp: P2L_RING rounds x 64 bodies
     const int lane = threadIdx.x & 31;
     const int half = lane >> 4, tl = lane & 15;
     const int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1538,9 +1553,11 @@ __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_
 #pragma unroll
     for (int k = 0; k < NC; k++) acc[k] = f2splat(0.f);
     const int rounds = (nq + 1) >> 1;  // both halves run the same number of rounds
-    // round r: this half's source k = 2r + half; its first 32 bodies are requested one
-    // round ahead (leaves above 32 bodies load the rest in place)
-    auto fetch = [&](int r, float4 &pA, float4 &pB, int32_t &j0, int32_t &j1, float &ox, float &oy) {
+    // round r: this half's source k = 2r + half (its first 32 bodies: lane tl loads bodies
+    // tl and tl + 16).  They are copied global -> shared by cp.async P2L_RING - 1 rounds
+    // ahead, each lane reading back only its own copies, so the loads in flight hold no
+    // registers; leaves above 32 bodies load the rest in place.
+    auto src = [&](int r, int32_t &j0, int32_t &j1, float &ox, float &oy) {
         const int k = 2 * r + half;
         const int kk = k < nq ? k : 0;
         j0 = __shfl_sync(0xffffffffu, sb, kk);
@@ -1548,9 +1565,6 @@ __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_
         j1 = k < nq ? e1 : j0;  // the half without a source this round runs no body
         ox = __shfl_sync(0xffffffffu, shx, kk);
         oy = __shfl_sync(0xffffffffu, shy, kk);
-        const int32_t jA = j0 + tl, jB = j0 + tl + 16;
-        pA = jA < j1 ? pos[jA] : make_float4(0.f, 0.f, 0.f, 0.f);
-        pB = jB < j1 ? pos[jB] : make_float4(0.f, 0.f, 0.f, 0.f);
     };
     auto body_pair = [&](const float4 &pA, const float4 &pB, float ox, float oy) {
         // com_a - x_j = (com_a - com_s) - (x_j - com_s); an empty slot has m = 0 and
@@ -1563,29 +1577,37 @@ __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_
 #pragma unroll
         for (int q = 0; q < NC; q++) acc[q] = f2fma(mm, c[q], acc[q]);
     };
-    float4 cA = make_float4(0.f, 0.f, 0.f, 0.f), cB = cA;
-    int32_t c0 = 0, c1 = 0;
-    float cox = 0.f, coy = 0.f;
-    if (rounds > 0) fetch(0, cA, cB, c0, c1, cox, coy);
+    float4 *ring = &p2l_ring[threadIdx.x >> 5][0][0];
+    auto issue = [&](int r) {
+        if (r < rounds) {
+            int32_t j0, j1;
+            float ox, oy;
+            src(r, j0, j1, ox, oy);
+            const int32_t jA = j0 + tl, jB = j0 + tl + 16;
+            float4 *dst = ring + (r % P2L_RING) * 64 + lane;  // body A at lane, B at 32 + lane
+            cp_async16_zfill(dst, pos + (jA < j1 ? jA : 0), jA < j1);
+            cp_async16_zfill(dst + 32, pos + (jB < j1 ? jB : 0), jB < j1);
+        }
+        cp_async_commit();  // an empty group past the last round keeps the count uniform
+    };
+#pragma unroll
+    for (int r = 0; r < P2L_RING - 1; r++) issue(r);
     for (int r = 0; r < rounds; r++) {
-        float4 nA = make_float4(0.f, 0.f, 0.f, 0.f), nB = nA;
-        int32_t n0 = 0, n1 = 0;
-        float nox = 0.f, noy = 0.f;
-        if (r + 1 < rounds) fetch(r + 1, nA, nB, n0, n1, nox, noy);
-        if (c0 < c1) body_pair(cA, cB, cox, coy);
+        issue(r + P2L_RING - 1);
+        cp_async_wait<P2L_RING - 1>();  // round r's copies have landed
+        int32_t c0, c1;
+        float cox, coy;
+        src(r, c0, c1, cox, coy);
+        const float4 *slot = ring + (r % P2L_RING) * 64 + lane;
+        if (c0 < c1) body_pair(slot[0], slot[32], cox, coy);
         for (int32_t b0 = c0 + 32; b0 < c1; b0 += 32) {
             const int32_t jA = b0 + tl, jB = b0 + tl + 16;
             const float4 pA = jA < c1 ? pos[jA] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float4 pB = jB < c1 ? pos[jB] : make_float4(0.f, 0.f, 0.f, 0.f);
             body_pair(pA, pB, cox, coy);
         }
-        cA = nA;
-        cB = nB;
-        c0 = n0;
-        c1 = n1;
-        cox = nox;
-        coy = noy;
     }
+    cp_async_wait<0>();
     const bool single = leaf_u[a + 1] - leaf_u[a] == 1;
 #pragma unroll
     for (int q = 0; q < NC; q++) {

@@ -98,6 +98,7 @@ struct gx_ctx {
 
     // bodies (device, tree order)
     DevBuf x, y, vx, vy, m, ax, ay;
+    DevBuf body_alt[7];  // spare copies of x, y, vx, vy, m, ax, ay: the targets of a device sort's gather
     bool have_bodies = false;
 
     // REF lists, reference layout (built with the tree by gx_build_tree, lazily after

@@ -31,15 +31,31 @@ __device__ __forceinline__ uint64_t normalize_ref(double x, double lo, double hi
 // differ by at most 2^-51; times 2^21 (exact) that is 2^-30.  Hence when s = q * 2^21 lies
 // farther than 2^-29 from an integer, floor(s) = floor(RN(a/w) * 2^21) exactly; values
 // that near a cell boundary, and non-finite ones, take the correctly rounded division.
-// One multiply instead of a correctly rounded FP64 division per coordinate.
-__device__ __forceinline__ uint64_t normalize_dev(double x, double lo, double hi, double iw) {
-    if (iw > 0.0) {
-        const double s = __dmul_rn(__dmul_rn(__dsub_rn(x, lo), iw), 2097152.0);
-        if (s < 2097152.0 * 2.0 && s > -1.0) {      // finite and |t| < 2: the window of the bound
-            if (s <= 0.0) return 0ull;               // a <= 0 or RN(a/w) < 2^-21: the low cell
-            if (s >= 2097151.5) return 2097151ull;   // RN(a/w) 2^21 >= 2097151.49: the top cell
-            const double f = floor(s), fr = __dsub_rn(s, f);
-            if (fr > 0x1p-29 && fr < 1.0 - 0x1p-29) return (uint64_t)f;
+// One multiply instead of a correctly rounded FP64 division per coordinate.  iw21 =
+// iw * 2^21 (exact), so s = RN(a * iw21) = RN(a * iw) * 2^21 wherever RN(a * iw) is
+// normal; where it is not, s < 2^-29 and both take the division.  FP64 throughput on
+// this part is a small fraction of FP32, so the tests on s (the window, the end cells,
+// floor and the distance to the nearest integer) are integer operations on its bits,
+// each equal to the FP64 comparison it replaces: for 1 <= s < 2^22 with exponent e the
+// integer part is the significand shifted right by 52 - e and the fraction its low
+// 52 - e bits, so "fraction in (2^-29, 1 - 2^-29)" is "low bits in (2^(23-e),
+// 2^(52-e) - 2^(23-e))".
+__device__ __forceinline__ uint64_t normalize_dev(double x, double lo, double hi, double iw21) {
+    if (iw21 > 0.0) {
+        const double s = __dmul_rn(__dsub_rn(x, lo), iw21);
+        const int64_t b = __double_as_longlong(s);
+        const uint64_t mag = (uint64_t)b & 0x7fffffffffffffffull;
+        if (b <= 0) {                                            // s <= 0 (or a NaN with the sign bit)
+            if (mag < 0x3ff0000000000000ull) return 0ull;        // -1 < s <= 0: the low cell
+        } else if (b >= 0x413fffff80000000ll) {                  // s >= 2097151.5 (or +inf, NaN)
+            if (b < 0x4150000000000000ll) return 2097151ull;     // s < 2^22: the top cell
+        } else if (b < 0x3ff0000000000000ll) {                   // 0 < s < 1: cell 0 away from both ends
+            if (b > 0x3e20000000000000ll && b < 0x3fefffffff000000ll) return 0ull;  // 2^-29 < s < 1 - 2^-29
+        } else {                                                 // 1 <= s < 2097151.5
+            const int sh = 52 - ((int)(b >> 52) - 1023);         // 32 .. 52
+            const uint64_t sig = ((uint64_t)b & 0x000fffffffffffffull) | 0x0010000000000000ull;
+            const uint64_t fr = sig & ((1ull << sh) - 1ull), eps = 1ull << (sh - 29);
+            if (fr > eps && fr < (1ull << sh) - eps) return sig >> sh;
         }
     }
     return normalize_ref(x, lo, hi);
@@ -57,40 +73,55 @@ __device__ __forceinline__ uint64_t spread_dev(uint64_t v) {
 }
 
 __global__ void k_morton(const double *__restrict__ x, const double *__restrict__ y, int64_t n, double x0, double x1,
-                         double y0, double y1, double ixw, double iyw, uint64_t *__restrict__ keys,
+                         double y0, double y1, double ixw21, double iyw21, uint64_t *__restrict__ keys,
                          uint32_t *__restrict__ idx) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    keys[i] = spread_dev(normalize_dev(x[i], x0, x1, ixw)) | (spread_dev(normalize_dev(y[i], y0, y1, iyw)) << 1);
+    keys[i] = spread_dev(normalize_dev(x[i], x0, x1, ixw21)) | (spread_dev(normalize_dev(y[i], y0, y1, iyw21)) << 1);
     if (idx) idx[i] = (uint32_t)i;
 }
 
 }  // namespace
 
-// RN(1 / (hi - lo)) for the division-free normalisation, or 0 (the division path) when the
-// width is not a positive finite number whose reciprocal is a normal number
-double gx_inv_width(double lo, double hi) {
+// RN(1 / (hi - lo)) * 2^21 for the division-free normalisation, or 0 (the division path)
+// when the width is not a positive finite number whose reciprocal is a normal number with
+// a finite 2^21 multiple
+double gx_inv_width21(double lo, double hi) {
     const double w = hi - lo;
     if (!(w > 0.0) || !std::isfinite(w)) return 0.0;
-    const double iw = 1.0 / w;
-    return (std::isfinite(iw) && std::fpclassify(iw) == FP_NORMAL) ? iw : 0.0;
+    const double iw = 1.0 / w, iw21 = iw * 2097152.0;
+    return (std::isfinite(iw21) && std::fpclassify(iw) == FP_NORMAL) ? iw21 : 0.0;
 }
 
 void gx_launch_morton(gx_ctx *ctx, const double *x, const double *y, int64_t n, const double bounds[4], uint64_t *keys,
                       uint32_t *idx) {
     k_morton<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(x, y, n, bounds[0], bounds[1], bounds[2], bounds[3],
-                                                         gx_inv_width(bounds[0], bounds[1]),
-                                                         gx_inv_width(bounds[2], bounds[3]), keys, idx);
+                                                         gx_inv_width21(bounds[0], bounds[1]),
+                                                         gx_inv_width21(bounds[2], bounds[3]), keys, idx);
     ctx->launches++;
 }
 
 namespace {
 
-// gather of the seven body arrays (Tree::permute, lib.rs:146-161)
-__global__ void k_permute(const uint32_t *__restrict__ idx, int64_t n, const double *__restrict__ in,
-                          double *__restrict__ out) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = in[idx[i]];
+// gather of the seven body arrays (Tree::permute, lib.rs:146-161), na of them per
+// launch: the index read once per body and a body's loads in flight together.  The
+// launch's source arrays are meant to fit the L2 together (a gather from unsorted order
+// touches them at random; from the previous step's order, almost in sequence).
+struct Arrays7 {
+    const double *in[7];
+    double *out[7];
+};
+__global__ void k_permute7(const uint32_t *__restrict__ idx, int64_t n, int na, Arrays7 a) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = idx[i];
+    double v[7];
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+        if (k < na) v[k] = a.in[k][j];
+#pragma unroll
+    for (int k = 0; k < 7; k++)
+        if (k < na) a.out[k][i] = v[k];
 }
 
 __device__ __forceinline__ double fmin_rs(double a, double b) { return (a != a) ? b : ((b != b) ? a : (b < a ? b : a)); }
@@ -611,15 +642,22 @@ int gx_tree_build_device(gx_ctx *ctx, int64_t n, int64_t n_max, const double bou
             GX_CUDA(ctx, cudaMemcpyAsync(keys, keys_alt, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
             idx = idx_alt;
         }
-        // permute the seven arrays through scratch_d
-        GX_TRY(gx_ensure(ctx, ctx->scratch_d, sizeof(double) * n));
+        // permute the seven arrays into their spare copies, then swap them in; as many
+        // arrays per launch as fit in half of the 129 MB L2 together (all seven at 1M)
         DevBuf *arrs[7] = {&ctx->x, &ctx->y, &ctx->vx, &ctx->vy, &ctx->m, &ctx->ax, &ctx->ay};
-        for (DevBuf *a : arrs) {
-            k_permute<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(idx, n, dptr<double>(*a), dptr<double>(ctx->scratch_d));
+        const int per = (int)std::max<int64_t>(1, std::min<int64_t>(7, ((int64_t)64 << 20) / (8 * n)));
+        for (int k0 = 0; k0 < 7; k0 += per) {
+            const int na = std::min(per, 7 - k0);
+            Arrays7 a7{};
+            for (int k = 0; k < na; k++) {
+                GX_TRY(gx_ensure(ctx, ctx->body_alt[k0 + k], sizeof(double) * n));
+                a7.in[k] = dptr<double>(*arrs[k0 + k]);
+                a7.out[k] = dptr<double>(ctx->body_alt[k0 + k]);
+            }
+            k_permute7<<<gx_blocks(n, 256), 256, 0, ctx->stream>>>(idx, n, na, a7);
             ctx->launches++;
-            std::swap(a->p, ctx->scratch_d.p);
-            std::swap(a->bytes, ctx->scratch_d.bytes);
         }
+        for (int k = 0; k < 7; k++) std::swap(*arrs[k], ctx->body_alt[k]);
         GX_TRY(gx_ensure(ctx, ctx->perm, sizeof(uint32_t) * n));
         GX_CUDA(ctx, cudaMemcpyAsync(ctx->perm.p, idx, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
         GX_CUDA(ctx, cudaGetLastError());
