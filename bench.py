@@ -758,8 +758,9 @@ def run_ours(args, rank, world, local, pg):
                 "d2h_bytes_per_step": 2 * 8 * n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                      "frac": achieved / peak32 if peak32 else None, "traffic": P2P_TRAFFIC_1M if n == N_DEFAULT else None,
-                     "kernel": "k_p2p32_rows (P2P, packed FP32; timed on its own stream while it shares the SMs "
-                               "with M2L)",
+                     "kernel": "k_p2p32_rows (P2P, packed FP32; timed on its own stream, where for most of its run "
+                               "it shares the SMs with the far-field chain M2M, M2L, L2L, P2L; *_alone: started after "
+                               "that chain)",
                      "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)",
                      "kernel_ms": kms, "kernel_ms_alone": float(np.mean(k_alone)),
                      "achieved_alone": flops / (float(np.mean(k_alone)) * 1e-3) / 1e12,
