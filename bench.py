@@ -60,10 +60,17 @@ N_DEFAULT = 1_000_000
 # of two launches of a one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum:
 # 34.92 + 1.14 MB and 34.88 + 0.49 MB): the kernel works out of L2
 P2P_TRAFFIC_1M = 35.72e6
+# the same for k_p2p32_stream (the body-level P2L on, theta_b = 0.3): 50.4 + 4.1 MB and
+# 50.5 + 2.7 MB
+P2P_STREAM_TRAFFIC_1M = 53.85e6
 P, N_MAX, THETA = 4, 32, 0.5
 # leaf-level near-list split (M2P / P2L) of the ACCURATE forms: near leaf pairs that are
 # far on one side at this opening angle leave P2P
 THETA_W = 0.4
+# body-level P2L of the P2P pairs the split leaves: source bodies with
+# |x_j - com_a| theta_b > R_a join the target leaf's local expansion (0 = off); at 0.3
+# the error against the exact sum is that of the split alone (--sweep thetab)
+THETA_B = 0.3
 
 
 def _dist():
@@ -239,6 +246,7 @@ def run_uniform10k(G, presets, args, with_cpu: bool):
     gb = presets.uniform(n, seed=0)
     ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=P, eps64=0.1))
     ctx.set_near_split(args.theta_w)
+    ctx.set_body_split(args.theta_b)
     ctx.build_tree(gb, N_MAX, bounds)  # permutes gb into Morton order, as Tree::build does
     eps = presets.cli_softening(gb.x, gb.y)
     ctx.set_params(P, eps)
@@ -404,6 +412,7 @@ def run_disk_compact(G, presets, args):
     b = presets.disk(n, seed=args.seed + 3)
     ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 28, p=8, eps64=0.1))
     ctx.set_near_split(args.theta_w)
+    ctx.set_body_split(args.theta_b)
     ctx.build_tree(b, n_max, bounds)
     eps = presets.cli_softening(b.x, b.y)
     ctx.upload_bodies(b)
@@ -442,6 +451,7 @@ def run_build_only(args):
     ctx.set_params(P, presets.cli_softening(b.x, b.y))
     ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, THETA)
     ctx.set_near_split(args.theta_w)
+    ctx.set_body_split(args.theta_b)
     times, plan = [], []
     for _ in range(max(1, args.steps)):
         ctx.upload_bodies(b)  # unsorted order again: the sort does full work
@@ -569,13 +579,19 @@ def run_sweep_thetaw(args):
     idx = np.sort(np.random.default_rng(1234).choice(n, min(1000, n), replace=False))
     ex, ey = ctx.n2_sampled(idx)
     rows = []
-    grid = [(THETA, tw) for tw in (0.0, 0.3, 0.35, 0.4, 0.45, 0.5)]
-    grid += [(th, tw) for th in args.sweep_thetas for tw in (0.3, 0.35, 0.4) if th != THETA]
-    for theta, tw in grid:
+    if args.sweep == "thetab":
+        grid = [(THETA, tw, tb) for tw in (0.35, 0.4, 0.45) for tb in (0.0, 0.25, 0.3, 0.35)]
+    else:
+        grid = [(THETA, tw, 0.0) for tw in (0.0, 0.3, 0.35, 0.4, 0.45, 0.5)]
+        grid += [(th, tw, 0.0) for th in args.sweep_thetas for tw in (0.3, 0.35, 0.4) if th != THETA]
+    for theta, tw, tb in grid:
         ctx.set_near_split(tw)
+        ctx.set_body_split(tb)
         # the FP64 form has the mixed form's error (to the third digit); it is timed at the
         # headline opening angle only
-        forms = (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)) if theta == THETA else (("mixed", G.PREC_MIXED),)
+        forms = (("mixed", G.PREC_MIXED),)
+        if theta == THETA and args.sweep != "thetab":
+            forms += (("fp64", G.PREC_FP64),)
         for name, prec in forms:
             ctx.set_mode(G.MODE_ACCURATE, prec, theta)
             ctx.forces_resident()
@@ -584,18 +600,20 @@ def run_sweep_thetaw(args):
             ctx.download_bodies(r)
             far, near, inter = ctx.plan_info()
             m2p, p2l = ctx.plan_split_info()
-            row = {"theta": theta, "theta_w": tw, "form": name, "ms": float(np.mean(ms)),
+            moved, body_evals = ctx.plan_body_split_info()
+            row = {"theta": theta, "theta_w": tw, "theta_b": tb, "p2p_moved_to_body_p2l": moved,
+                   "body_p2l_evaluations": body_evals, "form": name, "ms": float(np.mean(ms)),
                    "p2p_kernel_ms": float(np.mean(kms)),
                    "pass_ms": ctx.last_timings().tolist(), "bodies_per_s": n / (float(np.mean(ms)) * 1e-3),
                    "far_pairs": far, "near_p2p_leaf_pairs": near, "m2p_leaf_pairs": m2p, "p2l_leaf_pairs": p2l,
-                   "p2p_interactions": inter}
+                   "p2p_interactions": inter - moved}
             if name == "mixed":
                 _, kal = ctx.bench_forces(5, True, 2)
                 row["p2p_kernel_ms_alone"] = float(np.mean(kal))
             row.update(_err_stats(r.ax[idx], r.ay[idx], ex, ey))
             rows.append(row)
     ctx.close()
-    print(json.dumps({"sweep": "theta_w", "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "seed": args.seed,
+    print(json.dumps({"sweep": "theta_w" if args.sweep != "thetab" else "theta_b", "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "seed": args.seed,
                       "rows": rows}), flush=True)
     return 0
 
@@ -619,6 +637,7 @@ def run_ours(args, rank, world, local, pg):
     nn, nl, nlev, _ = ctx.tree_info()
 
     ctx.set_near_split(args.theta_w)  # ACCURATE forms only; REF keeps the reference's lists
+    ctx.set_body_split(args.theta_b)
     forms = [("mixed", G.MODE_ACCURATE, G.PREC_MIXED), ("fp64", G.MODE_ACCURATE, G.PREC_FP64),
              ("ref_fp64", G.MODE_REF, G.PREC_FP64)]
     res = {}
@@ -641,9 +660,12 @@ def run_ours(args, rank, world, local, pg):
         if sampler is not None:
             clocks = sampler.stop()
         far, near, inter = ctx.plan_info()
+        moved, body_evals = ctx.plan_body_split_info() if mode == G.MODE_ACCURATE else (0, 0)
         bb = G.Bodies.new(n)
         ctx.download_bodies(bb)
-        res[name] = dict(ms=ms, kms=kms, plan_s=plan_s, far=far, near=near, inter=inter,
+        # P2P interactions left after the body-level P2L moved `moved` of them
+        res[name] = dict(ms=ms, kms=kms, plan_s=plan_s, far=far, near=near, inter=inter - moved, moved=moved,
+                         body_evals=body_evals,
                          launches=ctx.last_launch_count(), passes=ctx.last_timings().tolist(),
                          ax=bb.ax.copy(), ay=bb.ay.copy(), steps=steps)
         if name == "ref_fp64":
@@ -750,17 +772,20 @@ def run_ours(args, rank, world, local, pg):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed: FP32 P2M/M2L/L2L/L2P/P2P, FP64 state)",
         "data": "synthetic (seeded Plummer preset: a=1, r<=10a, equal masses 1/N)",
         "config": {"workload": f"plummer N={n}, p={P}, n_max={N_MAX}, one force evaluation per step, static tree",
-                   "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "theta_w": args.theta_w, "mode": "ACCURATE",
+                   "n": n, "p": P, "n_max": N_MAX, "theta": THETA, "theta_w": args.theta_w,
+                   "theta_b": args.theta_b, "mode": "ACCURATE",
                    "eps": eps,
                    "l2": "flushed (256 MB write) before every step, outside its timed interval",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "bodies/s", "h2d_bytes_per_step": 3 * 8 * n,
                 "d2h_bytes_per_step": 2 * 8 * n},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
-                     "frac": achieved / peak32 if peak32 else None, "traffic": P2P_TRAFFIC_1M if n == N_DEFAULT else None,
-                     "kernel": "k_p2p32_rows (P2P, packed FP32; timed on its own stream, where for most of its run "
-                               "it shares the SMs with the far-field chain M2M, M2L, L2L, P2L; *_alone: started after "
-                               "that chain)",
+                     "frac": achieved / peak32 if peak32 else None,
+                     "traffic": (P2P_STREAM_TRAFFIC_1M if args.theta_b > 0 else P2P_TRAFFIC_1M)
+                     if n == N_DEFAULT and args.theta_w == THETA_W and args.theta_b in (0.0, THETA_B) else None,
+                     "kernel": ("k_p2p32_stream" if args.theta_b > 0 else "k_p2p32_rows") +
+                               " (P2P, packed FP32; timed on its own stream, where for most of its run it shares the "
+                               "SMs with the far-field chain M2M, M2L, L2L, P2L; *_alone: started after that chain)",
                      "peak_source": "FP32 FMA peak measured in this run (gx_probe_fp32_tflops)",
                      "kernel_ms": kms, "kernel_ms_alone": float(np.mean(k_alone)),
                      "achieved_alone": flops / (float(np.mean(k_alone)) * 1e-3) / 1e12,
@@ -772,6 +797,7 @@ def run_ours(args, rank, world, local, pg):
                       "err_median": r["err_median"], "err_p99": r["err_p99"], "err_mag_mean": r["err_mag_mean"],
                       "err_mag_max": r["err_mag_max"], "plan_s": r["plan_s"],
                       "far_pairs": r["far"], "near_leaf_pairs": r["near"], "p2p_interactions": r["inter"],
+                      "p2p_moved_to_body_p2l": r["moved"], "body_p2l_evaluations": r["body_evals"],
                       "pass_ms": dict(zip(["total", "prepare", "p2m", "m2m", "m2l", "l2l", "l2p_p2p"], r["passes"]))}
                   for k, r in res.items()},
         "mixed_vs_fp64": {"speedup": float(np.mean(res["fp64"]["ms"])) / float(np.mean(mix["ms"])),
@@ -809,11 +835,12 @@ def main():
     ap.add_argument("--adj-k", type=lambda s: [int(v) for v in s.split(",")], default=[10, 22, 50, 1])
     ap.add_argument("--fd-dirs", type=int, default=16)
     ap.add_argument("--fd-dirs-1m", type=int, default=8)
-    ap.add_argument("--sweep", choices=["disk", "theta", "thetaw"], default=None)
+    ap.add_argument("--sweep", choices=["disk", "theta", "thetaw", "thetab"], default=None)
     ap.add_argument("--build-only", action="store_true")
     ap.add_argument("--sweep-n", type=int, default=4_000_000)
     ap.add_argument("--no-disk", action="store_true")
     ap.add_argument("--theta-w", type=float, default=THETA_W)
+    ap.add_argument("--theta-b", type=float, default=THETA_B)
     ap.add_argument("--sweep-thetas", type=lambda v: [float(x) for x in v.split(",")], default=[0.55, 0.6])
     ap.add_argument("--hbm-budget-gb", type=float, default=32.0)
     args = ap.parse_args()
@@ -827,7 +854,7 @@ def main():
             return run_sweep_disk(args) if rank == 0 else 0
         if args.sweep == "theta":
             return run_sweep_theta(args) if rank == 0 else 0
-        if args.sweep == "thetaw":
+        if args.sweep in ("thetaw", "thetab"):
             return run_sweep_thetaw(args) if rank == 0 else 0
         if args.build_only:
             return run_build_only(args) if rank == 0 else 0

@@ -79,6 +79,8 @@ def lib():
         "gx_set_mode": (C.c_int, [_VP, C.c_int, C.c_int, C.c_double]),
         "gx_set_params": (C.c_int, [_VP, C.c_uint32, C.c_double]),
         "gx_set_near_split": (C.c_int, [_VP, C.c_double]),
+        "gx_set_body_split": (C.c_int, [_VP, C.c_double]),
+        "gx_plan_body_split_info": (C.c_int, [_VP, _I64, _I64]),
         "gx_plan_split_info": (C.c_int, [_VP, _I64, _I64]),
         "gx_upload_tree": (C.c_int, [_VP, C.c_int64, C.c_int64, _D, _D, _D, _D, _D, _D, _I64, _I64, _I32, _I32, _U8,
                                      _U32, _U8, _U32, _U8]),
@@ -304,6 +306,20 @@ class GpuContext:
         """(M2P leaf pairs, P2L leaf pairs) of the current ACCURATE plan."""
         a, b = C.c_int64(), C.c_int64()
         self._check(lib().gx_plan_split_info(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_body_split(self, theta_b: float) -> None:
+        """Body-level P2L of the P2P pairs the near-list split leaves: a source body far
+        enough from the target leaf's COM (|x_j - com_a| theta_b > R_a) joins its local
+        expansion instead of P2P (needs theta_w > 0 and leaves of at most 32 bodies; 0
+        turns it off)."""
+        self._check(lib().gx_set_body_split(self._h, float(theta_b)))
+
+    def plan_body_split_info(self):
+        """(P2P interactions moved to body-level P2L, body-level P2L evaluations) of the
+        current ACCURATE plan."""
+        a, b = C.c_int64(), C.c_int64()
+        self._check(lib().gx_plan_body_split_info(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
     # -- trees

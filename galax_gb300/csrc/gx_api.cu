@@ -191,7 +191,8 @@ int gx_destroy(gx_ctx *ctx) {
                       &ctx->m2l_units.node, &ctx->m2l_units.start, &ctx->m2l_units.len, &ctx->m2l_units.node_u,
                       &ctx->m2l_part, &ctx->plan_ctr, &ctx->tree_state, &ctx->m2l_cnt, &ctx->split_cnt,
                       &ctx->split_tot, &ctx->p2l_units.leaf, &ctx->p2l_units.start, &ctx->p2l_units.len,
-                      &ctx->p2l_units.leaf_u, &ctx->p2l_part, &ctx->m2p_list, &ctx->m2p_off};
+                      &ctx->p2l_units.leaf_u, &ctx->p2l_units.body_u, &ctx->p2l_part, &ctx->m2p_list,
+                      &ctx->m2p_off, &ctx->p2p_mask, &ctx->body_off32};
     for (DevBuf *b : bufs) free_buf(*b);
     for (DevBuf &b : ctx->body_alt) free_buf(b);
     for (gx_tree_plan &t : ctx->tp_cache) gx_tree_plan_free(t);
@@ -226,6 +227,14 @@ int gx_set_near_split(gx_ctx *ctx, double theta_w) {
     if (!(theta_w >= 0.0 && theta_w < 2.0)) return gx_fail(ctx, GX_ERR_INVALID_ARG, "theta_w must be in [0, 2)");
     if (theta_w != ctx->theta_w) ctx->plan_acc_valid = false;
     ctx->theta_w = theta_w;
+    return GX_OK;
+}
+
+int gx_set_body_split(gx_ctx *ctx, double theta_b) {
+    GX_TRY(check_ctx(ctx));
+    if (!(theta_b >= 0.0 && theta_b < 2.0)) return gx_fail(ctx, GX_ERR_INVALID_ARG, "theta_b must be in [0, 2)");
+    if (theta_b != ctx->theta_b) ctx->plan_acc_valid = false;
+    ctx->theta_b = theta_b;
     return GX_OK;
 }
 
@@ -568,6 +577,7 @@ static int ensure_plan(gx_ctx *ctx) {
             GX_TRY(gx_plan_accurate(ctx));
             if (ctx->theta_w > 0.0) GX_TRY(gx_plan_near_split(ctx));
             GX_TRY(gx_plan_items(ctx, true));
+            GX_TRY(gx_plan_body_masks(ctx));
             ctx->plan_theta_w = ctx->theta_w;
         }
     } else {
@@ -593,6 +603,43 @@ int gx_plan_split_info(gx_ctx *ctx, int64_t *n_m2p_pairs, int64_t *n_p2l_pairs) 
     const bool on = ctx->mode == GX_MODE_ACCURATE && ctx->theta_w > 0.0;
     if (n_m2p_pairs) *n_m2p_pairs = on ? ctx->n_m2p_pairs : 0;
     if (n_p2l_pairs) *n_p2l_pairs = on ? ctx->n_p2l_pairs : 0;
+    return GX_OK;
+}
+
+int gx_plan_body_split_info(gx_ctx *ctx, int64_t *n_p2p_moved, int64_t *n_body_p2l) {
+    GX_TRY(check_ctx(ctx));
+    GX_TRY(ensure_plan(ctx));
+    int64_t moved = 0, evals = 0;
+    if (ctx->plan_body_split && gx_body_split_on(ctx)) {
+        // from host copies of the P2P items and their masks: a masked body of row (a <- s)
+        // moves |a| interactions to one body-P2L evaluation
+        const gx_ctx::Items &I = ctx->items_acc;
+        const int64_t nn = ctx->n_nodes;
+        std::vector<int32_t> leaf((size_t)I.n + 1), nq((size_t)I.n + 1), bs((size_t)nn), be((size_t)nn);
+        std::vector<int64_t> qb((size_t)I.n + 1);
+        if (I.n > 0) {
+            GX_CUDA(ctx, cudaMemcpyAsync(leaf.data(), I.leaf.p, 4 * I.n, cudaMemcpyDeviceToHost, ctx->stream));
+            GX_CUDA(ctx, cudaMemcpyAsync(nq.data(), I.nq.p, 4 * I.n, cudaMemcpyDeviceToHost, ctx->stream));
+            GX_CUDA(ctx, cudaMemcpyAsync(qb.data(), I.qb.p, 8 * I.n, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        GX_CUDA(ctx, cudaMemcpyAsync(bs.data(), ctx->bs.p, 4 * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaMemcpyAsync(be.data(), ctx->be.p, 4 * nn, cudaMemcpyDeviceToHost, ctx->stream));
+        const size_t nm = ctx->p2p_mask.bytes / 4;
+        std::vector<uint32_t> mask(nm);
+        GX_CUDA(ctx, cudaMemcpyAsync(mask.data(), ctx->p2p_mask.p, 4 * nm, cudaMemcpyDeviceToHost, ctx->stream));
+        GX_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int64_t it = 0; it < I.n; it++) {
+            if (nq[it] <= 0) continue;
+            const int64_t nt = be[leaf[it]] - bs[leaf[it]];
+            for (int k = 0; k < nq[it]; k++) {
+                const int64_t c = __builtin_popcount(mask[qb[it] + k]);
+                evals += c;
+                moved += c * nt;
+            }
+        }
+    }
+    if (n_p2p_moved) *n_p2p_moved = moved;
+    if (n_body_p2l) *n_body_p2l = evals;
     return GX_OK;
 }
 

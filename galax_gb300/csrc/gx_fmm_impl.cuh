@@ -817,7 +817,8 @@ __global__ void __launch_bounds__(128) k_p2p64_items(int64_t n_items, const int3
                                                      const double *__restrict__ x, const double *__restrict__ y,
                                                      const double *__restrict__ m, const int32_t *__restrict__ bs,
                                                      const int32_t *__restrict__ be, const int32_t *__restrict__ src_idx,
-                                                     double eps2, int tchunks, double2 *__restrict__ part) {
+                                                     const uint32_t *__restrict__ p2p_mask, double eps2, int tchunks,
+                                                     double2 *__restrict__ part) {
     __shared__ double3 sb[4][32];
     int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -829,6 +830,8 @@ __global__ void __launch_bounds__(128) k_p2p64_items(int64_t n_items, const int3
     int32_t t0 = bs[leaf], t1 = be[leaf];
     int sl = lane < nq ? src_idx[qb + lane] : -1;
     int sbeg = sl >= 0 ? bs[sl] : 0, send = sl >= 0 ? be[sl] : 0;
+    // the body-level P2L (p2p_mask != null): a row's masked bodies are skipped here
+    const uint32_t skip = (p2p_mask && sl >= 0) ? p2p_mask[qb + lane] : 0u;
     auto fetch = [&](int k, int sc) -> double3 {
         int s0 = __shfl_sync(0xffffffffu, sbeg, k) + sc, s1 = __shfl_sync(0xffffffffu, send, k);
         int j = s0 + lane;
@@ -844,6 +847,7 @@ __global__ void __launch_bounds__(128) k_p2p64_items(int64_t n_items, const int3
             for (int k = 0; k < nq; k++) {
                 int s0 = __shfl_sync(0xffffffffu, sbeg, k), s1 = __shfl_sync(0xffffffffu, send, k);
                 int srcl = __shfl_sync(0xffffffffu, sl, k);
+                const uint32_t sk = __shfl_sync(0xffffffffu, skip, k);
                 for (int sc = 0; sc < s1 - s0; sc += 32) {
                     double3 nxt;
                     if (sc + 32 < s1 - s0) nxt = fetch(k, sc + 32);
@@ -859,6 +863,16 @@ __global__ void __launch_bounds__(128) k_p2p64_items(int64_t n_items, const int3
                             double ir = rsqrt(dx * dx + dy * dy + eps2);
                             double f = bb.z * (ir * ir * ir);
                             if (s0 + sc + kk == i) f = 0.0;
+                            accx += f * dx;
+                            accy += f * dy;
+                        }
+                    } else if (sk) {
+                        for (int kk = 0; kk < ns; kk++) {
+                            if ((sk >> kk) & 1u) continue;  // leaves of at most 32 bodies: sc = 0
+                            double3 bb = sb[w][kk];
+                            double dx = bb.x - xi, dy = bb.y - yi;
+                            double ir = rsqrt(dx * dx + dy * dy + eps2);
+                            double f = bb.z * (ir * ir * ir);
                             accx += f * dx;
                             accy += f * dy;
                         }
@@ -1240,6 +1254,170 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
     }
 }
 
+// The near field of k_p2p32_rows with the body-level P2L (leaves of at most 32 bodies):
+// row k of an item keeps the bodies of its source leaf outside the plan's mask (the
+// masked ones went to the target leaf's local expansion).  The self row runs first, as
+// the scalar own row of k_p2p32_rows; the other rows' kept bodies are laid out as one
+// stream per item in shared memory (entry (row << 5) | body, in row and body order) and
+// computed 32 at a time with the packed quads of k_p2p32_rows, the last chunk padded with
+// zero-mass sources far away (r^-3 underflows to 0).  With empty masks the stream is
+// every body of every row, so the same kernel serves the plain split.
+__global__ void __launch_bounds__(128, 8) k_p2p32_stream(
+    int64_t n_items, const int32_t *__restrict__ item_leaf, const int64_t *__restrict__ item_qb,
+    const int32_t *__restrict__ item_nq, const float4 *__restrict__ pos, const double *__restrict__ comx,
+    const double *__restrict__ comy, const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+    const int32_t *__restrict__ src_idx, const uint32_t *__restrict__ p2p_mask, float eps2,
+    float2 *__restrict__ part) {
+    __shared__ __align__(16) float sx[4][32], sy[4][32], sm[4][32];
+    __shared__ __align__(16) int4 meta[4][32];  // per source leaf: begin, end, shift x, shift y (FP32 bits)
+    __shared__ uint16_t strm[4][32 * 32];       // the item's kept bodies: (row << 5) | body
+    const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const int half = lane >> 4, tl = lane & 15;  // lane: targets tl and tl + 16, source quads of its half
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const float4 far4 = make_float4(1e18f, 1e18f, 0.f, 0.f);
+    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
+        const int32_t leaf = item_leaf[it];
+        const int nq = item_nq[it];
+        if (nq < 0) continue;  // an M2P item of the near-list split (k_m2p)
+        const int32_t t0 = bs[leaf], t1 = be[leaf];
+        bool own_lane = false;
+        uint32_t keep = 0;
+        __syncwarp();  // the previous item's reads of meta[w] and strm[w] are done
+        if (lane < nq) {
+            const int64_t q = item_qb[it] + lane;
+            const int32_t sl = src_idx[q];
+            const int32_t b0 = bs[sl], b1 = be[sl];
+            const double tcx = comx[leaf], tcy = comy[leaf];
+            meta[w][lane] = make_int4(b0, b1, __float_as_int((float)(comx[sl] - tcx)),
+                                      __float_as_int((float)(comy[sl] - tcy)));
+            own_lane = sl == leaf;
+            const int ns = b1 - b0;
+            const uint32_t all = ns >= 32 ? full : ((1u << ns) - 1u);
+            keep = own_lane ? 0u : (all & ~p2p_mask[q]);
+        }
+        const unsigned ownm = __ballot_sync(full, own_lane);
+        const int kown = ownm ? __ffs(ownm) - 1 : -1;
+        // exclusive scan of the rows' kept counts; T = the stream's length
+        const int c = __popc(keep);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int excl = incl - c, T = __shfl_sync(full, incl, 31);
+        for (int k = 0; k < nq; k++) {
+            const uint32_t mk = __shfl_sync(full, keep, k);
+            const int ek = __shfl_sync(full, excl, k);
+            if ((mk >> lane) & 1u) strm[w][ek + __popc(mk & lt)] = (uint16_t)((k << 5) | lane);
+        }
+        __syncwarp();
+        const int32_t iA = t0 + tl, iB = t0 + tl + 16;
+        const float4 mA = iA < t1 ? pos[iA] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 mB = iB < t1 ? pos[iB] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const uint64_t XA = pk2(mA.x, mA.x), YA = pk2(mA.y, mA.y), XB = pk2(mB.x, mB.x), YB = pk2(mB.y, mB.y);
+        const uint64_t E2 = pk2(eps2, eps2);
+        uint64_t AXA = 0, AYA = 0, AXB = 0, AYB = 0;
+        float sxA = 0.f, syA = 0.f, sxB = 0.f, syB = 0.f;
+        if (kown >= 0) {
+            // the self row: gather, scalar, each half its own quads, the body itself excluded
+            const int4 mo = meta[w][kown];
+            const int j = mo.x + lane;
+            const float4 v = j < mo.y ? pos[j] : far4;
+            __syncwarp();
+            sx[w][lane] = v.x;
+            sy[w][lane] = v.y;
+            sm[w][lane] = v.z;
+            __syncwarp();
+            const int ns = mo.y - mo.x;
+            float xa, ya, xb, yb, d;
+            upk2(XA, xa, d);
+            upk2(YA, ya, d);
+            upk2(XB, xb, d);
+            upk2(YB, yb, d);
+            for (int q = 0; q < 4; q++)
+                for (int u = 0; u < 4; u++) {
+                    const int kk = 8 * q + 4 * half + u;
+                    if (kk >= ns) continue;
+                    const float xj = sx[w][kk], yj = sy[w][kk], mj = sm[w][kk];
+                    float dx = xj - xa, dy = yj - ya;
+                    float ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                    float fk = mj * (ir * ir * ir);
+                    fk = mo.x + kk == iA ? 0.f : fk;
+                    sxA = fmaf(fk, dx, sxA);
+                    syA = fmaf(fk, dy, syA);
+                    dx = xj - xb;
+                    dy = yj - yb;
+                    ir = rsqrt_fast(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                    fk = mj * (ir * ir * ir);
+                    fk = mo.x + kk == iB ? 0.f : fk;
+                    sxB = fmaf(fk, dx, sxB);
+                    syB = fmaf(fk, dy, syB);
+                }
+        }
+        // the stream, 32 sources at a time (this lane stages position ch * 32 + lane)
+        auto fetch = [&](int p) -> float4 {
+            if (p >= T) return far4;
+            const int e = strm[w][p];
+            const int4 mo = meta[w][e >> 5];
+            float4 v = pos[mo.x + (e & 31)];
+            v.x += __int_as_float(mo.z);
+            v.y += __int_as_float(mo.w);
+            return v;
+        };
+        const int nch = (T + 31) >> 5;
+        float4 cur = nch > 0 ? fetch(lane) : far4;
+        for (int ch = 0; ch < nch; ch++) {
+            const float4 nxt = ch + 1 < nch ? fetch((ch + 1) * 32 + lane) : far4;
+            __syncwarp();
+            sx[w][lane] = cur.x;
+            sy[w][lane] = cur.y;
+            sm[w][lane] = cur.z;
+            __syncwarp();
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int kk = 8 * q + 4 * half;
+                float4 X = *reinterpret_cast<const float4 *>(&sx[w][kk]);
+                float4 Y = *reinterpret_cast<const float4 *>(&sy[w][kk]);
+                float4 Mq = *reinterpret_cast<const float4 *>(&sm[w][kk]);
+                const uint64_t X0 = pk2(X.x, X.y), X1 = pk2(X.z, X.w), Y0 = pk2(Y.x, Y.y), Y1 = pk2(Y.z, Y.w);
+                const uint64_t M0 = pk2(Mq.x, Mq.y), M1 = pk2(Mq.z, Mq.w);
+                auto pair = [&](uint64_t XS, uint64_t YS, uint64_t MS, uint64_t XI, uint64_t YI, uint64_t &AX,
+                                uint64_t &AY) {
+                    uint64_t dx = sub2(XS, XI), dy = sub2(YS, YI);
+                    uint64_t r = fma2(dx, dx, fma2(dy, dy, E2));
+                    float ra, rb;
+                    upk2(r, ra, rb);
+                    uint64_t ir = pk2(rsqrt_fast(ra), rsqrt_fast(rb));
+                    uint64_t fq = mul2(MS, mul2(mul2(ir, ir), ir));
+                    AX = fma2(fq, dx, AX);
+                    AY = fma2(fq, dy, AY);
+                };
+                pair(X0, Y0, M0, XA, YA, AXA, AYA);
+                pair(X0, Y0, M0, XB, YB, AXB, AYB);
+                pair(X1, Y1, M1, XA, YA, AXA, AYA);
+                pair(X1, Y1, M1, XB, YB, AXB, AYB);
+            }
+            cur = nxt;
+        }
+        float a0, a1, b0, b1, c0, c1, e0, e1;
+        upk2(AXA, a0, a1);
+        upk2(AYA, b0, b1);
+        upk2(AXB, c0, c1);
+        upk2(AYB, e0, e1);
+        float xA = (a0 + a1) + sxA, yA = (b0 + b1) + syA, xB = (c0 + c1) + sxB, yB = (e0 + e1) + syB;
+        // the two halves hold the same targets over different sources: half 0 + half 1
+        const float oxA = __shfl_xor_sync(full, xA, 16), oyA = __shfl_xor_sync(full, yA, 16);
+        const float oxB = __shfl_xor_sync(full, xB, 16), oyB = __shfl_xor_sync(full, yB, 16);
+        float2 res;
+        if (half == 0) res = make_float2(xA + oxA, yA + oyA);  // target tl
+        else res = make_float2(oxB + xB, oyB + yB);             // target tl + 16 (half 0's part first)
+        part[it * 32 + lane] = res;
+    }
+}
+
 // ---------------------------------------------------------------- M2P / P2L
 // The leaf-level split of the ACCURATE near lists (theta_w > 0): a near leaf pair whose
 // target bodies are all far from the source leaf takes the source's multipole at each
@@ -1524,7 +1702,7 @@ constexpr int P2L_RING = 4;  // rounds of P2L source bodies in flight per warp (
 template <int P>
 __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_t *__restrict__ uleaf,
                                                 const int64_t *__restrict__ ustart, const int32_t *__restrict__ ulen,
-                                                const int64_t *__restrict__ leaf_u,
+                                                const int64_t *__restrict__ leaf_u, const int64_t *__restrict__ body_u,
                                                 const int32_t *__restrict__ src_idx, const float4 *__restrict__ pos,
                                                 const double *__restrict__ comx, const double *__restrict__ comy,
                                                 const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
@@ -1539,6 +1717,7 @@ __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_
     if (u >= n_units) return;
     const int32_t a = uleaf[u];
     const int nq = ulen[u];
+    if (nq < 0) return;  // a body-level unit (k_p2l_body_x2)
     int32_t sb = 0, se = 0;
     float shx = 0.f, shy = 0.f;
     if (lane < nq) {
@@ -1608,7 +1787,138 @@ __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_
         }
     }
     cp_async_wait<0>();
-    const bool single = leaf_u[a + 1] - leaf_u[a] == 1;
+    const bool single = (leaf_u[a + 1] - leaf_u[a]) + (body_u ? body_u[a + 1] - body_u[a] : 0) == 1;
+#pragma unroll
+    for (int q = 0; q < NC; q++) {
+        float lo, hi;
+        upk2(acc[q].v, lo, hi);
+        const float v = warp_sum_t<float>(lo + hi);
+        if (lane == (q & 31)) {
+            if (single) Lf[(int64_t)a * NS + q] -= v;
+            else ppart[u * NS + q] = v;
+        }
+    }
+}
+
+// Body-level P2L units, mixed form, p <= 5: a unit is up to GX_BODY_UNIT consecutive
+// P2P rows (a <- s) of one target leaf with the plan's masks.  Each lane takes rows lane
+// and lane + 32: it loads the row, and after a warp scan of the rows' mask counts writes
+// its masked bodies to the unit's stream in shared memory (entry (row << 5) | body, row
+// and body order).  The stream is taken two bodies per lane, 64 at a time (positions
+// c + lane and c + 32 + lane), each with its row's com_a - com_s; a padding slot has zero
+// mass at a unit offset.  Writes like k_p2l_x2 (the leaf's units are summed in unit
+// order, or a leaf with one unit subtracts its sum from its local directly).
+template <int P>
+__global__ void __launch_bounds__(128, 6) k_p2l_body_x2(int64_t u_base, int64_t n_units,
+                                                     const int32_t *__restrict__ uleaf,
+                                                     const int64_t *__restrict__ ustart,
+                                                     const int32_t *__restrict__ ulen,
+                                                     const int64_t *__restrict__ leaf_u,
+                                                     const int64_t *__restrict__ body_u,
+                                                     const int32_t *__restrict__ src_idx,
+                                                     const uint32_t *__restrict__ p2p_mask,
+                                                     const float4 *__restrict__ pos, const double *__restrict__ comx,
+                                                     const double *__restrict__ comy, const int32_t *__restrict__ bs,
+                                                     float eps2, float *__restrict__ Lf, float *__restrict__ ppart) {
+    static_assert(P <= 5, "paired accumulators are sized for p <= 5");
+    static_assert(GX_BODY_UNIT == 64, "two rows per lane");
+    constexpr int NC = nc2(P);
+    constexpr int NS = row_stride<float>(NC);
+    __shared__ __align__(16) float2 rsh[4][GX_BODY_UNIT];  // per row: com_a - com_s in FP32
+    __shared__ int32_t rb0[4][GX_BODY_UNIT];               // per row: the source leaf's first body
+    __shared__ uint16_t strm[4][GX_BODY_UNIT * 32];        // the unit's masked bodies: (row << 5) | body
+    const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t wu = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (wu >= n_units) return;
+    const int64_t u = u_base + wu;  // the body-level units follow the leaf-level ones
+    const int raw = ulen[u];
+    if (raw >= 0) return;  // a leaf-level unit (k_p2l_x2)
+    const int nq = -raw;
+    const int32_t a = uleaf[u];
+    const double acx = comx[a], acy = comy[a];
+    uint32_t take[2] = {0u, 0u};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int r = 32 * h + lane;
+        if (r < nq) {
+            const int64_t q = ustart[u] + r;
+            const int32_t sl = src_idx[q];
+            take[h] = p2p_mask[q];  // 0 for the self row
+            rb0[w][r] = bs[sl];
+            rsh[w][r] = make_float2((float)(acx - comx[sl]), (float)(acy - comy[sl]));
+        }
+    }
+    // exclusive scan of the 64 rows' counts (rows lane, then rows 32 + lane)
+    int base = 0, T = 0;
+    int excl[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int c = __popc(take[h]);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += t;
+        }
+        excl[h] = base + incl - c;
+        base += __shfl_sync(full, incl, 31);
+    }
+    T = base;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        uint32_t m = take[h];
+        int pp = excl[h];
+        const int r = 32 * h + lane;
+        while (m) {
+            const int j = __ffs(m) - 1;
+            m &= m - 1u;
+            strm[w][pp++] = (uint16_t)((r << 5) | j);
+        }
+    }
+    __syncwarp();
+    const f2v E2 = f2splat(eps2);
+    f2v acc[NC];
+#pragma unroll
+    for (int k = 0; k < NC; k++) acc[k] = f2splat(0.f);
+    auto get = [&](int p, float4 &v, float2 &o) {
+        if (p < T) {
+            const int e = strm[w][p];
+            v = pos[rb0[w][e >> 5] + (e & 31)];
+            o = rsh[w][e >> 5];
+        } else {
+            v = make_float4(0.f, 0.f, 0.f, 0.f);
+            o = make_float2(1.f, 1.f);
+        }
+    };
+    float4 cA = make_float4(0.f, 0.f, 0.f, 0.f), cB = cA;
+    float2 oA = make_float2(1.f, 1.f), oB = oA;
+    if (T > 0) {
+        get(lane, cA, oA);
+        get(32 + lane, cB, oB);
+    }
+    for (int c0 = 0; c0 < T; c0 += 64) {
+        float4 nA = make_float4(0.f, 0.f, 0.f, 0.f), nB = nA;
+        float2 pA = make_float2(1.f, 1.f), pB = pA;
+        if (c0 + 64 < T) {
+            get(c0 + 64 + lane, nA, pA);
+            get(c0 + 96 + lane, nB, pB);
+        }
+        // com_a - x_j = (com_a - com_s) - (x_j - com_s)
+        const f2v dx = f2sub(f2pair(oA.x, oB.x), f2pair(cA.x, cB.x));
+        const f2v dy = f2sub(f2pair(oA.y, oB.y), f2pair(cA.y, cB.y));
+        const f2v ir = rsqrt_x2(f2fma(dx, dx, f2fma(dy, dy, E2)));
+        f2v cf[NC];
+        taylor_1r_x2<P>(dx, dy, ir, f2mul(ir, ir), cf);
+        const f2v mm = f2pair(cA.z, cB.z);
+#pragma unroll
+        for (int q = 0; q < NC; q++) acc[q] = f2fma(mm, cf[q], acc[q]);
+        cA = nA;
+        cB = nB;
+        oA = pA;
+        oB = pB;
+    }
+    const bool single = (leaf_u[a + 1] - leaf_u[a]) + (body_u ? body_u[a + 1] - body_u[a] : 0) == 1;
 #pragma unroll
     for (int q = 0; q < NC; q++) {
         float lo, hi;
@@ -1652,11 +1962,13 @@ __device__ __forceinline__ void p2l_body(T dx, T dy, T mj, T eps2, T *acc) {
 template <int P, class T>
 __global__ void __launch_bounds__(128) k_p2l(int64_t n_units, const int32_t *__restrict__ uleaf,
                                              const int64_t *__restrict__ ustart, const int32_t *__restrict__ ulen,
-                                             const int64_t *__restrict__ leaf_u, const int32_t *__restrict__ src_idx,
+                                             const int64_t *__restrict__ leaf_u, const int64_t *__restrict__ body_u,
+                                             const int32_t *__restrict__ src_idx,
                                              const float4 *__restrict__ pos, const double *__restrict__ X,
                                              const double *__restrict__ Y, const double *__restrict__ Mb,
                                              const double *__restrict__ comx, const double *__restrict__ comy,
                                              const int32_t *__restrict__ bs, const int32_t *__restrict__ be, T eps2,
+                                             const uint32_t *__restrict__ p2p_mask, int body_units,
                                              T *__restrict__ Lf, T *__restrict__ ppart) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<T>(NC);
@@ -1667,70 +1979,84 @@ __global__ void __launch_bounds__(128) k_p2l(int64_t n_units, const int32_t *__r
     const int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (u >= n_units) return;
     const int32_t a = uleaf[u];
-    const int nq = ulen[u];
+    // a body-level unit (length stored negated): up to GX_BODY_UNIT P2P rows of the leaf,
+    // their masked bodies only (source leaves of at most 32 bodies); body_units = 0 leaves
+    // them to k_p2l_body_x2
+    const int raw = ulen[u];
+    if (raw < 0 && !body_units) return;
+    const bool body = raw < 0;
+    const int nq = body ? -raw : raw;
     const double tcx = comx[a], tcy = comy[a];
-    int32_t sb = 0, se = 0;
-    T shx = T(0), shy = T(0);
-    double scx = 0.0, scy = 0.0;
-    if (lane < nq) {
-        const int32_t sl = src_idx[ustart[u] + lane];
-        sb = bs[sl];
-        se = be[sl];
-        scx = comx[sl];
-        scy = comy[sl];
-        shx = (T)(tcx - scx);
-        shy = (T)(tcy - scy);
-    }
     T acc[NC];
 #pragma unroll
     for (int k = 0; k < NCr; k++) acc[k] = T(0);
-    // one body of source k per lane (the first 32 of the leaf): relative position, mass
-    auto fetch = [&](int k, T &px, T &py, T &pm) {
-        const int32_t j = __shfl_sync(0xffffffffu, sb, k) + lane, j1 = __shfl_sync(0xffffffffu, se, k);
-        if constexpr (sizeof(T) == 4) {
-            const float4 v = j < j1 ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-            px = v.x;
-            py = v.y;
-            pm = v.z;
-        } else {
-            const double cx = __shfl_sync(0xffffffffu, scx, k), cy = __shfl_sync(0xffffffffu, scy, k);
-            px = j < j1 ? X[j] - cx : 0.0;
-            py = j < j1 ? Y[j] - cy : 0.0;
-            pm = j < j1 ? Mb[j] : 0.0;
+    // the unit's rows 32 at a time (a body-level unit has up to GX_BODY_UNIT)
+    for (int g0 = 0; g0 < nq; g0 += 32) {
+        const int ng = min(32, nq - g0);
+        int32_t sb = 0, se = 0;
+        uint32_t take = 0xffffffffu;
+        T shx = T(0), shy = T(0);
+        double scx = 0.0, scy = 0.0;
+        if (lane < ng) {
+            const int64_t q = ustart[u] + g0 + lane;
+            if (body) take = p2p_mask[q];
+            const int32_t sl = src_idx[q];
+            sb = bs[sl];
+            se = be[sl];
+            scx = comx[sl];
+            scy = comy[sl];
+            shx = (T)(tcx - scx);
+            shy = (T)(tcy - scy);
         }
-    };
-    T cx_ = T(0), cy_ = T(0), cm = T(0);
-    if (nq > 0) fetch(0, cx_, cy_, cm);
-    for (int k = 0; k < nq; k++) {
-        T nx = T(0), ny = T(0), nm = T(0);
-        if (k + 1 < nq) fetch(k + 1, nx, ny, nm);
-        const T ox = __shfl_sync(0xffffffffu, shx, k), oy = __shfl_sync(0xffffffffu, shy, k);
-        const int32_t j0 = __shfl_sync(0xffffffffu, sb, k), j1 = __shfl_sync(0xffffffffu, se, k);
-        const double ckx = __shfl_sync(0xffffffffu, scx, k), cky = __shfl_sync(0xffffffffu, scy, k);
-        (void)ckx;
-        (void)cky;
-        // com_a - x_j = (com_a - com_s) - (x_j - com_s)
-        if (j0 + lane < j1) p2l_body<P, T>(ox - cx_, oy - cy_, cm, eps2, acc);
-        // leaves above 32 bodies (n_max > 32): the rest of the source's bodies
-        for (int32_t j = j0 + 32 + lane; j < j1; j += 32) {
-            T px, py, pm;
+        // one body of source k per lane (the first 32 of the leaf): relative position, mass
+        auto fetch = [&](int k, T &px, T &py, T &pm) {
+            const int32_t j = __shfl_sync(0xffffffffu, sb, k) + lane, j1 = __shfl_sync(0xffffffffu, se, k);
             if constexpr (sizeof(T) == 4) {
-                const float4 v = pos[j];
+                const float4 v = j < j1 ? pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
                 px = v.x;
                 py = v.y;
                 pm = v.z;
             } else {
-                px = X[j] - ckx;
-                py = Y[j] - cky;
-                pm = Mb[j];
+                const double cx = __shfl_sync(0xffffffffu, scx, k), cy = __shfl_sync(0xffffffffu, scy, k);
+                px = j < j1 ? X[j] - cx : 0.0;
+                py = j < j1 ? Y[j] - cy : 0.0;
+                pm = j < j1 ? Mb[j] : 0.0;
             }
-            p2l_body<P, T>(ox - px, oy - py, pm, eps2, acc);
+        };
+        T cx_ = T(0), cy_ = T(0), cm = T(0);
+        fetch(0, cx_, cy_, cm);
+        for (int k = 0; k < ng; k++) {
+            T nx = T(0), ny = T(0), nm = T(0);
+            if (k + 1 < ng) fetch(k + 1, nx, ny, nm);
+            const T ox = __shfl_sync(0xffffffffu, shx, k), oy = __shfl_sync(0xffffffffu, shy, k);
+            const int32_t j0 = __shfl_sync(0xffffffffu, sb, k), j1 = __shfl_sync(0xffffffffu, se, k);
+            const double ckx = __shfl_sync(0xffffffffu, scx, k), cky = __shfl_sync(0xffffffffu, scy, k);
+            (void)ckx;
+            (void)cky;
+            const uint32_t tk = __shfl_sync(0xffffffffu, take, k);
+            // com_a - x_j = (com_a - com_s) - (x_j - com_s)
+            if (j0 + lane < j1 && ((tk >> lane) & 1u)) p2l_body<P, T>(ox - cx_, oy - cy_, cm, eps2, acc);
+            // leaves above 32 bodies (n_max > 32, never a body-level unit): the rest of the source's bodies
+            for (int32_t j = j0 + 32 + lane; j < j1; j += 32) {
+                T px, py, pm;
+                if constexpr (sizeof(T) == 4) {
+                    const float4 v = pos[j];
+                    px = v.x;
+                    py = v.y;
+                    pm = v.z;
+                } else {
+                    px = X[j] - ckx;
+                    py = Y[j] - cky;
+                    pm = Mb[j];
+                }
+                p2l_body<P, T>(ox - px, oy - py, pm, eps2, acc);
+            }
+            cx_ = nx;
+            cy_ = ny;
+            cm = nm;
         }
-        cx_ = nx;
-        cy_ = ny;
-        cm = nm;
     }
-    const bool single = leaf_u[a + 1] - leaf_u[a] == 1;
+    const bool single = (leaf_u[a + 1] - leaf_u[a]) + (body_u ? body_u[a + 1] - body_u[a] : 0) == 1;
 #pragma unroll
     for (int k = 0; k < NCr; k++) {
         const T v = warp_sum_t<T>(acc[k]);
@@ -1743,8 +2069,8 @@ __global__ void __launch_bounds__(128) k_p2l(int64_t n_units, const int32_t *__r
 
 // Leaves with several P2L units: the partials in unit order, subtracted from the local.
 template <int P, class T>
-__global__ void k_p2l_combine(int64_t nl, const int64_t *__restrict__ leaf_u, const T *__restrict__ ppart,
-                              T *__restrict__ Lf) {
+__global__ void k_p2l_combine(int64_t nl, const int64_t *__restrict__ leaf_u, const int64_t *__restrict__ body_u,
+                              int64_t n_leafu, const T *__restrict__ ppart, T *__restrict__ Lf) {
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<T>(NC);
     const int PP = gx_rt_order(P);
@@ -1754,9 +2080,11 @@ __global__ void k_p2l_combine(int64_t nl, const int64_t *__restrict__ leaf_u, co
     const int k = (int)(t - a * NC);
     if (a >= nl || k >= NCr) return;
     const int64_t u0 = leaf_u[a], u1 = leaf_u[a + 1];
-    if (u1 - u0 < 2) return;
+    const int64_t b0 = body_u ? n_leafu + body_u[a] : 0, b1 = body_u ? n_leafu + body_u[a + 1] : 0;
+    if ((u1 - u0) + (b1 - b0) < 2) return;
     T s = T(0);
-    for (int64_t q = u0; q < u1; q++) s += ppart[q * NS + k];
+    for (int64_t q = u0; q < u1; q++) s += ppart[q * NS + k];  // leaf-level units, then body-level ones
+    for (int64_t q = b0; q < b1; q++) s += ppart[q * NS + k];
     Lf[a * NS + k] -= s;
 }
 
@@ -1992,6 +2320,9 @@ int run_forces(gx_ctx *ctx, bool timed) {
     const int32_t *src_idx = mode == GX_MODE_ACCURATE ? dptr<int32_t>(ctx->near_idx) : dptr<int32_t>(ctx->p2p_idx);
     const unsigned gi = (unsigned)((I.n * 32 + 127) / 128);  // warp per item
     const bool split = mode == GX_MODE_ACCURATE && ctx->theta_w > 0.0;  // near-list split: M2P items, P2L units
+    // body-level P2L of the P2P rows: masks in the plan, body-level P2L units
+    const bool body = split && ctx->plan_body_split && gx_body_split_on(ctx);
+    const uint32_t *p2p_mask = body ? dptr<uint32_t>(ctx->p2p_mask) : nullptr;
 
     auto passes = [&](auto tag) -> int {
         using T = decltype(tag);
@@ -2025,7 +2356,11 @@ int run_forces(gx_ctx *ctx, bool timed) {
         if (I.n > 0) {
             // two targets per lane pays when leaves fill most of a row; with leaves of at
             // most 16 bodies (n_max <= 16) the second target would be empty
-            if (mixed && tchunks == 1 && ctx->max_leaf <= 16)
+            if (mixed && body)
+                k_p2p32_stream<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
+                                                             dptr<int32_t>(I.nq), pos, comx, comy, bs, be, src_idx,
+                                                             p2p_mask, (float)eps2, dptr<float2>(ctx->part));
+            else if (mixed && tchunks == 1 && ctx->max_leaf <= 16)
                 k_p2p32_rows1<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
                                                             dptr<int32_t>(I.nq), pos, comx, comy, bs, be, src_idx,
                                                             (float)eps2, dptr<float2>(ctx->part));
@@ -2039,7 +2374,7 @@ int run_forces(gx_ctx *ctx, bool timed) {
                                                             (float)eps2, tchunks, dptr<float2>(ctx->part));
             else
                 k_p2p64_items<<<gi, 128, 0, ctx->stream2>>>(I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb),
-                                                            dptr<int32_t>(I.nq), X, Y, Mb, bs, be, src_idx, eps2,
+                                                            dptr<int32_t>(I.nq), X, Y, Mb, bs, be, src_idx, p2p_mask, eps2,
                                                             tchunks, dptr<double2>(ctx->part));
             ctx->launches++;
         }
@@ -2150,19 +2485,33 @@ int run_forces(gx_ctx *ctx, bool timed) {
             const gx_ctx::P2LUnits &PU = ctx->p2l_units;
             GX_TRY(gx_ensure(ctx, ctx->p2l_part, sizeof(T) * NS * (size_t)(PU.n + 1)));
             const int64_t *leaf_u = dptr<int64_t>(PU.leaf_u);
+            const int64_t *body_u = body ? dptr<int64_t>(PU.body_u) : nullptr;
             const unsigned gu = (unsigned)((PU.n * 32 + 127) / 128);
+            const unsigned gl = (unsigned)((PU.n_leafu * 32 + 127) / 128);
+            const unsigned gb = (unsigned)((PU.n_body * 32 + 127) / 128);
             bool packed = false;
             if constexpr (P <= 5 && sizeof(T) == 4) {
-                k_p2l_x2<P><<<gu, 128, 0, st>>>(PU.n, dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
-                                                dptr<int32_t>(PU.len), leaf_u, src_idx, pos, comx, comy, bs, be,
-                                                (float)eps2, Lf, dptr<float>(ctx->p2l_part));
+                // leaf-level units, then (body-level P2L) the body-level ones
+                if (PU.n_leafu > 0)
+                    k_p2l_x2<P><<<gl, 128, 0, st>>>(PU.n_leafu, dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
+                                                    dptr<int32_t>(PU.len), leaf_u, body_u, src_idx, pos, comx, comy,
+                                                    bs, be, (float)eps2, Lf, dptr<float>(ctx->p2l_part));
+                if (body && PU.n_body > 0) {
+                    k_p2l_body_x2<P><<<gb, 128, 0, st>>>(PU.n_leafu, PU.n_body, dptr<int32_t>(PU.leaf),
+                                                         dptr<int64_t>(PU.start), dptr<int32_t>(PU.len), leaf_u,
+                                                         body_u, src_idx, p2p_mask, pos, comx, comy, bs, (float)eps2,
+                                                         Lf, dptr<float>(ctx->p2l_part));
+                    ctx->launches++;
+                }
                 packed = true;
             }
             if (!packed)
                 k_p2l<P, T><<<gu, 128, 0, st>>>(PU.n, dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
-                                                dptr<int32_t>(PU.len), leaf_u, src_idx, pos, X, Y, Mb, comx, comy, bs,
-                                                be, (T)eps2, Lf, dptr<T>(ctx->p2l_part));
-            k_p2l_combine<P, T><<<gx_blocks(nl * NC, 256), 256, 0, st>>>(nl, leaf_u, dptr<T>(ctx->p2l_part), Lf);
+                                                dptr<int32_t>(PU.len), leaf_u, body_u, src_idx, pos, X, Y, Mb, comx,
+                                                comy, bs, be, (T)eps2, p2p_mask, body ? 1 : 0, Lf,
+                                                dptr<T>(ctx->p2l_part));
+            k_p2l_combine<P, T><<<gx_blocks(nl * NC, 256), 256, 0, st>>>(nl, leaf_u, body_u, PU.n_leafu,
+                                                                         dptr<T>(ctx->p2l_part), Lf);
             ctx->launches += 2;
         }
         float2 *fl = nullptr;

@@ -155,11 +155,24 @@ struct gx_ctx {
     int64_t n_m2p_pairs = 0, n_p2l_pairs = 0, n_m2p_items = 0;
     DevBuf m2p_list;  // int32: the item indices of the M2P items, leaf by leaf
     DevBuf m2p_off;   // int64 [n_leaves + 1]: each leaf's first entry in m2p_list
+    // [leaf-level units | body-level units]: leaf_u[a] is leaf a's first leaf-level unit,
+    // n_leafu + body_u[a] its first body-level one
     struct P2LUnits {
-        DevBuf leaf, start, len, leaf_u;  // int32, int64, int32, int64[n_leaves+1]
-        int64_t n = 0;
+        DevBuf leaf, start, len, leaf_u, body_u;  // int32, int64, int32, int64[n_leaves+1] x 2
+        int64_t n = 0, n_leafu = 0, n_body = 0;
     } p2l_units;
     DevBuf p2l_part;  // per-unit partial locals of leaves with several P2L units
+    // Body-level P2L of the P2P pairs (theta_b > 0, leaves of at most 32 bodies): a
+    // source body j of a P2P row (a <- s), s != a, with |x_j - com_a| theta_b > R_a joins
+    // a's local expansion instead of P2P.  p2p_mask holds, per P2P entry of near_idx, the
+    // bit set of such bodies of s (0 for the self row); the P2P items then run over the
+    // other bodies, and every GX_BODY_UNIT P2P rows of a leaf are a body-P2L unit (its
+    // length stored negated in the P2L units) over the masked ones.
+    double theta_b = 0.0, plan_theta_b = 0.0;
+    bool plan_body_split = false;  // the current ACCURATE plan has the masks
+    DevBuf p2p_mask;               // uint32 per near_idx entry
+    DevBuf body_off32;             // plan scratch: float2 (x - com_leaf, y - com_leaf) per body
+    int64_t n_body_p2l = 0, n_p2p_moved = 0;  // body-P2L evaluations, P2P interactions moved to them
     DevBuf m2l_cnt;   // plan scratch: units per node
     DevBuf plan_ctr;       // ACCURATE plan: device running totals and overflow flags
     // sizes of the last tree and plan: the first capacities of the next build and plan
@@ -227,6 +240,7 @@ int gx_plan_accurate(gx_ctx *ctx);
 int gx_plan_items(gx_ctx *ctx, bool accurate);
 int gx_plan_tree_aux(gx_ctx *ctx);
 int gx_plan_near_split(gx_ctx *ctx);
+int gx_plan_body_masks(gx_ctx *ctx);
 // gx_fmm.cu
 int gx_forces_device(gx_ctx *ctx, bool timed);
 // gx_api.cu: device rebuild with the last build's parameters (permutes the resident
@@ -257,6 +271,13 @@ int gx_n2_device(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, dou
 // grid helpers
 inline unsigned gx_blocks(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// The body-level P2L applies to the P2P pairs of the near-list split (ACCURATE, theta_w
+// > 0) with theta_b > 0 over leaves of at most 32 bodies (one mask word per P2P row);
+// otherwise every P2P row keeps all its bodies.
+inline bool gx_body_split_on(const gx_ctx *ctx) {
+    return ctx->mode == GX_MODE_ACCURATE && ctx->theta_w > 0.0 && ctx->theta_b > 0.0 && ctx->max_leaf <= 32;
+}
+
 // ---------------------------------------------------------------- device helpers
 #ifdef __CUDACC__
 __device__ __forceinline__ double warp_sum(double v) {
@@ -272,6 +293,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 __host__ __device__ constexpr int gx_nc(int p) { return (p + 1) * (p + 2) / 2; }
 constexpr int GX_M2L_UNIT = 256;  // far sources per M2L work unit (8 rounds of a warp)
 constexpr int GX_P2L_UNIT = 32;   // source leaves per P2L work unit (one per lane)
+constexpr int GX_BODY_UNIT = 64;  // P2P rows per body-level P2L unit (two per lane)
 __host__ __device__ constexpr int gx_mi(int i, int j) { return (i + j) * (i + j + 1) / 2 + j; }
 __host__ __device__ constexpr int gx_kdi(int k, int l, int p) { return (k + l) * (2 * p + 1) + l; }
 #endif

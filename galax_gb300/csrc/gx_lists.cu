@@ -1643,25 +1643,100 @@ __global__ void k_items_fill(int64_t nl, const int64_t *start, const int32_t *cn
 }
 
 // P2L units: per leaf the number of units of at most GX_P2L_UNIT source leaves (its P2L
-// sources follow its P2P and M2P sources); then unit -> (leaf, first, length)
+// sources follow its P2P and M2P sources), and with the body-level P2L the number of
+// units of at most GX_BODY_UNIT of its P2P rows (the masked bodies: length stored
+// negated); then unit -> (leaf, first, length), every leaf-level unit (leaf by leaf)
+// before every body-level one, so that each kernel's grid covers its own units only
 __global__ void k_p2l_units_count(int64_t nl, const int32_t *split, int64_t *nunits) {
     int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (a > nl) return;
     nunits[a] = a == nl ? 0 : (split[2 * a + 1] + GX_P2L_UNIT - 1) / GX_P2L_UNIT;
 }
 
-__global__ void k_p2l_units_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split,
-                                 const int64_t *leaf_u, int32_t *uleaf, int64_t *ustart, int32_t *ulen) {
+__global__ void k_body_units_count(int64_t nl, const int32_t *cnt, int64_t *nunits) {
+    int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a > nl) return;
+    nunits[a] = a == nl ? 0 : (cnt[a] + GX_BODY_UNIT - 1) / GX_BODY_UNIT;
+}
+
+__global__ void k_p2l_units_fill(int64_t nl, const int64_t *start, const int32_t *cnt, const int32_t *split, int body,
+                                 const int64_t *leaf_u, const int64_t *body_u, int32_t *uleaf, int64_t *ustart,
+                                 int32_t *ulen) {
     const int64_t a = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // a warp per leaf
     const int lane = threadIdx.x & 31;
     if (a >= nl) return;
     const int64_t s0 = start[a] + cnt[a] + split[2 * a];
     const int32_t c = split[2 * a + 1];
     const int64_t u0 = leaf_u[a];
-    for (int32_t k = lane; k * GX_P2L_UNIT < c; k += 32) {
+    const int32_t nlu = (c + GX_P2L_UNIT - 1) / GX_P2L_UNIT;
+    for (int32_t k = lane; k < nlu; k += 32) {
         uleaf[u0 + k] = (int32_t)a;
         ustart[u0 + k] = s0 + (int64_t)k * GX_P2L_UNIT;
         ulen[u0 + k] = min(GX_P2L_UNIT, c - k * GX_P2L_UNIT);
+    }
+    if (!body) return;
+    const int32_t cp = cnt[a];
+    const int64_t b0 = leaf_u[nl] + body_u[a];
+    for (int32_t k = lane; k * GX_BODY_UNIT < cp; k += 32) {
+        uleaf[b0 + k] = (int32_t)a;
+        ustart[b0 + k] = start[a] + (int64_t)k * GX_BODY_UNIT;
+        ulen[b0 + k] = -min(GX_BODY_UNIT, cp - k * GX_BODY_UNIT);
+    }
+}
+
+// Body-level P2L masks.  Per body its FP32 offset from its leaf's COM (each axis the FP64
+// difference rounded once), then per P2P row (a <- s), s != a, the bit set of s's bodies
+// with |o_j + (com_s - com_a)|^2 theta_b^2 > R_a^2, in separately rounded FP32 operations
+// (o_j and the leaf-pair shift each rounded once from FP64), so that the oracle decides
+// every body alike.  A warp per P2P item, a lane per body of each row in turn.
+__global__ void k_body_off32(int64_t nl, const double *x, const double *y, const double *comx, const double *comy,
+                             const int32_t *bs, const int32_t *be, float2 *off) {
+    const int64_t L = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (L >= nl) return;
+    const double cx = comx[L], cy = comy[L];
+    for (int32_t j = bs[L] + lane; j < be[L]; j += 32)
+        off[j] = make_float2(__double2float_rn(__dsub_rn(x[j], cx)), __double2float_rn(__dsub_rn(y[j], cy)));
+}
+
+__global__ void __launch_bounds__(128) k_body_masks(int64_t n_items, const int32_t *__restrict__ item_leaf,
+                                                    const int64_t *__restrict__ item_qb,
+                                                    const int32_t *__restrict__ item_nq,
+                                                    const int32_t *__restrict__ near_idx,
+                                                    const double *__restrict__ comx, const double *__restrict__ comy,
+                                                    const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
+                                                    const float *__restrict__ R32, const float2 *__restrict__ off,
+                                                    float tb2, uint32_t *__restrict__ mask) {
+    const unsigned full = 0xffffffffu;
+    const int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (it >= n_items) return;
+    const int nq = item_nq[it];
+    if (nq <= 0) return;  // an M2P item
+    const int32_t a = item_leaf[it];
+    const int64_t qb = item_qb[it];
+    int32_t s = -1, b0 = 0, b1 = 0;
+    float shx = 0.f, shy = 0.f;
+    if (lane < nq) {
+        s = near_idx[qb + lane];
+        b0 = bs[s];
+        b1 = be[s];
+        shx = __double2float_rn(__dsub_rn(comx[s], comx[a]));
+        shy = __double2float_rn(__dsub_rn(comy[s], comy[a]));
+    }
+    const float ra = R32[a], ra2 = __fmul_rn(ra, ra);
+    for (int k = 0; k < nq; k++) {
+        const int32_t sk = __shfl_sync(full, s, k), j0 = __shfl_sync(full, b0, k), j1 = __shfl_sync(full, b1, k);
+        const float hx = __shfl_sync(full, shx, k), hy = __shfl_sync(full, shy, k);
+        bool far = false;
+        if (sk != a && j0 + lane < j1) {
+            const float2 o = off[j0 + lane];
+            const float ex = __fadd_rn(o.x, hx), ey = __fadd_rn(o.y, hy);
+            const float d2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+            far = __fmul_rn(d2, tb2) > ra2;
+        }
+        const unsigned m = __ballot_sync(full, far);
+        if (lane == 0) mask[qb + k] = m;
     }
 }
 
@@ -1760,13 +1835,15 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     // the P2P items and (ACCURATE) the M2L units: counts and scans of both, one wait for
     // their two totals, then both fills
     const bool split = accurate && ctx->theta_w > 0.0;
+    const bool body = split && nl > 0 && gx_body_split_on(ctx);  // body-level P2L units after the leaf-level ones
+    if (accurate) ctx->plan_body_split = false;  // the masks follow these items (gx_plan_body_masks)
     const int32_t *scnt = split ? dptr<int32_t>(ctx->split_cnt) : nullptr;
     GX_TRY(gx_ensure(ctx, I.off, sizeof(int64_t) * (size_t)(nl + 1)));
     GX_TRY(gx_ensure(ctx, ctx->scratch_c, sizeof(int64_t) * (size_t)(nl + 1)));
     int64_t *nit = dptr<int64_t>(ctx->scratch_c);
     k_items_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, nit);
     GX_TRY(gx_exclusive_scan_i64(ctx, nit, dptr<int64_t>(I.off), nl + 1));
-    int64_t tot[4] = {0, 0, 0, 0};
+    int64_t tot[5] = {0, 0, 0, 0, 0};
     unsigned long long stot[4] = {0, 0, 0, 0};
     gx_ctx::P2LUnits &PU = ctx->p2l_units;
     if (split) {
@@ -1785,6 +1862,14 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
         GX_TRY(gx_exclusive_scan_i64(ctx, npu, dptr<int64_t>(PU.leaf_u), nl + 1));
         GX_CUDA(ctx, cudaMemcpyAsync(&tot[2], dptr<int64_t>(PU.leaf_u) + nl, sizeof(int64_t), cudaMemcpyDeviceToHost,
                                      ctx->stream));
+        GX_TRY(gx_ensure(ctx, PU.body_u, sizeof(int64_t) * (size_t)(nl + 1)));
+        if (body) {
+            k_body_units_count<<<gx_blocks(nl + 1, 256), 256, 0, ctx->stream>>>(nl, cnt, npu);
+            GX_TRY(gx_exclusive_scan_i64(ctx, npu, dptr<int64_t>(PU.body_u), nl + 1));
+            GX_CUDA(ctx, cudaMemcpyAsync(&tot[4], dptr<int64_t>(PU.body_u) + nl, sizeof(int64_t),
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+            ctx->launches++;
+        }
         GX_CUDA(ctx, cudaMemcpyAsync(stot, ctx->split_tot.p, sizeof(stot), cudaMemcpyDeviceToHost, ctx->stream));
         ctx->launches++;
     }
@@ -1816,21 +1901,23 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     ctx->launches += 2;
     I.n = tot[0];
     ctx->n_m2p_items = split ? tot[3] : 0;
-    PU.n = 0;
+    PU.n = PU.n_leafu = PU.n_body = 0;
     ctx->n_m2p_pairs = ctx->n_p2l_pairs = 0;
     if (split) {
         ctx->n_near_pairs = (int64_t)stot[0];
         ctx->n_m2p_pairs = (int64_t)stot[1];
         ctx->n_p2l_pairs = (int64_t)stot[2];
-        const int64_t npu = tot[2];
+        const int64_t npu = tot[2] + (body ? tot[4] : 0);
         GX_TRY(gx_ensure(ctx, PU.leaf, sizeof(int32_t) * (size_t)(npu + 1)));
         GX_TRY(gx_ensure(ctx, PU.start, sizeof(int64_t) * (size_t)(npu + 1)));
         GX_TRY(gx_ensure(ctx, PU.len, sizeof(int32_t) * (size_t)(npu + 1)));
-        k_p2l_units_fill<<<gx_blocks(nl * 32, 256), 256, 0, ctx->stream>>>(nl, start, cnt, scnt, dptr<int64_t>(PU.leaf_u),
-                                                                      dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start),
-                                                                      dptr<int32_t>(PU.len));
+        k_p2l_units_fill<<<gx_blocks(nl * 32, 256), 256, 0, ctx->stream>>>(
+            nl, start, cnt, scnt, body ? 1 : 0, dptr<int64_t>(PU.leaf_u), dptr<int64_t>(PU.body_u),
+            dptr<int32_t>(PU.leaf), dptr<int64_t>(PU.start), dptr<int32_t>(PU.len));
         ctx->launches++;
         PU.n = npu;
+        PU.n_leafu = tot[2];
+        PU.n_body = body ? tot[4] : 0;
     }
     if (accurate) {
         const int64_t nun = tot[1];
@@ -1845,6 +1932,32 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
     }
     GX_CUDA(ctx, cudaGetLastError());
     I.valid = true;
+    return GX_OK;
+}
+
+// The body-level P2L masks of the current ACCURATE plan (after gx_plan_items, whose P2L
+// units include the body-level ones when gx_body_split_on).
+int gx_plan_body_masks(gx_ctx *ctx) {
+    ctx->plan_body_split = false;
+    const int64_t nl = ctx->n_leaves, n = ctx->n_bodies;
+    const gx_ctx::Items &I = ctx->items_acc;
+    if (!gx_body_split_on(ctx) || nl == 0 || !I.valid) return GX_OK;
+    const int64_t ncap = (int64_t)(ctx->near_idx.bytes / sizeof(int32_t));
+    GX_TRY(gx_ensure(ctx, ctx->p2p_mask, sizeof(uint32_t) * (size_t)(ncap + 1)));
+    GX_TRY(gx_ensure(ctx, ctx->body_off32, sizeof(float2) * (size_t)(n + 1)));
+    k_body_off32<<<gx_blocks(nl * 32, 256), 256, 0, ctx->stream>>>(
+        nl, dptr<double>(ctx->x), dptr<double>(ctx->y), dptr<double>(ctx->comx), dptr<double>(ctx->comy),
+        dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be), dptr<float2>(ctx->body_off32));
+    const float tb = (float)ctx->theta_b, tb2 = tb * tb;
+    if (I.n > 0)
+        k_body_masks<<<gx_blocks(I.n * 32, 128), 128, 0, ctx->stream>>>(
+            I.n, dptr<int32_t>(I.leaf), dptr<int64_t>(I.qb), dptr<int32_t>(I.nq), dptr<int32_t>(ctx->near_idx),
+            dptr<double>(ctx->comx), dptr<double>(ctx->comy), dptr<int32_t>(ctx->bs), dptr<int32_t>(ctx->be),
+            dptr<float>(ctx->radius32), dptr<float2>(ctx->body_off32), tb2, dptr<uint32_t>(ctx->p2p_mask));
+    ctx->launches += 2;
+    GX_CUDA(ctx, cudaGetLastError());
+    ctx->plan_body_split = true;
+    ctx->plan_theta_b = ctx->theta_b;
     return GX_OK;
 }
 

@@ -92,6 +92,17 @@ int gx_set_mode(gx_ctx *ctx, int mode, int precision, double theta);
 int gx_set_near_split(gx_ctx *ctx, double theta_w);
 /* Leaf pairs of the current ACCURATE plan taken by M2P and by P2L (0 with the split off). */
 int gx_plan_split_info(gx_ctx *ctx, int64_t *n_m2p_pairs, int64_t *n_p2l_pairs);
+/* The body-level P2L of the P2P pairs left by the near-list split (no counterpart in the
+ * reference).  With theta_b > 0, theta_w > 0 and leaves of at most 32 bodies, a source
+ * body j of a P2P leaf pair (target a, source s, s != a) with |x_j - com_a| theta_b > R_a
+ * goes into a's local expansion (truncation bounded by theta_b^(p+1)) instead of P2P;
+ * decided per body in FP32 from the plan's positions, like the leaf-level tests.
+ * theta_b = 0 (the default) turns it off; the adjoint entry points need the near-list
+ * split, and with it this, off. */
+int gx_set_body_split(gx_ctx *ctx, double theta_b);
+/* Of the current ACCURATE plan: body-body P2P interactions moved to body-level P2L, and
+ * the body-level P2L evaluations (one per source body and target leaf); 0 when off. */
+int gx_plan_body_split_info(gx_ctx *ctx, int64_t *n_p2p_moved, int64_t *n_body_p2l);
 /* Changes p and the softening of an existing context. */
 int gx_set_params(gx_ctx *ctx, uint32_t p, double eps);
 

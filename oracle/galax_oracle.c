@@ -1531,7 +1531,31 @@ void gxo_compute_fmm_force_mac(double *x, double *y, double *m, double *ax, doub
 void gxo_compute_fmm_force_wx(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
                               const gxo_csr *far, const gxo_csr *near, const gxo_csr *m2p, const gxo_csr *p2l,
                               int64_t p, double eps) {
+    gxo_compute_fmm_force_wxb(x, y, m, ax, ay, t, far, near, m2p, p2l, p, eps, NULL, 0.0);
+}
+
+/* Body-level P2L of a P2P pair (a <- s), s != a (not in the reference): a source body j
+ * of s with |x_j - com_a| theta_b > R_a goes into a's local expansion instead of P2P, the
+ * truncation bounded by theta_b^(p+1) as the leaf-level P2L's.  Decided in float,
+ * squared, with separately rounded operations: the offset is (x_j - com_s) + (com_s -
+ * com_a), each difference formed in double and rounded once, as the device forms it. */
+int gxo_body_p2l(const double *x, const double *y, const gxo_tree *t, const double *R, int64_t a, int64_t s,
+                 int64_t j, double theta_b) {
+    const float ox = (float)(x[j] - t->comx[s]), oy = (float)(y[j] - t->comy[s]);
+    const float hx = (float)(t->comx[s] - t->comx[a]), hy = (float)(t->comy[s] - t->comy[a]);
+    const float ex = ox + hx, ey = oy + hy;
+    const float d2 = ex * ex + ey * ey;
+    const float tb = (float)theta_b, tb2 = tb * tb, ra = (float)R[a];
+    return d2 * tb2 > ra * ra;
+}
+
+/* gxo_compute_fmm_force_wx, and with theta_b > 0 (R the node radii) the body-level P2L
+ * of the P2P pairs: those source bodies join the P2L sums and leave P2P. */
+void gxo_compute_fmm_force_wxb(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
+                               const gxo_csr *far, const gxo_csr *near, const gxo_csr *m2p, const gxo_csr *p2l,
+                               int64_t p, double eps, const double *R, double theta_b) {
     init_tables();
+    const int body_split = R != NULL && theta_b > 0.0;
     int64_t n = t->n_nodes > 0 ? t->body_end[t->n_nodes - 1] : 0;
     for (int64_t i = 0; i < n; i++) {
         if (fabs(x[i]) > 1e100 || fabs(y[i]) > 1e100 || !isfinite(x[i]) || !isfinite(y[i])) { x[i] = 0.0; y[i] = 0.0; }
@@ -1562,6 +1586,29 @@ void gxo_compute_fmm_force_wx(double *x, double *y, double *m, double *ax, doubl
         free(G);
     }
     gxo_l2l(loc, t, p, 1);
+    if (body_split) {
+        /* sanitising happened above, so the tests here and in P2P see the same positions */
+#pragma omp parallel num_threads(gxo_get_threads())
+        {
+            double *G = (double *)malloc(sizeof(double) * DS);
+#pragma omp for schedule(dynamic, 16)
+            for (int64_t id = 0; id < t->n_nodes; id++) {
+                double *L = loc + id * st;
+                for (int64_t q = near->off[id]; q < near->off[id + 1]; q++) {
+                    int64_t s = near->idx[q];
+                    if (s == id) continue;
+                    for (int64_t j = t->body_start[s]; j < t->body_end[s]; j++) {
+                        if (!gxo_body_p2l(x, y, t, R, id, s, j, theta_b)) continue;
+                        gxo_kernel_derivs_recurrence(t->comx[id] - x[j], t->comy[id] - y[j], eps, p, G);
+                        for (int64_t oi = 0; oi <= p; oi++)
+                            for (int64_t oj = 0; oj <= p - oi; oj++)
+                                L[MI(oi, oj)] += m[j] * G[kdi(oi, oj, p)] / (g_fact[oi] * g_fact[oj]);
+                    }
+                }
+            }
+            free(G);
+        }
+    }
     if (p2l) {
 #pragma omp parallel num_threads(gxo_get_threads())
         {
@@ -1620,8 +1667,10 @@ void gxo_compute_fmm_force_wx(double *x, double *y, double *m, double *ax, doubl
             double fx = 0.0, fy = 0.0;
             for (int64_t q = near->off[id]; q < near->off[id + 1]; q++) {
                 int64_t s = near->idx[q];
+                const int split_s = body_split && s != id;
                 for (int64_t j = t->body_start[s]; j < t->body_end[s]; j++) {
                     if (j == i) continue;
+                    if (split_s && gxo_body_p2l(x, y, t, R, id, s, j, theta_b)) continue;
                     double dx = x[j] - x[i], dy = y[j] - y[i];
                     double r2 = dx * dx + dy * dy + s2;
                     double ir = 1.0 / sqrt(r2);

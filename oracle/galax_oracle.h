@@ -151,6 +151,11 @@ void gxo_near_split(const gxo_tree *t, const double *R, double theta_w, const gx
 void gxo_compute_fmm_force_wx(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
                               const gxo_csr *far, const gxo_csr *near, const gxo_csr *m2p, const gxo_csr *p2l,
                               int64_t p, double eps);
+int gxo_body_p2l(const double *x, const double *y, const gxo_tree *t, const double *R, int64_t a, int64_t s,
+                 int64_t j, double theta_b);
+void gxo_compute_fmm_force_wxb(double *x, double *y, double *m, double *ax, double *ay, const gxo_tree *t,
+                               const gxo_csr *far, const gxo_csr *near, const gxo_csr *m2p, const gxo_csr *p2l,
+                               int64_t p, double eps, const double *R, double theta_b);
 
 /* ---- N^2 adjoint (not in the reference; the reference gradient of the GPU adjoint) ---- */
 void gxo_n2_vjp(const double *x, const double *y, const double *m, int64_t n, double eps, const double *lx,

@@ -452,6 +452,9 @@ def _mac_setup():
     L.gxo_compute_fmm_force_mac.argtypes = [_D] * 5 + [_TP, CP, CP, C.c_int64, C.c_double]
     L.gxo_near_split.argtypes = [_TP, _D, C.c_double, CP, C.POINTER(CP), C.POINTER(CP), C.POINTER(CP)]
     L.gxo_compute_fmm_force_wx.argtypes = [_D] * 5 + [_TP, CP, CP, CP, CP, C.c_int64, C.c_double]
+    L.gxo_compute_fmm_force_wxb.argtypes = [_D] * 5 + [_TP, CP, CP, CP, CP, C.c_int64, C.c_double, _D, C.c_double]
+    L.gxo_body_p2l.argtypes = [_D, _D, _TP, _D, C.c_int64, C.c_int64, C.c_int64, C.c_double]
+    L.gxo_body_p2l.restype = C.c_int
     L._mac_ready = True
     return L
 
@@ -490,6 +493,23 @@ def compute_fmm_force_wx(b: Bodies, t: Tree, far: Csr, near: Csr, m2p: Csr, p2l:
     _mac_setup().gxo_compute_fmm_force_wx(_d(b.x), _d(b.y), _d(b.mass), _d(b.ax), _d(b.ay), t.ptr, far.ptr,
                                           near.ptr, m2p.ptr if m2p is not None else None,
                                           p2l.ptr if p2l is not None else None, int(p), float(eps))
+
+
+def body_p2l(b: Bodies, t: Tree, radius: np.ndarray, a: int, s: int, j: int, theta_b: float) -> bool:
+    """The per-body test of the body-level P2L: body j of source leaf s joins target leaf
+    a's local expansion."""
+    r = _arr(radius)
+    return bool(_mac_setup().gxo_body_p2l(_d(b.x), _d(b.y), t.ptr, _d(r), int(a), int(s), int(j), float(theta_b)))
+
+
+def compute_fmm_force_wxb(b: Bodies, t: Tree, far: Csr, near: Csr, m2p: Csr, p2l: Csr, p: int, eps: float,
+                          radius: np.ndarray, theta_b: float) -> None:
+    """compute_fmm_force_wx with the body-level P2L of the P2P pairs (theta_b > 0)."""
+    r = _arr(radius)
+    _mac_setup().gxo_compute_fmm_force_wxb(_d(b.x), _d(b.y), _d(b.mass), _d(b.ax), _d(b.ay), t.ptr, far.ptr,
+                                           near.ptr, m2p.ptr if m2p is not None else None,
+                                           p2l.ptr if p2l is not None else None, int(p), float(eps), _d(r),
+                                           float(theta_b))
 
 
 # ------------------------------------------------------------ N^2 adjoint

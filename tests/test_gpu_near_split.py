@@ -161,3 +161,145 @@ def test_split_with_rebuild_every_step(G):
         ctx.close()
     assert np.array_equal(outs[0].x, outs[1].x) and np.array_equal(outs[0].ax, outs[1].ax)
     assert np.all(np.isfinite(outs[0].ax))
+
+
+# ---------------------------------------------------------------- body-level P2L
+THETA_B = 0.3
+
+
+def _body_split_counts(ob, t, R, p2p, theta_b):
+    """(P2P interactions moved, body-level P2L evaluations) by the oracle's per-body test
+    (gxo_body_p2l): float32, separately rounded operations, as numpy evaluates them."""
+    nl = t.n_leaves
+    off, idx = p2p.off, p2p.idx
+    A = np.repeat(np.arange(nl), np.diff(off[: nl + 1]))
+    S = idx[: off[nl]].astype(np.int64)
+    keep = S != A
+    A, S = A[keep], S[keep]
+    bs, be = t.body_start, t.body_end
+    tb = np.float32(theta_b)
+    tb2 = tb * tb
+    ra = R[A].astype(np.float32)
+    ra2 = ra * ra
+    hx = (t.comx[S] - t.comx[A]).astype(np.float32)
+    hy = (t.comy[S] - t.comy[A]).astype(np.float32)
+    moved = evals = 0
+    for k in range(32):
+        j = bs[S] + k
+        ok = j < be[S]
+        jj = np.where(ok, j, 0)
+        ex = (ob.x[jj] - t.comx[S]).astype(np.float32) + hx
+        ey = (ob.y[jj] - t.comy[S]).astype(np.float32) + hy
+        far = ok & ((ex * ex + ey * ey) * tb2 > ra2)
+        evals += int(far.sum())
+        moved += int((far * (be[A] - bs[A])).sum())
+    return moved, evals
+
+
+def _oracle_wxb(O, ob, t, theta, theta_w, theta_b, p, eps):
+    R = O.node_radii(ob, t)
+    far, near = O.mac_lists_build(t, R, theta)
+    p2p, m2p, p2l = O.near_split(t, R, theta_w, near)
+    ref = ob.copy()
+    O.compute_fmm_force_wxb(ref, t, far, p2p, m2p, p2l, p, eps, R, theta_b)
+    return ref, R, p2p
+
+
+def _gpu_b(G, ob, t, v, u, p, eps, prec, theta_w, theta_b):
+    n = len(ob.x)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 24, p=p, eps64=eps))
+    ctx.set_mode(G.MODE_ACCURATE, prec, 0.5)
+    ctx.set_near_split(theta_w)
+    ctx.set_body_split(theta_b)
+    ctx.upload_tree_data(t, v, u)
+    ctx.upload_bodies(G.Bodies.from_arrays(ob.x.copy(), ob.y.copy(), ob.mass.copy()))
+    ax, ay = np.zeros(n), np.zeros(n)
+    ctx.compute_forces(ob.x.copy(), ob.y.copy(), ob.mass.copy(), ax, ay)
+    info = ctx.plan_body_split_info()
+    ctx.close()
+    return ax, ay, info
+
+
+@pytest.mark.parametrize("preset,n,n_max,p", [
+    ("plummer", 30_000, 32, 4),
+    ("uniform", 10_007, 32, 4),
+    ("galaxy", 5_001, 32, 4),
+    ("disk", 20_000, 16, 4),
+    ("plummer", 10_000, 32, 6),
+    ("plummer", 10_000, 32, 2),
+])
+def test_body_split_fp64_matches_oracle(G, oracle, preset, n, n_max, p):
+    """Body-level P2L of the P2P rows (source bodies far from the target leaf's COM join
+    its local expansion): the FP64 form against the oracle's evaluation of the same split
+    (gxo_compute_fmm_force_wxb) within 1e-10, and the same bodies moved."""
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=47)
+    ob, t, v, u, eps = oracle_case(oracle, b, n_max, presets.BOUNDS[preset], p)
+    ref, R, p2p = _oracle_wxb(oracle, ob, t, 0.5, 0.4, THETA_B, p, eps)
+    ax, ay, (moved, evals) = _gpu_b(G, ob, t, v, u, p, eps, G.PREC_FP64, 0.4, THETA_B)
+    assert (moved, evals) == _body_split_counts(ob, t, R, p2p, THETA_B)
+    if preset != "galaxy":
+        assert moved > 0
+    err = rel_vec_err(ax, ay, ref.ax, ref.ay)
+    assert err.max() < TOL_FP64, f"max {err.max():.3e} at body {err.argmax()}"
+
+
+@pytest.mark.parametrize("preset,n,n_max,p", [("plummer", 30_017, 32, 4), ("uniform", 10_000, 32, 4),
+                                              ("disk", 20_000, 16, 4), ("plummer", 20_000, 32, 6)])
+def test_body_split_mixed_error_budget(G, oracle, preset, n, n_max, p):
+    """The mixed form with the body-level P2L: against the oracle's FP64 evaluation of the
+    same split (the FP32 floor), and against the exact sum no worse than 1.15x the oracle's
+    split without it."""
+    from galax_gb300 import presets
+    b = presets.make(preset, n, seed=53)
+    ob, t, v, u, eps = oracle_case(oracle, b, n_max, presets.BOUNDS[preset], p)
+    ref, R, p2p = _oracle_wxb(oracle, ob, t, 0.5, 0.4, THETA_B, p, eps)
+    mx, my, _ = _gpu_b(G, ob, t, v, u, p, eps, G.PREC_MIXED, 0.4, THETA_B)
+    assert np.all(np.isfinite(mx)) and np.all(np.isfinite(my))
+    d = rel_vec_err(mx, my, ref.ax, ref.ay)
+    assert np.median(d) < 2e-6 and d.max() < 1e-3, (np.median(d), d.max())
+    base, *_ = _oracle_wxb(oracle, ob, t, 0.5, 0.4, 0.0, p, eps)
+    idx = np.random.default_rng(0).choice(n, 1000, replace=False)
+    ex, ey = oracle.n2_sampled(ob.x, ob.y, ob.mass, eps, idx)
+    e_body = np.median(rel_vec_err(mx[idx], my[idx], ex, ey))
+    e_base = np.median(rel_vec_err(base.ax[idx], base.ay[idx], ex, ey))
+    assert e_body <= 1.15 * e_base + 2e-7, (e_body, e_base)
+
+
+def test_body_split_off_is_the_split_and_repeats(G):
+    """theta_b = 0 gives the near-list split's evaluation bit for bit; with it on, the
+    same evaluation twice gives the same bits, and the plan reports the moved work."""
+    from galax_gb300 import presets
+    n = 8_000
+    b = presets.plummer(n, seed=59)
+    gb = b.copy()
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=4, eps64=0.01))
+    ctx.build_tree(gb, 32, presets.BOUNDS["plummer"])
+    ctx.upload_bodies(gb)
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    ctx.set_near_split(0.4)
+    out = []
+    for tb in (0.0, THETA_B, THETA_B, 0.0):
+        ctx.set_body_split(tb)
+        ctx.forces_resident()
+        r = G.Bodies.new(n)
+        ctx.download_bodies(r)
+        out.append((r.ax.copy(), r.ay.copy(), ctx.plan_body_split_info()))
+    assert np.array_equal(out[0][0], out[3][0]) and np.array_equal(out[0][1], out[3][1])
+    assert np.array_equal(out[1][0], out[2][0]) and np.array_equal(out[1][1], out[2][1])
+    assert not np.array_equal(out[0][0], out[1][0])
+    assert out[0][2] == (0, 0) and out[1][2][0] > 0 and out[1][2][1] > 0
+    # the REF form's plan in between leaves the ACCURATE plan's split as it was
+    ctx.set_body_split(THETA_B)
+    ctx.forces_resident()
+    ctx.set_mode(G.MODE_REF, G.PREC_FP64, 0.5)
+    ctx.forces_resident()
+    ctx.set_mode(G.MODE_ACCURATE, G.PREC_MIXED, 0.5)
+    ctx.forces_resident()
+    r = G.Bodies.new(n)
+    ctx.download_bodies(r)
+    assert np.array_equal(r.ax, out[1][0]) and np.array_equal(r.ay, out[1][1])
+    assert ctx.plan_body_split_info() == out[1][2]
+    with pytest.raises(G.GpuError):
+        ctx.set_body_split(-0.1)
+    ctx.close()

@@ -126,3 +126,45 @@ def test_near_split_partitions_the_near_lists(oracle):
             for s in part:
                 cover[t.body_start[a]:t.body_end[a], t.body_start[s]:t.body_end[s]] += 1
     assert np.all(cover == 1)
+
+
+def test_body_split_oracle(oracle):
+    """The oracle's body-level P2L (gxo_compute_fmm_force_wxb): theta_b = 0 is the
+    near-list split bit for bit; at theta_b = 0.3 it moves source bodies out of P2P and
+    keeps the error against the exact sum within 1.15x of the split without it; every
+    moved body passes the per-body test (|x_j - com_a| theta_b > R_a, truncation bounded
+    by theta_b^(p+1))."""
+    n, p = 6000, 4
+    b = presets.plummer(n, seed=61)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, 32, presets.BOUNDS["plummer"])
+    eps = oracle.cli_softening(ob)
+    R = oracle.node_radii(ob, t)
+    far, near = oracle.mac_lists_build(t, R, 0.5)
+    p2p, m2p, p2l = oracle.near_split(t, R, 0.4, near)
+    a0, a1, a2 = ob.copy(), ob.copy(), ob.copy()
+    oracle.compute_fmm_force_wx(a0, t, far, p2p, m2p, p2l, p, eps)
+    oracle.compute_fmm_force_wxb(a1, t, far, p2p, m2p, p2l, p, eps, R, 0.0)
+    oracle.compute_fmm_force_wxb(a2, t, far, p2p, m2p, p2l, p, eps, R, 0.3)
+    assert np.array_equal(a0.ax, a1.ax) and np.array_equal(a0.ay, a1.ay)
+    assert not np.array_equal(a0.ax, a2.ax)
+    idx = np.arange(0, n, 6)
+    ex, ey = oracle.n2_sampled(ob.x, ob.y, ob.mass, eps, idx)
+    def med(bb):
+        return np.median(np.hypot(bb.ax[idx] - ex, bb.ay[idx] - ey) / np.hypot(ex, ey))
+    assert med(a2) <= 1.15 * med(a0) + 1e-8, (med(a2), med(a0))
+    # a moved body is at least R_a / theta_b from the target leaf's COM (up to the FP32
+    # rounding of the test)
+    nl = t.n_leaves
+    moved = 0
+    for a in range(0, nl, 7):
+        for q in range(p2p.off[a], p2p.off[a + 1]):
+            s = p2p.idx[q]
+            if s == a:
+                continue
+            for j in range(t.body_start[s], t.body_end[s]):
+                if oracle.body_p2l(ob, t, R, a, s, j, 0.3):
+                    moved += 1
+                    d = np.hypot(ob.x[j] - t.comx[a], ob.y[j] - t.comy[a])
+                    assert d * 0.3 > R[a] * (1 - 1e-6)
+    assert moved > 0
