@@ -1688,7 +1688,7 @@ __global__ void k_p2l_units_fill(int64_t nl, const int64_t *start, const int32_t
 // difference rounded once), then per P2P row (a <- s), s != a, the bit set of s's bodies
 // with |o_j + (com_s - com_a)|^2 theta_b^2 > R_a^2, in separately rounded FP32 operations
 // (o_j and the leaf-pair shift each rounded once from FP64), so that the oracle decides
-// every body alike.  A warp per P2P item, a lane per body of each row in turn.
+// every body alike.
 __global__ void k_body_off32(int64_t nl, const double *x, const double *y, const double *comx, const double *comy,
                              const int32_t *bs, const int32_t *be, float2 *off) {
     const int64_t L = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1707,36 +1707,48 @@ __global__ void __launch_bounds__(128) k_body_masks(int64_t n_items, const int32
                                                     const int32_t *__restrict__ bs, const int32_t *__restrict__ be,
                                                     const float *__restrict__ R32, const float2 *__restrict__ off,
                                                     float tb2, uint32_t *__restrict__ mask) {
+    // a warp per P2P item: lane k stages row k (first body, body count or 0 for the self
+    // row, the FP32 shift) in shared memory, then the warp takes the rows eight at a time,
+    // a lane per body, the eight rows' loads in flight together
+    __shared__ __align__(16) int4 rmeta[4][32];
     const unsigned full = 0xffffffffu;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
     if (it >= n_items) return;
     const int nq = item_nq[it];
     if (nq <= 0) return;  // an M2P item
     const int32_t a = item_leaf[it];
     const int64_t qb = item_qb[it];
-    int32_t s = -1, b0 = 0, b1 = 0;
-    float shx = 0.f, shy = 0.f;
     if (lane < nq) {
-        s = near_idx[qb + lane];
-        b0 = bs[s];
-        b1 = be[s];
-        shx = __double2float_rn(__dsub_rn(comx[s], comx[a]));
-        shy = __double2float_rn(__dsub_rn(comy[s], comy[a]));
+        const int32_t s = near_idx[qb + lane];
+        const int32_t b0 = bs[s], ns = s == a ? 0 : be[s] - b0;
+        const float hx = __double2float_rn(__dsub_rn(comx[s], comx[a]));
+        const float hy = __double2float_rn(__dsub_rn(comy[s], comy[a]));
+        rmeta[w][lane] = make_int4(b0, ns, __float_as_int(hx), __float_as_int(hy));
     }
+    __syncwarp();
     const float ra = R32[a], ra2 = __fmul_rn(ra, ra);
-    for (int k = 0; k < nq; k++) {
-        const int32_t sk = __shfl_sync(full, s, k), j0 = __shfl_sync(full, b0, k), j1 = __shfl_sync(full, b1, k);
-        const float hx = __shfl_sync(full, shx, k), hy = __shfl_sync(full, shy, k);
-        bool far = false;
-        if (sk != a && j0 + lane < j1) {
-            const float2 o = off[j0 + lane];
-            const float ex = __fadd_rn(o.x, hx), ey = __fadd_rn(o.y, hy);
-            const float d2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
-            far = __fmul_rn(d2, tb2) > ra2;
+    constexpr int G = 8;
+    for (int k0 = 0; k0 < nq; k0 += G) {
+        float2 o[G];
+        bool live[G];
+        float hx[G], hy[G];
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            const int k = k0 + g;
+            const int4 r = rmeta[w][k & 31];
+            live[g] = k < nq && lane < r.y;
+            hx[g] = __int_as_float(r.z);
+            hy[g] = __int_as_float(r.w);
+            o[g] = live[g] ? off[r.x + lane] : make_float2(0.f, 0.f);
         }
-        const unsigned m = __ballot_sync(full, far);
-        if (lane == 0) mask[qb + k] = m;
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            const float ex = __fadd_rn(o[g].x, hx[g]), ey = __fadd_rn(o[g].y, hy[g]);
+            const float d2 = __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ey, ey));
+            const unsigned m = __ballot_sync(full, live[g] && __fmul_rn(d2, tb2) > ra2);
+            if (lane == 0 && k0 + g < nq) mask[qb + k0 + g] = m;
+        }
     }
 }
 
@@ -1900,9 +1912,13 @@ int gx_plan_items(gx_ctx *ctx, bool accurate) {
         split ? dptr<int64_t>(ctx->m2p_off) : nullptr, split ? dptr<int32_t>(ctx->m2p_list) : nullptr);
     ctx->launches += 2;
     I.n = tot[0];
-    ctx->n_m2p_items = split ? tot[3] : 0;
-    PU.n = PU.n_leafu = PU.n_body = 0;
-    ctx->n_m2p_pairs = ctx->n_p2l_pairs = 0;
+    if (accurate) {
+        // the near-list split's state belongs to the ACCURATE plan: a REF plan made in
+        // between (its own items) leaves it as it is
+        ctx->n_m2p_items = split ? tot[3] : 0;
+        PU.n = PU.n_leafu = PU.n_body = 0;
+        ctx->n_m2p_pairs = ctx->n_p2l_pairs = 0;
+    }
     if (split) {
         ctx->n_near_pairs = (int64_t)stot[0];
         ctx->n_m2p_pairs = (int64_t)stot[1];
