@@ -1256,12 +1256,13 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_rows(int64_t n_items, const in
 
 // The near field of k_p2p32_rows with the body-level P2L (leaves of at most 32 bodies):
 // row k of an item keeps the bodies of its source leaf outside the plan's mask (the
-// masked ones went to the target leaf's local expansion).  The self row runs first, as
-// the scalar own row of k_p2p32_rows; the other rows' kept bodies are laid out as one
-// stream per item in shared memory (entry (row << 5) | body, in row and body order) and
-// computed 32 at a time with the packed quads of k_p2p32_rows, the last chunk padded with
-// zero-mass sources far away (r^-3 underflows to 0).  With empty masks the stream is
-// every body of every row, so the same kernel serves the plain split.
+// masked ones went to the target leaf's local expansion).  The rows' kept bodies are laid
+// out as one stream per item in shared memory (entry (row << 5) | body, in row and body
+// order) and computed 32 at a time with the packed quads of k_p2p32_rows, the last chunk
+// padded with zero-mass sources far away (r^-3 underflows to 0).  The self row is in the
+// stream when eps > 0 (each body's term on itself is exactly 0); with eps = 0 it runs
+// first, as the scalar own row of k_p2p32_rows.  With empty masks the stream is every body
+// of every row, so the same kernel serves the plain split.
 __global__ void __launch_bounds__(128, 8) k_p2p32_stream(
     int64_t n_items, const int32_t *__restrict__ item_leaf, const int64_t *__restrict__ item_qb,
     const int32_t *__restrict__ item_nq, const float4 *__restrict__ pos, const double *__restrict__ comx,
@@ -1277,6 +1278,7 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_stream(
     const int half = lane >> 4, tl = lane & 15;  // lane: targets tl and tl + 16, source quads of its half
     const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
     const float4 far4 = make_float4(1e18f, 1e18f, 0.f, 0.f);
+    const bool self_in_stream = eps2 > 0.f;
     for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n_items; it += nwarps) {
         const int32_t leaf = item_leaf[it];
         const int nq = item_nq[it];
@@ -1295,10 +1297,12 @@ __global__ void __launch_bounds__(128, 8) k_p2p32_stream(
             own_lane = sl == leaf;
             const int ns = b1 - b0;
             const uint32_t all = ns >= 32 ? full : ((1u << ns) - 1u);
-            keep = own_lane ? 0u : (all & ~p2p_mask[q]);
+            // with eps > 0 the self row joins the stream: a body against itself has
+            // dx = dy = 0 exactly and adds fq * 0 = 0 (its mask is 0)
+            keep = (own_lane && !self_in_stream) ? 0u : (all & ~p2p_mask[q]);
         }
         const unsigned ownm = __ballot_sync(full, own_lane);
-        const int kown = ownm ? __ffs(ownm) - 1 : -1;
+        const int kown = (ownm && !self_in_stream) ? __ffs(ownm) - 1 : -1;
         // exclusive scan of the rows' kept counts; T = the stream's length
         const int c = __popc(keep);
         int incl = c;
@@ -1801,8 +1805,8 @@ __global__ void __launch_bounds__(128, 6) k_p2l_x2(int64_t n_units, const int32_
 }
 
 // Body-level P2L units, mixed form, p <= 5: a unit is up to GX_BODY_UNIT consecutive
-// P2P rows (a <- s) of one target leaf with the plan's masks.  Each lane takes rows lane
-// and lane + 32: it loads the row, and after a warp scan of the rows' mask counts writes
+// P2P rows (a <- s) of one target leaf with the plan's masks.  Each lane takes rows lane,
+// lane + 32, ...: it loads the row, and after a warp scan of the rows' mask counts writes
 // its masked bodies to the unit's stream in shared memory (entry (row << 5) | body, row
 // and body order).  The stream is taken two bodies per lane, 64 at a time (positions
 // c + lane and c + 32 + lane), each with its row's com_a - com_s; a padding slot has zero
@@ -1821,7 +1825,8 @@ __global__ void __launch_bounds__(128, 6) k_p2l_body_x2(int64_t u_base, int64_t 
                                                      const double *__restrict__ comy, const int32_t *__restrict__ bs,
                                                      float eps2, float *__restrict__ Lf, float *__restrict__ ppart) {
     static_assert(P <= 5, "paired accumulators are sized for p <= 5");
-    static_assert(GX_BODY_UNIT == 64, "two rows per lane");
+    static_assert(GX_BODY_UNIT % 32 == 0 && GX_BODY_UNIT * 32 <= 65536, "whole rows per lane, 16-bit entries");
+    constexpr int RPL = GX_BODY_UNIT / 32;  // rows per lane
     constexpr int NC = nc2(P);
     constexpr int NS = row_stride<float>(NC);
     __shared__ __align__(16) float2 rsh[4][GX_BODY_UNIT];  // per row: com_a - com_s in FP32
@@ -1837,9 +1842,10 @@ __global__ void __launch_bounds__(128, 6) k_p2l_body_x2(int64_t u_base, int64_t 
     const int nq = -raw;
     const int32_t a = uleaf[u];
     const double acx = comx[a], acy = comy[a];
-    uint32_t take[2] = {0u, 0u};
+    uint32_t take[RPL];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < RPL; h++) {
+        take[h] = 0u;
         const int r = 32 * h + lane;
         if (r < nq) {
             const int64_t q = ustart[u] + r;
@@ -1849,11 +1855,11 @@ __global__ void __launch_bounds__(128, 6) k_p2l_body_x2(int64_t u_base, int64_t 
             rsh[w][r] = make_float2((float)(acx - comx[sl]), (float)(acy - comy[sl]));
         }
     }
-    // exclusive scan of the 64 rows' counts (rows lane, then rows 32 + lane)
+    // exclusive scan of the rows' counts (rows lane, then rows 32 + lane, ...)
     int base = 0, T = 0;
-    int excl[2];
+    int excl[RPL];
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < RPL; h++) {
         const int c = __popc(take[h]);
         int incl = c;
 #pragma unroll
@@ -1866,7 +1872,7 @@ __global__ void __launch_bounds__(128, 6) k_p2l_body_x2(int64_t u_base, int64_t 
     }
     T = base;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
+    for (int h = 0; h < RPL; h++) {
         uint32_t m = take[h];
         int pp = excl[h];
         const int r = 32 * h + lane;

@@ -293,7 +293,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 __host__ __device__ constexpr int gx_nc(int p) { return (p + 1) * (p + 2) / 2; }
 constexpr int GX_M2L_UNIT = 256;  // far sources per M2L work unit (8 rounds of a warp)
 constexpr int GX_P2L_UNIT = 32;   // source leaves per P2L work unit (one per lane)
-constexpr int GX_BODY_UNIT = 64;  // P2P rows per body-level P2L unit (two per lane)
+constexpr int GX_BODY_UNIT = 96;  // P2P rows per body-level P2L unit (three per lane)
 __host__ __device__ constexpr int gx_mi(int i, int j) { return (i + j) * (i + j + 1) / 2 + j; }
 __host__ __device__ constexpr int gx_kdi(int k, int l, int p) { return (k + l) * (2 * p + 1) + l; }
 #endif
