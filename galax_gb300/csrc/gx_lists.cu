@@ -1695,8 +1695,13 @@ __global__ void k_body_off32(int64_t nl, const double *x, const double *y, const
     const int lane = threadIdx.x & 31;
     if (L >= nl) return;
     const double cx = comx[L], cy = comy[L];
-    for (int32_t j = bs[L] + lane; j < be[L]; j += 32)
-        off[j] = make_float2(__double2float_rn(__dsub_rn(x[j], cx)), __double2float_rn(__dsub_rn(y[j], cy)));
+    for (int32_t j = bs[L] + lane; j < be[L]; j += 32) {
+        // the evaluation's sanitising (k_prepare, which runs after the plan: a position
+        // beyond 1e100 or not finite counts as the origin), as the oracle applies it first
+        double xj = x[j], yj = y[j];
+        if (fabs(xj) > 1e100 || fabs(yj) > 1e100 || !isfinite(xj) || !isfinite(yj)) xj = yj = 0.0;
+        off[j] = make_float2(__double2float_rn(__dsub_rn(xj, cx)), __double2float_rn(__dsub_rn(yj, cy)));
+    }
 }
 
 __global__ void __launch_bounds__(128) k_body_masks(int64_t n_items, const int32_t *__restrict__ item_leaf,
