@@ -291,3 +291,28 @@ def test_mixed_form_with_other_leaf_sizes(G, n_max):
     d = rel_vec_err(out[G.PREC_MIXED].ax, out[G.PREC_MIXED].ay, out[G.PREC_FP64].ax, out[G.PREC_FP64].ay)
     assert np.isfinite(d).all()
     assert np.median(d) < 2e-6 and np.percentile(d, 99) < 1e-4
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_mixed_form_at_low_orders(G, p):
+    """The mixed form below p = 4 (the FP32 instantiations for p = 1..3) stays within FP32
+    rounding of the FP64 form on the same tree and lists."""
+    from galax_gb300 import presets
+    n = 30_000
+    b = presets.plummer(n, seed=57)
+    ctx = G.GpuContext(G.GpuConfig(max_n=n, max_nodes=1 << 22, p=p, eps64=0.05))
+    ctx.build_tree(b, 32, presets.BOUNDS["plummer"])
+    ctx.upload_bodies(b)
+    out = {}
+    for prec in (G.PREC_FP64, G.PREC_MIXED):
+        ctx.set_mode(G.MODE_ACCURATE, prec, 0.5)
+        ctx.forces_resident()
+        r = G.Bodies.new(n)
+        ctx.download_bodies(r)
+        out[prec] = r
+    n_far = ctx.plan_info()[0]
+    ctx.close()
+    assert n_far > 0
+    d = rel_vec_err(out[G.PREC_MIXED].ax, out[G.PREC_MIXED].ay, out[G.PREC_FP64].ax, out[G.PREC_FP64].ay)
+    assert np.isfinite(d).all()
+    assert np.median(d) < 2e-6 and np.percentile(d, 99) < 1e-4, (np.median(d), np.percentile(d, 99))
