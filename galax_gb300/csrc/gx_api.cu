@@ -831,6 +831,7 @@ int gx_n2_sampled(gx_ctx *ctx, const int64_t *idx, int64_t n_idx, double *ax, do
 
 int gx_last_timings(gx_ctx *ctx, double out[7]) {
     GX_TRY(check_ctx(ctx));
+    if (!out) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null output");
     for (int k = 0; k < 7; k++) out[k] = ctx->last_ms[k];
     return GX_OK;
 }
@@ -844,6 +845,7 @@ int gx_last_status(gx_ctx *ctx, uint32_t *status) {
 
 int gx_last_launch_count(gx_ctx *ctx, int64_t *count) {
     GX_TRY(check_ctx(ctx));
+    if (!count) return gx_fail(ctx, GX_ERR_INVALID_ARG, "null output");
     *count = ctx->last_launches;
     return GX_OK;
 }

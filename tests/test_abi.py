@@ -68,6 +68,33 @@ def test_invalid_arguments_are_rejected_without_a_device(G):
     assert L.gx_rollout_forward(None, 1, 0.1, 1, 0) == 4
     assert L.gx_rollout_backward(None, *([None] * 10)) == 4
     assert L.gx_last_status(None, None) == 4
+    for f, args in (("gx_set_near_split", (0.4,)), ("gx_set_body_split", (0.3,)), ("gx_set_params", (4, 0.1)),
+                    ("gx_plan_split_info", (None, None)), ("gx_plan_body_split_info", (None, None)),
+                    ("gx_plan_info", (None, None, None)), ("gx_tree_info", (None, None, None, None)),
+                    ("gx_diagnostics", (None,)), ("gx_n2_sampled", (None, 0, None, None)),
+                    ("gx_last_timings", (None,)), ("gx_last_launch_count", (None,)),
+                    ("gx_forces_resident", ())):
+        assert getattr(L, f)(None, *args) == 4, f
+    assert L.gx_destroy(None) == 0  # a null context is nothing to free
+
+
+def test_static_n2_arguments_are_checked_before_any_device_call(G):
+    """gx_n2_sampled_static validates sizes, softening and every sample index on the host
+    before it touches a device: no GPU is needed to see these errors."""
+    L = G.lib()
+    x = np.zeros(8)
+    idx = np.array([0, 3, 8], np.int64)  # 8 is out of range for n = 8
+    ax, ay = np.zeros(3), np.zeros(3)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)
+    pi = idx.ctypes.data_as(C.POINTER(C.c_int64))
+    pd = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    assert L.gx_n2_sampled_static(p(x), p(x), p(x), -1, 0.1, pi, 3, pd(ax), pd(ay), None) == 4
+    assert L.gx_n2_sampled_static(p(x), p(x), p(x), 8, float("nan"), pi, 3, pd(ax), pd(ay), None) == 4
+    assert L.gx_n2_sampled_static(p(x), p(x), p(x), 8, 0.1, pi, 3, pd(ax), pd(ay), None) == 4
+    assert L.gx_n2_sampled_static(p(x), p(x), p(x), 8, 0.1, pi, G.N2_STATIC_MAX_SAMPLES + 1, pd(ax), pd(ay),
+                                  None) == 6
+    assert L.gx_n2_sampled_static(None, None, None, 8, 0.1, None, 0, None, None, None) == 0
+    assert L.gx_n2_sampled_static(None, p(x), p(x), 8, 0.1, pi, 2, pd(ax), pd(ay), None) == 4
 
 
 def test_no_device_reports_init_failure(G):
