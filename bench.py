@@ -23,7 +23,8 @@ adjoint/forward time of reverse-mode rollouts.
              *_alone keys time it again started after that chain
   cpu_baseline  the oracle (C restatement of galax-core's CPU FMM, REF semantics,
              OpenMP where the reference uses Rayon) on the host cores
-  kdk_steps  leapfrog steps/s, static tree and tree rebuilt every step
+  kdk_steps  leapfrog steps/s, static tree and tree rebuilt every step (the latter
+             also with theta_b = 0: no body-level P2L mask plan per tree)
   uniform_10k  the uniform N=10,000 case: 10 leapfrog steps/s of the REF FP64,
              ACCURATE FP64 and mixed forms, force errors against the exact N^2 sum,
              and the oracle's steps/s and end-state difference (CPU leg)
@@ -702,9 +703,14 @@ def run_ours(args, rank, world, local, pg):
     peak32 = ctx.probe_fp32_tflops()
 
     # whole steps (kick, drift, forces, kick) with the static tree and with the tree
-    # rebuilt on the device before every force evaluation (mixed form, dt = 1e-3)
+    # rebuilt on the device before every force evaluation (mixed form, dt = 1e-3); the
+    # rebuild also without the body-level P2L, whose mask plan is redone for every tree
     steps_cmp = {}
-    for rb in (0, 1):
+    runs = [(0, args.theta_b, "static_tree"), (1, args.theta_b, "rebuild_every_step")]
+    if args.theta_b > 0:
+        runs.append((1, 0.0, "rebuild_every_step_theta_b_0"))
+    for rb, tb, key in runs:
+        ctx.set_body_split(tb)
         ctx.upload_bodies(gb)
         if rb:
             ctx.rebuild_resident(N_MAX, bounds)
@@ -714,8 +720,9 @@ def run_ours(args, rank, world, local, pg):
         t0 = time.perf_counter()
         ctx.kdk_run(args.steps, 1e-3, 0, rebuild_every=rb)
         t_s = (time.perf_counter() - t0) / args.steps
-        steps_cmp["rebuild_every_step" if rb else "static_tree"] = {
-            "ms_per_step": t_s * 1e3, "bodies_per_s": n / t_s, "steps_per_s": 1.0 / t_s}
+        steps_cmp[key] = {"ms_per_step": t_s * 1e3, "bodies_per_s": n / t_s, "steps_per_s": 1.0 / t_s,
+                          "theta_b": tb}
+    ctx.set_body_split(args.theta_b)
     ctx.upload_bodies(gb)
     ctx.rebuild_resident(N_MAX, bounds)  # back to the tree of the starting positions (gb is in its order)
 
