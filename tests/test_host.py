@@ -86,3 +86,15 @@ def test_rollout_loss_partials_match_finite_differences():
     L2 = fdcheck.rollout_loss(x0, y0, xT, yT, R)[0]
     L3 = fdcheck.rollout_loss(x0, y0, xT, yT, R, np.arange(n))[0]
     assert L2 == L3
+
+
+def test_magnitude_error_metric_known_values():
+    """validate_fmm's per-body metric (galax-core/src/lib.rs:1553-1557): the magnitudes
+    are compared, not the vectors, and a zero exact force divides by 1e-20."""
+    from galax_gb300 import _mag_rel_err
+    ax, ay = np.array([3.0, 0.0, 1.0, 0.0]), np.array([4.0, 2.0, 0.0, 1e-30])
+    ex, ey = np.array([0.0, 0.0, 2.0, 0.0]), np.array([5.0, 1.0, 0.0, 0.0])
+    r = _mag_rel_err(ax, ay, ex, ey)
+    assert r[0] == 0.0  # same magnitude, different direction
+    assert r[1] == 1.0 and r[2] == 0.5
+    assert r[3] == 1e-30 / 1e-20
