@@ -168,3 +168,32 @@ def test_body_split_oracle(oracle):
                     d = np.hypot(ob.x[j] - t.comx[a], ob.y[j] - t.comy[a])
                     assert d * 0.3 > R[a] * (1 - 1e-6)
     assert moved > 0
+
+
+@pytest.mark.parametrize("p", [4, 8])
+def test_near_split_oracle_converges_like_the_unsplit_form(oracle, p):
+    """The oracle's M2P and P2L (gxo_compute_fmm_force_wx) against the exact sum: at each
+    order the split's error stays within 1.5x of the unsplit ACCURATE form's, and both
+    fall with p (a wrong M2P or P2L formula would leave an error of the size of the moved
+    interactions, independent of p)."""
+    n = 3000
+    b = presets.plummer(n, seed=63)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, 16, presets.BOUNDS["plummer"])
+    eps = oracle.cli_softening(ob)
+    R = oracle.node_radii(ob, t)
+    far, near = oracle.mac_lists_build(t, R, 0.5)
+    p2p, m2p, p2l = oracle.near_split(t, R, 0.4, near)
+    assert m2p.off[-1] > 0 and p2l.off[-1] > 0
+    idx = np.arange(0, n, 3)
+    ex, ey = oracle.n2_sampled(ob.x, ob.y, ob.mass, eps, idx)
+
+    def med(bb):
+        return float(np.median(np.hypot(bb.ax[idx] - ex, bb.ay[idx] - ey) / np.hypot(ex, ey)))
+
+    a0, a1 = ob.copy(), ob.copy()
+    oracle.compute_fmm_force_mac(a0, t, far, near, p, eps)
+    oracle.compute_fmm_force_wx(a1, t, far, p2p, m2p, p2l, p, eps)
+    e0, e1 = med(a0), med(a1)
+    assert e1 <= 1.5 * e0 + 1e-12, (e1, e0)
+    assert e1 < (1e-4 if p == 4 else 1e-6), e1  # 6.4e-5 and 3.1e-7 here
