@@ -197,3 +197,31 @@ def test_near_split_oracle_converges_like_the_unsplit_form(oracle, p):
     e0, e1 = med(a0), med(a1)
     assert e1 <= 1.5 * e0 + 1e-12, (e1, e0)
     assert e1 < (1e-4 if p == 4 else 1e-6), e1  # 6.4e-5 and 3.1e-7 here
+
+
+@pytest.mark.parametrize("p", [6, 8])
+def test_body_split_oracle_at_high_orders(oracle, p):
+    """The oracle's body-level P2L at p = 6 and 8: the error against the exact sum stays
+    within 1.1x of the near-list split without it (2.4e-6 and 2.2e-7 here), so the moved
+    bodies' expansion is right to high order, not only at p = 4."""
+    n = 6000
+    b = presets.plummer(n, seed=61)
+    ob = oracle.Bodies.from_arrays(b.x, b.y, b.mass)
+    t = oracle.tree_build(ob, 32, presets.BOUNDS["plummer"])
+    eps = oracle.cli_softening(ob)
+    R = oracle.node_radii(ob, t)
+    far, near = oracle.mac_lists_build(t, R, 0.5)
+    p2p, m2p, p2l = oracle.near_split(t, R, 0.4, near)
+    idx = np.arange(0, n, 6)
+    ex, ey = oracle.n2_sampled(ob.x, ob.y, ob.mass, eps, idx)
+
+    def med(bb):
+        return float(np.median(np.hypot(bb.ax[idx] - ex, bb.ay[idx] - ey) / np.hypot(ex, ey)))
+
+    a0, a1 = ob.copy(), ob.copy()
+    oracle.compute_fmm_force_wx(a0, t, far, p2p, m2p, p2l, p, eps)
+    oracle.compute_fmm_force_wxb(a1, t, far, p2p, m2p, p2l, p, eps, R, 0.3)
+    assert not np.array_equal(a0.ax, a1.ax)
+    e0, e1 = med(a0), med(a1)
+    assert e1 <= 1.1 * e0, (e1, e0)
+    assert e1 < (5e-6 if p == 6 else 5e-7), e1
