@@ -125,7 +125,6 @@ int gx_upload_tree(gx_ctx *ctx, int64_t n_nodes, int64_t n_bodies, const double 
  * bounds = {x_min, x_max, y_min, y_max}. */
 int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, double *vy, double *m,
                   double *ax, double *ay, int64_t n_max, const double bounds[4], int flags);
-/* Tree shape of the current tree. */
 /* Tree::build (galax-core/src/lib.rs:163-361) over the RESIDENT bodies: Morton keys,
  * device radix sort, permutation of the seven resident arrays, leaves and parents, with
  * no host round trip -- for a run that rebuilds the tree every step instead of keeping
@@ -134,6 +133,7 @@ int gx_build_tree(gx_ctx *ctx, int64_t n, double *x, double *y, double *vx, doub
  * plans (and, in REF mode, the V/U lists) are rebuilt by the next evaluation.
  * GX_BUILD_BALANCED runs build_constrained (lib.rs:541-694), which does not reorder. */
 int gx_rebuild_resident(gx_ctx *ctx, int64_t n_max, const double bounds[4], int flags, int64_t *perm);
+/* Shape of the current tree (any output may be NULL). */
 int gx_tree_info(gx_ctx *ctx, int64_t *n_nodes, int64_t *n_leaves, int32_t *n_levels, int64_t *n_bodies);
 /* morton_encode (galax-core/src/lib.rs:95-109) of n bodies at once on the device, bit-exact:
  * host x, y in, host keys out; bounds = {x_min, x_max, y_min, y_max}. */
@@ -146,7 +146,8 @@ int gx_export_tree(gx_ctx *ctx, double *cx, double *cy, double *hw, double *mass
                    uint8_t *is_leaf, int64_t *level_start);
 /* Copies a REF list (GX_LIST_V / GX_LIST_U) in the reference layout. */
 int gx_export_lists(gx_ctx *ctx, int which, uint32_t *data, uint8_t *lengths);
-/* Sizes of the lists the current mode uses: far (M2L) pairs and P2P leaf pairs. */
+/* Sizes of the plan of the current mode (built if needed): far (M2L) pairs, near (P2P)
+ * leaf pairs and P2P body-body interactions (any output may be NULL). */
 int gx_plan_info(gx_ctx *ctx, int64_t *n_far_pairs, int64_t *n_near_pairs, int64_t *n_p2p_interactions);
 
 /* GpuContext::step + read_accelerations (galax-gpu/src/lib.rs:464-566): uploads
